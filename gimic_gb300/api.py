@@ -1,0 +1,206 @@
+"""Python host interface of the GB300 GIMIC path.
+
+``Gimic`` mirrors the reference's Cython class (src/libgimic/gimic.pyx:6-57,
+a ``GimicConnector``, src/pygimic/connector.pxd:6-9): ``jvector(r)``,
+``jtensor(r)`` and ``set_property(name, value)`` for one point, plus batched
+evaluation on numpy arrays or CUDA torch tensors and plane integrals.  All
+evaluation runs in libgimic_gb300.so on the GPU.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import GG_PREC_FP64, GG_PREC_SPLIT16, check
+
+try:  # torch is optional: used only to accept device tensors
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+SPINS = ("total", "alpha", "beta", "spindens")
+PRECISIONS = {"fp64": GG_PREC_FP64, "split16": GG_PREC_SPLIT16}
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _is_cuda(t):
+    return torch is not None and isinstance(t, torch.Tensor) and t.is_cuda
+
+
+def au2si(au):
+    """Current in atomic units -> nA/T (src/libgimic/globals.f90 au2si)."""
+    return _lib.load().gg_au2si(float(au))
+
+
+def gauss_data(a, b, order, npts, quadrature="gauss"):
+    """Composite Gauss(-Lobatto) nodes and weights on [0, b - a]
+    (src/libgimic/gaussint.f90:267-319)."""
+    pts = np.zeros(int(npts))
+    wgt = np.zeros(int(npts))
+    rc = _lib.load().gg_gauss_data(float(a), float(b), int(order), int(npts),
+                                   1 if quadrature == "lobatto" else 0, _dptr(pts), _dptr(wgt))
+    if rc != 0:
+        raise ValueError("quadrature: npts=%d is not a multiple of order=%d (or Newton failed)" % (npts, order))
+    return pts, wgt
+
+
+class Gimic:
+    """One molecule with its (perturbed) densities on the current CUDA device.
+
+    Defaults follow gimic_init (src/libgimic/gimic_interface.f90:26-70):
+    closed shell, screening 1e-6, GIAO/diamagnetic/paramagnetic terms on,
+    magnetic field zero until set.
+    """
+
+    def __init__(self, mol, xdens, uhf=False, screening=1e-6, precision="split16"):
+        L = _lib.load()
+        h = C.c_void_p()
+        rc = L.gg_ctx_create(str(mol).encode(), str(xdens).encode(), int(bool(uhf)),
+                             float(screening) if screening else -1.0, C.byref(h))
+        check(rc, None)
+        self._h = h
+        self._L = L
+        self.uhf = bool(uhf)
+        nbf, nat, nsh, tm = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        L.gg_basis_info(h, C.byref(nbf), C.byref(nat), C.byref(nsh), C.byref(tm))
+        self.nbf, self.natoms, self.nshells, self.turbomole = nbf.value, nat.value, nsh.value, bool(tm.value)
+        self.set_precision(precision)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gg_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- settings -------------------------------------------------------
+    def set_precision(self, mode):
+        check(self._L.gg_set_precision(self._h, PRECISIONS[mode] if isinstance(mode, str) else int(mode)), self._h)
+
+    def set_flags(self, giao=True, diamag=True, paramag=True):
+        check(self._L.gg_set_flags(self._h, int(giao), int(diamag), int(paramag)), self._h)
+
+    def set_max_batch(self, n):
+        check(self._L.gg_set_max_batch(self._h, int(n)), self._h)
+
+    def set_uhf(self, onoff):
+        if not isinstance(onoff, int):
+            raise TypeError
+        if bool(onoff) != self.uhf:
+            raise ValueError("open-shell mode is fixed when the context is created (pass uhf=True)")
+
+    def set_magnet(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64).reshape(3)
+        check(self._L.gg_set_magnet(self._h, _dptr(b)), self._h)
+
+    def get_magnet(self):
+        b = np.zeros(3)
+        check(self._L.gg_get_magnet(self._h, _dptr(b)), self._h)
+        return b
+
+    def set_spin(self, spin):
+        if not isinstance(spin, str):
+            raise TypeError
+        check(self._L.gg_set_spin(self._h, spin.encode()), self._h)
+
+    def set_screening(self, thrs):
+        if not isinstance(thrs, float):
+            raise TypeError
+        check(self._L.gg_set_screening(self._h, thrs), self._h)
+
+    def set_property(self, prop, val):
+        """GimicConnector.set_property: dispatches to set_<prop>(val)."""
+        getattr(self, "set_" + prop)(val)
+
+    def atoms(self):
+        xyz = np.zeros((self.natoms, 3))
+        q = np.zeros(self.natoms)
+        check(self._L.gg_atoms(self._h, _dptr(xyz), _dptr(q)), self._h)
+        return xyz, q
+
+    # ---- evaluation -----------------------------------------------------
+    def jtensor_batch(self, points, rho=False, divj=False, stream=None):
+        """Current tensors t(m,b) = dj_m/dB_b at points (N,3), returned as
+        (N,9) column-major (index m + 3b); optionally the density (N,) and
+        the tensor divergence (N,3).  numpy in -> numpy out; CUDA torch
+        tensors in -> CUDA torch tensors out (no host round trip)."""
+        if _is_cuda(points):
+            p = points.to(torch.float64).contiguous().reshape(-1, 3)
+            n = p.shape[0]
+            jt = torch.empty((n, 9), dtype=torch.float64, device=p.device)
+            rh = torch.empty(n, dtype=torch.float64, device=p.device) if rho else None
+            dv = torch.empty((n, 3), dtype=torch.float64, device=p.device) if divj else None
+            st = stream if stream is not None else torch.cuda.current_stream(p.device).cuda_stream
+            rc = self._L.gg_jtensor_batch(self._h, C.c_void_p(p.data_ptr()), n, C.c_void_p(jt.data_ptr()),
+                                          C.c_void_p(rh.data_ptr()) if rh is not None else None,
+                                          C.c_void_p(dv.data_ptr()) if dv is not None else None,
+                                          C.c_void_p(st))
+        else:
+            p = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+            n = p.shape[0]
+            jt = np.zeros((n, 9))
+            rh = np.zeros(n) if rho else None
+            dv = np.zeros((n, 3)) if divj else None
+            rc = self._L.gg_jtensor_batch(self._h, C.c_void_p(p.ctypes.data), n, C.c_void_p(jt.ctypes.data),
+                                          C.c_void_p(rh.ctypes.data) if rh is not None else None,
+                                          C.c_void_p(dv.ctypes.data) if dv is not None else None,
+                                          C.c_void_p(stream) if stream else None)
+        check(rc, self._h)
+        out = [jt]
+        if rho:
+            out.append(rh)
+        if divj:
+            out.append(dv)
+        return out[0] if len(out) == 1 else tuple(out)
+
+    def jvector_batch(self, points, magnet=None):
+        """j = t . B at points (N,3) for the context's (or the given) field."""
+        jt = self.jtensor_batch(points)
+        b = self.get_magnet() if magnet is None else np.asarray(magnet, dtype=np.float64)
+        if _is_cuda(jt):
+            t = jt.reshape(-1, 3, 3).transpose(1, 2)  # t[p, m, b]
+            return t @ torch.as_tensor(b, dtype=torch.float64, device=jt.device)
+        return jt.reshape(-1, 3, 3).transpose(0, 2, 1) @ b
+
+    def jtensor(self, r):
+        """One point, as Gimic.jtensor in gimic.pyx:14-21 (a list of 9)."""
+        return list(self.jtensor_batch(np.asarray(r, dtype=np.float64).reshape(1, 3))[0])
+
+    def jvector(self, r):
+        """One point, as Gimic.jvector in gimic.pyx:23-32 (a list of 3)."""
+        return list(self.jvector_batch(np.asarray(r, dtype=np.float64).reshape(1, 3))[0])
+
+    def plane_integral(self, origin, basv, axes, radius=1e10, stream=None):
+        """Quadrature over the product grid origin + x1 basv[:,0] + x2 basv[:,1]
+        + x3 basv[:,2] with axes = ((x1, w1), (x2, w2), (x3, w3)).  Returns a
+        dict of atomic-unit sums: current (total, positive, negative),
+        modulus (total, positive, negative) and acid (sqrt of the sum), as
+        printed by src/fgimic/integral.f90."""
+        g = _lib.GridSpec()
+        basv = np.asarray(basv, dtype=np.float64)
+        keep = []
+        for c in range(3):
+            g.origin[c] = float(origin[c])
+        for d in range(3):
+            for c in range(3):
+                g.basv[3 * d + c] = float(basv[c, d])
+        for d in range(3):
+            x = np.ascontiguousarray(axes[d][0], dtype=np.float64)
+            w = np.ascontiguousarray(axes[d][1], dtype=np.float64)
+            keep += [x, w]
+            g.npts[d] = len(x)
+            g.pts[d] = _dptr(x)
+            g.wgt[d] = _dptr(w)
+        g.radius = float(radius)
+        out = np.zeros(7)
+        check(self._L.gg_plane_integral(self._h, C.byref(g), _dptr(out), C.c_void_p(stream) if stream else None),
+              self._h)
+        return {"current": tuple(out[0:3]), "modulus": tuple(out[3:6]), "acid": float(np.sqrt(max(out[6], 0.0))),
+                "acid_sum": float(out[6])}

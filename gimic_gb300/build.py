@@ -1,0 +1,76 @@
+"""Builds libgimic_gb300.so from gimic_gb300/csrc with nvcc for sm_103a.
+
+Translation units are compiled in parallel into gimic_gb300/_build/ and
+linked into gimic_gb300/_lib/libgimic_gb300.so (both git-ignored).  The CUDA
+runtime is linked statically; the driver's cuTensorMapEncodeTiled is looked up
+at run time, so the library loads on machines without a GPU.
+"""
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIBDIR = os.path.join(HERE, "_lib")
+LIB = os.path.join(LIBDIR, "libgimic_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+         "-I" + os.path.join(HERE, "..", "include")]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _sources():
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+
+
+def _deps_mtime():
+    files = _sources() + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh"))
+    files.append(os.path.join(HERE, "..", "include", "gimic_gb300.h"))
+    return max(os.path.getmtime(f) for f in files)
+
+
+def build(force=False, verbose=False, extra=()):
+    """Compile and link; returns the library path.  Skips work when the
+    library is newer than every source and header."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime():
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    cc = nvcc()
+
+    def compile_one(src):
+        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        cmd = [cc] + ARCH + FLAGS + list(extra) + ["-c", src, "-o", obj]
+        if src.endswith(".cpp"):
+            cmd = [cc] + FLAGS + list(extra) + ["-x", "c++", "-c", src, "-o", obj]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("nvcc failed on %s:\n%s%s" % (src, res.stdout, res.stderr))
+        if verbose and (res.stdout or res.stderr):
+            sys.stderr.write(res.stdout + res.stderr)
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
+        objs = list(ex.map(compile_one, _sources()))
+    tmp = LIB + ".tmp"
+    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("link failed:\n%s%s" % (res.stdout, res.stderr))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+                extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else ()))

@@ -1,0 +1,746 @@
+// C ABI of libgimic_gb300.so: context management, device tables, dispatch
+// of the FP64 and split-FP16 paths, plane integrals and the
+// reference-compatible gimic_* / mkgausspoints entry points.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gimic_gb300.h"
+#include "gg_host.h"
+#include "gg_kernels.h"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+// Device buffer that grows on demand.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t reserve(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled get_encoder() {
+  static EncodeTiled fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  });
+  return fn;
+}
+
+// 2-D fp16 tensor [rows][cols] (cols contiguous) loaded in boxes of
+// box_rows x 64 with a 128-byte swizzle.
+bool encode_fp16_2d(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+  EncodeTiled enc = get_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {cols, rows};
+  const cuuint64_t strides[1] = {cols * 2};
+  const cuuint32_t box[2] = {64, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int spin_code(const char* s) {
+  if (!s) return -1;
+  if (!std::strcmp(s, "total")) return 0;
+  if (!std::strcmp(s, "alpha")) return 1;
+  if (!std::strcmp(s, "beta")) return 2;
+  if (!std::strcmp(s, "spindens")) return 3;
+  return -1;
+}
+
+}  // namespace
+
+struct gg_ctx {
+  std::mutex mu;
+  std::string err;
+  std::string molfile, xdensfile;
+  gg::Basis basis;
+  gg::Density dens;
+  bool uhf = false;
+  double screening = 1e-8;
+  int spin = 0;
+  double magnet[3] = {0, 0, 0};
+  gg::Flags flags{1, 1, 1};
+  int precision = GG_PREC_SPLIT16;
+  int device = 0;
+  int64_t max_batch = 1 << 20;
+
+  // device basis tables
+  bool tables_ready = false;
+  gg::DevBasis dB{};
+  std::vector<void*> table_allocs;
+
+  // matrices of the current spin case
+  int mats_spin = -1;
+  int mats_prec = -1;
+  DevBuf b_fp64, b_hi, b_lo, inv_col;
+  CUtensorMap tm_b_hi, tm_b_lo;
+
+  // scratch
+  DevBuf a_hi, a_lo, inv_row, pts, jt, rho, divt, jv;
+  DevBuf phi, gx, gy, gz, lap, w64;
+  DevBuf plane_rows, plane_out;
+  int* d_err = nullptr;
+
+  ~gg_ctx() { free_device(); }
+
+  void free_device() {
+    for (void* p : table_allocs) cudaFree(p);
+    table_allocs.clear();
+    tables_ready = false;
+    for (DevBuf* b : {&b_fp64, &b_hi, &b_lo, &inv_col, &a_hi, &a_lo, &inv_row, &pts, &jt, &rho, &divt, &jv, &phi, &gx,
+                      &gy, &gz, &lap, &w64, &plane_rows, &plane_out})
+      b->release();
+    if (d_err) cudaFree(d_err);
+    d_err = nullptr;
+    mats_spin = -1;
+  }
+
+  int fail(int code, const std::string& msg) {
+    err = msg;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? GG_ENOMEM : GG_ECUDA;
+  }
+
+  template <typename T>
+  cudaError_t upload(const std::vector<T>& v, const T** out) {
+    void* p = nullptr;
+    const size_t n = std::max<size_t>(1, v.size()) * sizeof(T);
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) return e;
+    table_allocs.push_back(p);
+    if (!v.empty()) e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    *out = static_cast<const T*>(p);
+    return e;
+  }
+
+  // Shell, primitive and function tables on the device.
+  int build_tables() {
+    if (tables_ready) return GG_OK;
+    for (void* p : table_allocs) cudaFree(p);
+    table_allocs.clear();
+    const gg::Basis& b = basis;
+    std::vector<double> axyz;
+    for (const gg::Atom& a : b.atoms) axyz.insert(axyz.end(), a.coord, a.coord + 3);
+    std::vector<int> f_shell = b.func_shell, f_ijk(b.nbf), sh_atom, sh_prim, sh_npf;
+    std::vector<double> sh_rad2, p_xpd, p_ccd;
+    std::vector<float> p_xp, p_xplo, p_cc;
+    for (int mu = 0; mu < b.nbf; ++mu) {
+      int e[3];
+      gg::component_exponents(b.shells[f_shell[mu]].l, b.func_comp[mu], b.turbomole, e);
+      f_ijk[mu] = e[0] | (e[1] << 4) | (e[2] << 8);
+    }
+    for (const gg::Shell& s : b.shells) {
+      sh_atom.push_back(s.atom);
+      sh_prim.push_back(static_cast<int>(p_xpd.size()));
+      sh_npf.push_back(static_cast<int>(s.xp.size()));
+      sh_rad2.push_back(s.radius * s.radius);
+      for (size_t i = 0; i < s.xp.size(); ++i) {
+        p_xpd.push_back(s.xp[i]);
+        p_ccd.push_back(s.ncc[i]);
+        p_xp.push_back(static_cast<float>(s.xp[i]));
+        p_xplo.push_back(static_cast<float>(s.xp[i] - static_cast<double>(static_cast<float>(s.xp[i]))));
+        p_cc.push_back(static_cast<float>(s.ncc[i]));
+      }
+    }
+    gg::DevBasis d{};
+    d.nbf = b.nbf;
+    d.natoms = static_cast<int>(b.atoms.size());
+    d.nshells = static_cast<int>(b.shells.size());
+    d.kpad = (b.nbf + gg::kBlockK - 1) / gg::kBlockK * gg::kBlockK;
+    d.nchunk = (b.nbf + gg::kChunkF - 1) / gg::kChunkF;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = upload(axyz, &d.atom_xyz);
+    if (e == cudaSuccess) e = upload(f_shell, &d.f_shell);
+    if (e == cudaSuccess) e = upload(f_ijk, &d.f_ijk);
+    if (e == cudaSuccess) e = upload(sh_atom, &d.sh_atom);
+    if (e == cudaSuccess) e = upload(sh_prim, &d.sh_prim);
+    if (e == cudaSuccess) e = upload(sh_npf, &d.sh_npf);
+    if (e == cudaSuccess) e = upload(sh_rad2, &d.sh_rad2);
+    if (e == cudaSuccess) e = upload(p_xp, &d.p_xp);
+    if (e == cudaSuccess) e = upload(p_xplo, &d.p_xplo);
+    if (e == cudaSuccess) e = upload(p_cc, &d.p_cc);
+    if (e == cudaSuccess) e = upload(p_xpd, &d.p_xpd);
+    if (e == cudaSuccess) e = upload(p_ccd, &d.p_ccd);
+    if (e != cudaSuccess) return cuda_fail(e, "uploading basis tables");
+    if (!d_err) {
+      e = cudaMalloc(&d_err, sizeof(int));
+      if (e == cudaSuccess) e = cudaMemset(d_err, 0, sizeof(int));
+      if (e != cudaSuccess) return cuda_fail(e, "allocating error word");
+    }
+    const size_t smem = gg::basis_smem_bytes(d.natoms);
+    if (smem > 48 * 1024) {
+      e = cudaFuncSetAttribute(gg::basis_split_kernel_ptr(), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(smem));
+      if (e != cudaSuccess) return cuda_fail(e, "basis kernel shared memory");
+    }
+    dB = d;
+    tables_ready = true;
+    return GG_OK;
+  }
+
+  // Effective (D, P_x, P_y, P_z) of the spin case, column-major, as ctensor
+  // combines the spin densities (src/libgimic/jtensor.F90:66-103).
+  int spin_density(std::vector<double>* out) {
+    const size_t nn = static_cast<size_t>(basis.nbf) * basis.nbf;
+    const std::vector<double>& a = dens.a;
+    switch (spin) {
+      case 1:
+        *out = a;
+        return GG_OK;
+      case 2:
+        if (!uhf) return fail(GG_EINVAL, "ctensor(): beta current requested, but not open-shell system!");
+        *out = dens.b;
+        return GG_OK;
+      case 0:
+        *out = a;
+        if (uhf)
+          for (size_t i = 0; i < 4 * nn; ++i) (*out)[i] += dens.b[i];
+        return GG_OK;
+      case 3:
+        if (!uhf) return fail(GG_EINVAL, "ctensor(): spindens requested, but not open-shell system!");
+        *out = a;
+        for (size_t i = 0; i < 4 * nn; ++i) (*out)[i] -= dens.b[i];
+        return GG_OK;
+    }
+    return fail(GG_EINVAL, "invalid spin case");
+  }
+
+  // GEMM right-hand side for the spin case: M_0 = D, M_{1+d} = C_d with
+  // C_d[mu,nu] = D[mu,nu] (R_d(nu) - R_d(mu)), M_{4+b} = P_b; the GEMM forms
+  // W[p, nu] = sum_mu phi_p,mu M[mu, nu] (matmul(bf, D) in jtensor.F90:167).
+  int build_matrices() {
+    if (mats_spin == spin && mats_prec == precision) return GG_OK;
+    std::vector<double> dm;
+    int rc = spin_density(&dm);
+    if (rc) return rc;
+    const int n = basis.nbf;
+    const size_t nn = static_cast<size_t>(n) * n;
+    auto M = [&](int m, int mu, int nu) -> double {
+      const size_t ij = mu + static_cast<size_t>(nu) * n;
+      if (m == 0) return dm[ij];
+      if (m >= 4) return dm[(m - 3) * nn + ij];
+      const int d = m - 1;
+      const double* Rn = basis.atoms[basis.func_atom[nu]].coord;
+      const double* Rm = basis.atoms[basis.func_atom[mu]].coord;
+      return dm[ij] * (Rn[d] - Rm[d]);
+    };
+    cudaError_t e;
+    if (precision == GG_PREC_FP64) {
+      std::vector<double> h(static_cast<size_t>(n) * 7 * n);
+      for (int mu = 0; mu < n; ++mu)
+        for (int m = 0; m < 7; ++m)
+          for (int nu = 0; nu < n; ++nu) h[static_cast<size_t>(mu) * 7 * n + m * n + nu] = M(m, mu, nu);
+      e = b_fp64.reserve(h.size() * sizeof(double));
+      if (e == cudaSuccess) e = cudaMemcpy(b_fp64.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return cuda_fail(e, "uploading FP64 matrices");
+    } else {
+      const int kpad = dB.kpad, nchunk = dB.nchunk;
+      const size_t ncol = static_cast<size_t>(nchunk) * gg::kBlockN;
+      std::vector<__half> hi(ncol * kpad, __float2half_rn(0.f)), lo(ncol * kpad, __float2half_rn(0.f));
+      std::vector<float> icol(ncol, 1.f);
+      std::vector<double> col(n);
+      for (int c = 0; c < nchunk; ++c)
+        for (int m = 0; m < 7; ++m)
+          for (int u = 0; u < gg::kChunkF; ++u) {
+            const int nu = c * gg::kChunkF + u;
+            if (nu >= n) continue;
+            const size_t cidx = static_cast<size_t>(c) * gg::kBlockN + m * gg::kChunkF + u;
+            double mx = 0.0;
+            for (int mu = 0; mu < n; ++mu) {
+              col[mu] = M(m, mu, nu);
+              mx = std::max(mx, std::fabs(col[mu]));
+            }
+            int ex = 0;
+            if (mx > 0.0) std::frexp(mx, &ex);
+            if (mx == 0.0 || ex < -100) continue;  // negligible column: keep zeros
+            const double t = std::ldexp(1.0, 14 - ex);
+            icol[cidx] = static_cast<float>(std::ldexp(1.0, ex - 14));
+            for (int mu = 0; mu < n; ++mu) {
+              const double v = col[mu] * t;
+              const __half h = __float2half_rn(static_cast<float>(v));
+              const double resid = v - static_cast<double>(__half2float(h));
+              hi[cidx * kpad + mu] = h;
+              lo[cidx * kpad + mu] = __float2half_rn(static_cast<float>(resid));
+            }
+          }
+      e = b_hi.reserve(hi.size() * sizeof(__half));
+      if (e == cudaSuccess) e = b_lo.reserve(lo.size() * sizeof(__half));
+      if (e == cudaSuccess) e = inv_col.reserve(icol.size() * sizeof(float));
+      if (e == cudaSuccess) e = cudaMemcpy(b_hi.p, hi.data(), hi.size() * sizeof(__half), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(b_lo.p, lo.data(), lo.size() * sizeof(__half), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(inv_col.p, icol.data(), icol.size() * sizeof(float), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return cuda_fail(e, "uploading split matrices");
+      if (!encode_fp16_2d(&tm_b_hi, b_hi.p, ncol, kpad, gg::kBlockN) ||
+          !encode_fp16_2d(&tm_b_lo, b_lo.p, ncol, kpad, gg::kBlockN))
+        return fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the matrix operand");
+    }
+    mats_spin = spin;
+    mats_prec = precision;
+    return GG_OK;
+  }
+
+  int prepare() {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    int rc = build_tables();
+    if (rc) return rc;
+    return build_matrices();
+  }
+
+  // One device-resident batch: pts, outputs all device pointers.
+  int run_batch(const double* d_pts, int64_t n, double* d_jt, double* d_rho, double* d_divt, cudaStream_t st) {
+    if (n <= 0) return GG_OK;
+    if (d_divt && !(flags.giao && flags.dia && flags.para))
+      return fail(GG_EUNSUPPORTED, "div j needs GIAO, diamagnetic and paramagnetic terms on");
+    gg::Outputs out{d_jt, d_rho, d_divt};
+    cudaError_t e;
+    if (precision == GG_PREC_FP64) {
+      const int nb = basis.nbf;
+      const size_t ld = static_cast<size_t>(nb);
+      const size_t b1 = static_cast<size_t>(n) * ld * sizeof(double);
+      for (DevBuf* b : {&phi, &gx, &gy, &gz, &lap}) {
+        e = b->reserve(b1);
+        if (e != cudaSuccess) return cuda_fail(e, "FP64 basis scratch");
+      }
+      e = w64.reserve(static_cast<size_t>(n) * 7 * ld * sizeof(double));
+      if (e != cudaSuccess) return cuda_fail(e, "FP64 GEMM scratch");
+      gg::launch_basis_fp64(dB, d_pts, n, ld, phi.as<double>(), gx.as<double>(), gy.as<double>(), gz.as<double>(),
+                            lap.as<double>(), st);
+      gg::launch_dgemm(phi.as<double>(), ld, b_fp64.as<double>(), 7 * ld, w64.as<double>(), 7 * ld, n, 7 * ld, ld,
+                       st);
+      gg::launch_assemble_fp64(dB, d_pts, n, w64.as<double>(), 7 * ld, phi.as<double>(), gx.as<double>(),
+                               gy.as<double>(), gz.as<double>(), lap.as<double>(), ld, flags, out, st);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return cuda_fail(e, "FP64 path launch");
+      return GG_OK;
+    }
+    const size_t abytes = static_cast<size_t>(n) * dB.kpad * sizeof(__half);
+    e = a_hi.reserve(abytes);
+    if (e == cudaSuccess) e = a_lo.reserve(abytes);
+    if (e == cudaSuccess) e = inv_row.reserve(static_cast<size_t>(n) * sizeof(float));
+    if (e != cudaSuccess) return cuda_fail(e, "split-path scratch");
+    gg::launch_basis_split(dB, d_pts, n, a_hi.as<__half>(), a_lo.as<__half>(), inv_row.as<float>(), st);
+    CUtensorMap tma_hi, tma_lo;
+    if (!encode_fp16_2d(&tma_hi, a_hi.p, n, dB.kpad, gg::kBlockM) ||
+        !encode_fp16_2d(&tma_lo, a_lo.p, n, dB.kpad, gg::kBlockM))
+      return fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
+    gg::TcArgs ta{&tma_hi, &tma_lo, &tm_b_hi, &tm_b_lo, inv_row.as<float>(), inv_col.as<float>(),
+                  d_pts,   n,       flags,    out,      d_err};
+    e = gg::launch_tc_fused(dB, ta, st);
+    if (e != cudaSuccess) return cuda_fail(e, "tensor-core kernel launch");
+    return GG_OK;
+  }
+
+  int check_device_error(cudaStream_t st) {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "device execution");
+    if (d_err) {
+      int h = 0;
+      e = cudaMemcpy(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "reading device error word");
+      if (h != 0) {
+        cudaMemset(d_err, 0, sizeof(int));
+        return fail(GG_ETIMEDOUT, "device pipeline wait gave up (code " + std::to_string(h) + ")");
+      }
+    }
+    return GG_OK;
+  }
+
+  int jtensor(const double* p, int64_t n, double* jto, double* rhoo, double* divo, cudaStream_t st) {
+    if (n < 0 || (n > 0 && !p)) return fail(GG_EINVAL, "bad point array");
+    if (n == 0) return GG_OK;
+    int rc = prepare();
+    if (rc) return rc;
+    const bool dev_in = is_device_ptr(p);
+    const bool dev_out = (!jto || is_device_ptr(jto)) && (!rhoo || is_device_ptr(rhoo)) &&
+                         (!divo || is_device_ptr(divo));
+    const int64_t batch = precision == GG_PREC_FP64 ? std::min<int64_t>(max_batch, 16384) : max_batch;
+    cudaError_t e;
+    for (int64_t off = 0; off < n; off += batch) {
+      const int64_t m = std::min(batch, n - off);
+      const double* dp = p + 3 * off;
+      if (!dev_in) {
+        e = pts.reserve(static_cast<size_t>(m) * 3 * sizeof(double));
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(pts.p, p + 3 * off, static_cast<size_t>(m) * 3 * sizeof(double),
+                              cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(e, "copying points");
+        dp = pts.as<double>();
+      }
+      double *dj = jto ? jto + 9 * off : nullptr, *dr = rhoo ? rhoo + off : nullptr,
+             *dd = divo ? divo + 3 * off : nullptr;
+      if (!dev_out) {
+        if (jto) {
+          if ((e = jt.reserve(static_cast<size_t>(m) * 9 * sizeof(double))) != cudaSuccess)
+            return cuda_fail(e, "output scratch");
+          dj = jt.as<double>();
+        }
+        if (rhoo) {
+          if ((e = rho.reserve(static_cast<size_t>(m) * sizeof(double))) != cudaSuccess)
+            return cuda_fail(e, "output scratch");
+          dr = rho.as<double>();
+        }
+        if (divo) {
+          if ((e = divt.reserve(static_cast<size_t>(m) * 3 * sizeof(double))) != cudaSuccess)
+            return cuda_fail(e, "output scratch");
+          dd = divt.as<double>();
+        }
+      }
+      rc = run_batch(dp, m, dj, dr, dd, st);
+      if (rc) return rc;
+      if (!dev_out) {
+        if (jto) e = cudaMemcpyAsync(jto + 9 * off, dj, m * 9 * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (rhoo && e == cudaSuccess) e = cudaMemcpyAsync(rhoo + off, dr, m * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (divo && e == cudaSuccess)
+          e = cudaMemcpyAsync(divo + 3 * off, dd, m * 3 * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return cuda_fail(e, "copying results");
+        // host staging buffers are reused by the next batch
+        if ((rc = check_device_error(st))) return rc;
+      }
+    }
+    return check_device_error(st);
+  }
+};
+
+extern "C" {
+
+int gg_ctx_create(const char* molfile, const char* xdens, int uhf, double screening, gg_ctx** out) {
+  if (!out) return GG_EINVAL;
+  *out = nullptr;
+  if (!molfile || !xdens) {
+    g_create_error = "gg_ctx_create: null file name";
+    return GG_EINVAL;
+  }
+  gg_ctx* c = new gg_ctx;
+  c->molfile = molfile;
+  c->xdensfile = xdens;
+  c->uhf = uhf != 0;
+  c->screening = screening;
+  std::string e = gg::read_intgrl(molfile, screening, &c->basis);
+  if (e.empty()) e = gg::read_xdens(xdens, c->basis, c->uhf, &c->dens);
+  if (!e.empty()) {
+    g_create_error = e;
+    delete c;
+    return GG_EIO;
+  }
+  cudaGetDevice(&c->device);
+  cudaGetLastError();
+  *out = c;
+  return GG_OK;
+}
+
+int gg_ctx_destroy(gg_ctx* ctx) {
+  if (!ctx) return GG_EINVAL;
+  cudaSetDevice(ctx->device);
+  delete ctx;
+  return GG_OK;
+}
+
+const char* gg_last_error(const gg_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+int gg_set_spin(gg_ctx* ctx, const char* spin) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  const int s = spin_code(spin);
+  if (s < 0) return ctx->fail(GG_EINVAL, "Invalid spin case.");
+  ctx->spin = s;
+  return GG_OK;
+}
+
+int gg_set_magnet(gg_ctx* ctx, const double b[3]) {
+  if (!ctx || !b) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  std::copy(b, b + 3, ctx->magnet);
+  return GG_OK;
+}
+
+int gg_get_magnet(const gg_ctx* ctx, double b[3]) {
+  if (!ctx || !b) return GG_EINVAL;
+  std::copy(ctx->magnet, ctx->magnet + 3, b);
+  return GG_OK;
+}
+
+int gg_set_screening(gg_ctx* ctx, double thrs) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->screening = thrs;
+  gg::set_screening(&ctx->basis, thrs);
+  ctx->tables_ready = false;
+  return GG_OK;
+}
+
+int gg_set_flags(gg_ctx* ctx, int giao, int dia, int para) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (!dia && !para) return ctx->fail(GG_EINVAL, "both diamagnetic and paramagnetic contributions switched off");
+  ctx->flags = gg::Flags{giao != 0, dia != 0, para != 0};
+  return GG_OK;
+}
+
+int gg_set_precision(gg_ctx* ctx, int mode) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (mode != GG_PREC_FP64 && mode != GG_PREC_SPLIT16) return ctx->fail(GG_EINVAL, "unknown precision mode");
+  ctx->precision = mode;
+  return GG_OK;
+}
+
+int gg_set_max_batch(gg_ctx* ctx, int64_t npts) {
+  if (!ctx || npts < 128) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->max_batch = npts;
+  return GG_OK;
+}
+
+int gg_basis_info(const gg_ctx* ctx, int* nbf, int* natoms, int* nshells, int* turbomole) {
+  if (!ctx) return GG_EINVAL;
+  if (nbf) *nbf = ctx->basis.nbf;
+  if (natoms) *natoms = static_cast<int>(ctx->basis.atoms.size());
+  if (nshells) *nshells = static_cast<int>(ctx->basis.shells.size());
+  if (turbomole) *turbomole = ctx->basis.turbomole ? 1 : 0;
+  return GG_OK;
+}
+
+int gg_atoms(const gg_ctx* ctx, double* coords, double* charges) {
+  if (!ctx) return GG_EINVAL;
+  for (size_t a = 0; a < ctx->basis.atoms.size(); ++a) {
+    if (coords)
+      for (int d = 0; d < 3; ++d) coords[3 * a + d] = ctx->basis.atoms[a].coord[d];
+    if (charges) charges[a] = ctx->basis.atoms[a].charge;
+  }
+  return GG_OK;
+}
+
+int gg_jtensor_batch(gg_ctx* ctx, const double* pts, int64_t n, double* jt, double* rho, double* divt, void* stream) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  return ctx->jtensor(pts, n, jt, rho, divt, static_cast<cudaStream_t>(stream));
+}
+
+int gg_jvector_batch(gg_ctx* ctx, const double* pts, int64_t n, double* jv, void* stream) {
+  if (!ctx || !jv) return GG_EINVAL;
+  std::vector<double> t(static_cast<size_t>(std::max<int64_t>(n, 0)) * 9);
+  const bool dev_out = is_device_ptr(jv);
+  if (dev_out) return ctx->fail(GG_EUNSUPPORTED, "gg_jvector_batch writes host memory only");
+  int rc = gg_jtensor_batch(ctx, pts, n, t.data(), nullptr, nullptr, stream);
+  if (rc) return rc;
+  const double* b = ctx->magnet;
+  for (int64_t i = 0; i < n; ++i)
+    for (int m = 0; m < 3; ++m) jv[3 * i + m] = t[9 * i + m] * b[0] + t[9 * i + m + 3] * b[1] + t[9 * i + m + 6] * b[2];
+  return GG_OK;
+}
+
+int gg_plane_integral(gg_ctx* ctx, const gg_grid* grid, double out[7], void* stream) {
+  if (!ctx || !grid || !out) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  const int p1 = grid->npts[0], p2 = grid->npts[1], p3 = grid->npts[2];
+  if (p1 <= 0 || p2 <= 0 || p3 <= 0) return ctx->fail(GG_EINVAL, "empty grid");
+  for (int d = 0; d < 3; ++d)
+    if (!grid->pts[d] || !grid->wgt[d]) return ctx->fail(GG_EINVAL, "missing grid axis");
+  const int64_t n = static_cast<int64_t>(p1) * p2 * p3;
+  // gridpoint (src/fgimic/grid.f90:498-511), i fastest
+  std::vector<double> hp(static_cast<size_t>(n) * 3), hw(static_cast<size_t>(p1 + p2 + p3));
+  for (int k = 0; k < p3; ++k)
+    for (int j = 0; j < p2; ++j)
+      for (int i = 0; i < p1; ++i) {
+        const int64_t idx = i + static_cast<int64_t>(p1) * (j + static_cast<int64_t>(p2) * k);
+        for (int c = 0; c < 3; ++c)
+          hp[3 * idx + c] = grid->origin[c] + grid->pts[0][i] * grid->basv[c] + grid->pts[1][j] * grid->basv[3 + c] +
+                            grid->pts[2][k] * grid->basv[6 + c];
+      }
+  std::copy(grid->wgt[0], grid->wgt[0] + p1, hw.begin());
+  std::copy(grid->wgt[1], grid->wgt[1] + p2, hw.begin() + p1);
+  std::copy(grid->wgt[2], grid->wgt[2] + p3, hw.begin() + p1 + p2);
+  int rc = ctx->prepare();
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = ctx->pts.reserve(hp.size() * sizeof(double));
+  if (e == cudaSuccess) e = ctx->jt.reserve(static_cast<size_t>(n) * 9 * sizeof(double));
+  if (e == cudaSuccess) e = ctx->plane_rows.reserve(static_cast<size_t>(p2) * p3 * 7 * sizeof(double) + hw.size() * sizeof(double));
+  if (e == cudaSuccess) e = ctx->plane_out.reserve(8 * sizeof(double));
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "plane scratch");
+  double* dw = ctx->plane_rows.as<double>() + static_cast<size_t>(p2) * p3 * 7;
+  e = cudaMemcpyAsync(ctx->pts.p, hp.data(), hp.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dw, hw.data(), hw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane points");
+  const int64_t batch = ctx->precision == GG_PREC_FP64 ? std::min<int64_t>(ctx->max_batch, 16384) : ctx->max_batch;
+  for (int64_t off = 0; off < n; off += batch) {
+    const int64_t m = std::min(batch, n - off);
+    rc = ctx->run_batch(ctx->pts.as<double>() + 3 * off, m, ctx->jt.as<double>() + 9 * off, nullptr, nullptr, st);
+    if (rc) return rc;
+  }
+  gg::PlaneArgs pa{};
+  pa.jt = ctx->jt.as<double>();
+  pa.pts = ctx->pts.as<double>();
+  pa.w1 = dw;
+  pa.w2 = dw + p1;
+  pa.w3 = dw + p1 + p2;
+  pa.p1 = p1;
+  pa.p2 = p2;
+  pa.p3 = p3;
+  // grid_center (grid.f90:529-541): midpoint of gridpoint(p1,1,1) and gridpoint(1,p2,1)
+  for (int c = 0; c < 3; ++c) {
+    const double v1 = grid->origin[c] + grid->pts[0][p1 - 1] * grid->basv[c] + grid->pts[1][0] * grid->basv[3 + c] +
+                      grid->pts[2][0] * grid->basv[6 + c];
+    const double v2 = grid->origin[c] + grid->pts[0][0] * grid->basv[c] + grid->pts[1][p2 - 1] * grid->basv[3 + c] +
+                      grid->pts[2][0] * grid->basv[6 + c];
+    pa.center[c] = (v1 + v2) * 0.5;
+    pa.normal[c] = grid->basv[6 + c];
+    pa.bb[c] = ctx->magnet[c];
+  }
+  pa.radius = grid->radius;
+  pa.row_out = ctx->plane_rows.as<double>();
+  pa.out = ctx->plane_out.as<double>();
+  gg::launch_plane_reduce(pa, st);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "plane reduction launch");
+  e = cudaMemcpyAsync(out, pa.out, 7 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane result");
+  return ctx->check_device_error(st);
+}
+
+int gg_gauss_data(double a, double b, int order, int npts, int type, double* pts, double* wgts) {
+  if (!pts || !wgts || npts <= 0 || (type != 0 && type != 1)) return GG_EINVAL;
+  return gg::gauss_data(a, b, order, npts, type, pts, wgts) == 0 ? GG_OK : GG_EINVAL;
+}
+
+double gg_au2si(double au) { return gg::au2si(au); }
+
+// ---------------------------------------------------------------------------
+// Reference-compatible interface (src/libgimic/gimic_interface.f90:26-163)
+// ---------------------------------------------------------------------------
+static gg_ctx* g_ctx = nullptr;
+static int g_uhf = 0;
+static double g_screen = 1e-6;  // SCREEN_THRS, src/libgimic/globals.f90:56
+static double g_magnet[3] = {0, 0, 0};
+
+static void gimic_stop(const std::string& msg) {
+  std::fprintf(stderr, "%s\n", msg.c_str());
+  std::exit(1);
+}
+
+void gimic_init(const char* molfile, const char* densfile) {
+  if (g_ctx) gg_ctx_destroy(g_ctx);
+  g_ctx = nullptr;
+  gg_ctx* c = nullptr;
+  if (gg_ctx_create(molfile, densfile, g_uhf, g_screen, &c) != GG_OK) gimic_stop(gg_last_error(nullptr));
+  g_ctx = c;
+  gg_set_magnet(g_ctx, g_magnet);
+}
+
+void gimic_finalize(void) {
+  if (g_ctx) gg_ctx_destroy(g_ctx);
+  g_ctx = nullptr;
+}
+
+void gimic_set_uhf(int* uhf) {
+  const int u = (uhf && *uhf != 0) ? 1 : 0;
+  if (g_ctx && u != g_uhf) {
+    g_uhf = u;
+    gg_ctx* c = nullptr;
+    if (gg_ctx_create(g_ctx->molfile.c_str(), g_ctx->xdensfile.c_str(), g_uhf, g_screen, &c) != GG_OK)
+      gimic_stop(gg_last_error(nullptr));
+    const int spin = g_ctx->spin;
+    gg_ctx_destroy(g_ctx);
+    g_ctx = c;
+    g_ctx->spin = spin;
+    gg_set_magnet(g_ctx, g_magnet);
+  }
+  g_uhf = u;
+}
+
+void gimic_set_magnet(const double* b) {
+  if (!b) return;
+  std::copy(b, b + 3, g_magnet);
+  if (g_ctx) gg_set_magnet(g_ctx, g_magnet);
+}
+
+void gimic_set_spin(const char* s) {
+  if (spin_code(s) < 0) gimic_stop("Invalid spin case.");
+  if (g_ctx) gg_set_spin(g_ctx, s);
+}
+
+void gimic_set_screening(const double* thrs) {
+  if (thrs) g_screen = *thrs;
+}
+
+void gimic_calc_jtensor(const double* r, double* jt) {
+  if (!g_ctx) gimic_stop("gimic_calc_jtensor(): gimic_init() has not been called");
+  if (gg_jtensor_batch(g_ctx, r, 1, jt, nullptr, nullptr, nullptr) != GG_OK) gimic_stop(gg_last_error(g_ctx));
+}
+
+void gimic_calc_jvector(const double* r, double* jv) {
+  if (!g_ctx) gimic_stop("gimic_calc_jvector(): gimic_init() has not been called");
+  if (gg_jvector_batch(g_ctx, r, 1, jv, nullptr) != GG_OK) gimic_stop(gg_last_error(g_ctx));
+}
+
+void gimic_calc_modj(const double* r, double* mj) {
+  (void)r;
+  (void)mj;
+  gimic_stop("gimic_calc_modj(): NOT IMPLEMENTED YET!");
+}
+
+void gimic_get_gauss_points(double* a, double* b, int* npts, int* order, double* pts, double* wgts) {
+  if (!a || !b || !npts || !order || !pts || !wgts) gimic_stop("gimic_get_gauss_points(): null argument");
+  if (gg::gauss_data(*a, *b, *order, *npts, 0, pts, wgts) != 0)
+    gimic_stop("gaussgrid(): npts is not dividable by ngp!");
+}
+
+void mkgausspoints(double* a, double* b, int* npts, int* order, double* pts, double* wgts) {
+  gimic_get_gauss_points(a, b, npts, order, pts, wgts);
+}
+
+}  // extern "C"

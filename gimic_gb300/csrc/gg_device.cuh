@@ -1,0 +1,232 @@
+// Device-side data layout and sm_103a PTX wrappers (mbarrier, TMA,
+// tcgen05/TMEM) shared by the GB300 GIMIC kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+namespace gg {
+
+// Device copy of the basis.  Function arrays are indexed by the basis
+// function (atom-major order, as in src/libgimic/bfeval.f90:81-122), shell
+// arrays by contraction, primitive arrays by shell.prim .. shell.prim+npf.
+struct DevBasis {
+  int nbf;        // basis functions
+  int natoms;
+  int nshells;
+  int kpad;       // nbf rounded up to a multiple of 64 (GEMM K extent)
+  int nchunk;     // ceil(nbf / 32): 32-function column chunks of the GEMM
+  const double* atom_xyz;  // natoms x 3
+  const int* f_shell;      // shell of each function
+  const int* f_ijk;        // Cartesian exponents packed i | j << 4 | k << 8
+  const int* sh_atom;
+  const int* sh_prim;      // first primitive
+  const int* sh_npf;
+  const double* sh_rad2;   // squared screening radius
+  const float* p_xp;       // primitive exponents (fp32, rounded)
+  const float* p_xplo;     // exponent residuals: p_xpd - p_xp (fp32)
+  const float* p_cc;       // normalised contraction coefficients (fp32)
+  const double* p_xpd;     // same in fp64
+  const double* p_ccd;
+};
+
+// Flags of the tensor assembly (src/libgimic/jtensor.F90:148-237 switches)
+struct Flags {
+  int giao, dia, para;
+};
+
+// Per-point outputs; any pointer may be null.
+struct Outputs {
+  double* jt;    // N x 9, column-major 3x3 (t(m,b) at m + 3b)
+  double* rho;   // N
+  double* divt;  // N x 3: sum_m d/dm t(m,b)
+};
+
+// Split-FP16 GEMM geometry
+constexpr int kChunkF = 32;              // functions per column chunk
+constexpr int kMats = 7;                 // D, C_x, C_y, C_z, P_x, P_y, P_z
+constexpr int kBlockN = kMats * kChunkF; // 224 GEMM columns per chunk
+constexpr int kBlockM = 128;             // points per CTA tile
+constexpr int kBlockK = 64;              // fp16 elements per 128-byte row
+constexpr float kScaleTarget = 16384.0f; // |scaled value| < 2^14
+
+// exp(-alpha r^2) in fp32 with the argument carried as a double-float:
+// alpha = ah + al, r^2 = rh + rl (both splits of fp64 values).  The product
+// error is recovered with an fma and applied to first order, so the result
+// is as accurate as expf itself even for large arguments.
+__device__ __forceinline__ float gauss_df(float ah, float al, float rh, float rl) {
+  const float xh = ah * rh;
+  const float xe = fmaf(ah, rh, -xh);
+  const float xl = xe + fmaf(ah, rl, al * rh);
+  return expf(-xh) * (1.0f - xl);
+}
+
+__device__ __forceinline__ int ipow_exp(int packed, int axis) { return (packed >> (4 * axis)) & 15; }
+
+template <typename T>
+__device__ __forceinline__ T powi(T x, int n) {
+  T r = T(1);
+  for (int i = 0; i < n; ++i) r *= x;
+  return r;
+}
+
+// Value, gradient and Laplacian of one Cartesian component
+// x^i y^j z^k f(r^2) with f1 = sum c e^{-a r^2}, f2 = sum a c e^{-a r^2},
+// f3 = sum a^2 c e^{-a r^2} (gradient as in src/libgimic/caos.f90:39-64).
+template <typename T>
+__device__ __forceinline__ void cart_eval(int packed, T x, T y, T z, T f1, T f2, T f3, T* phi, T* gx, T* gy, T* gz,
+                                          T* lap) {
+  const int i = packed & 15, j = (packed >> 4) & 15, k = (packed >> 8) & 15;
+  const T xi = powi(x, i), yj = powi(y, j), zk = powi(z, k);
+  const T xi1 = i > 0 ? powi(x, i - 1) : T(0);
+  const T yj1 = j > 0 ? powi(y, j - 1) : T(0);
+  const T zk1 = k > 0 ? powi(z, k - 1) : T(0);
+  const T xi2 = i > 1 ? powi(x, i - 2) : T(0);
+  const T yj2 = j > 1 ? powi(y, j - 2) : T(0);
+  const T zk2 = k > 1 ? powi(z, k - 2) : T(0);
+  const T xp1 = xi * x, yp1 = yj * y, zp1 = zk * z;
+  const T yz = yj * zk, xz = xi * zk, xy = xi * yj;
+  *phi = xi * yz * f1;
+  *gx = (T(i) * xi1 * f1 - T(2) * xp1 * f2) * yz;
+  *gy = (T(j) * yj1 * f1 - T(2) * yp1 * f2) * xz;
+  *gz = (T(k) * zk1 * f1 - T(2) * zp1 * f2) * xy;
+  if (lap) {
+    const T r2 = x * x + y * y + z * z;
+    const T second = T(i * (i - 1)) * xi2 * yz + T(j * (j - 1)) * yj2 * xz + T(k * (k - 1)) * zk2 * xy;
+    *lap = second * f1 - T(2 * (2 * (i + j + k) + 3)) * xi * yz * f2 + T(4) * r2 * xi * yz * f3;
+  }
+}
+
+// --------------------------------------------------------------------------
+// PTX wrappers
+// --------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: gives up after ~4 s (or 2^26 polls), or as soon as another
+// thread of the grid has reported an error; sets *err and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (int it = 1; it < (1 << 26); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255) == 0) {
+      if (*reinterpret_cast<volatile int*>(err) != 0) return false;
+      if (global_ns() - t0 > 4000000000ull) break;
+    }
+  }
+  atomicCAS(err, 0, code);
+  return false;
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, uint64_t* bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// D[tmem] (+)= A[smem] * B[smem]^T, fp16 inputs, fp32 accumulate
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// mbarrier arrives once all previously issued MMAs of this thread complete
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// 32 lanes x 32 bit, 8 consecutive columns per thread
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Shared-memory matrix descriptor (tcgen05 format): K-major operand whose
+// rows are 128 bytes, 128-byte swizzle, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc_sw128(const void* tile) {
+  const uint64_t addr = smem_u32(tile);
+  uint64_t d = 0;
+  d |= (addr >> 4) & 0x3FFFull;           // start address
+  d |= (uint64_t)(16 >> 4) << 16;         // leading byte offset (unused with swizzle)
+  d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset
+  d |= 1ull << 46;                        // descriptor version (tcgen05)
+  d |= 2ull << 61;                        // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor: kind::f16, fp16 A/B, fp32 D, K-major A and B.
+__host__ __device__ constexpr uint32_t idesc_f16(int m, int n) {
+  return (1u << 4)                            // D format: f32
+         | (0u << 7) | (0u << 10)             // A, B format: f16
+         | (0u << 15) | (0u << 16)            // A, B K-major
+         | ((uint32_t)(n >> 3) << 17)         // N
+         | ((uint32_t)(m >> 4) << 24);        // M
+}
+
+}  // namespace gg

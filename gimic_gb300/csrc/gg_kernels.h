@@ -1,0 +1,69 @@
+// Kernel launchers of the GB300 GIMIC path (host-callable, stream-ordered).
+#pragma once
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "gg_device.cuh"
+
+namespace gg {
+
+// Number of per-point bilinear forms produced by the contraction; layout:
+//   0 rho = W0.phi           1..3 X_c = W0.(s_c phi)     4..12 E_mc = W0.(s_c g_m)
+//   13..21 Y_dm = WC_d.g_m   22..24 YL_d = WC_d.lap      25..33 Z_bm = Q_b.g_m
+//   34..36 ZL_b = Q_b.lap
+// with W0 = phi^T D, WC_d = phi^T C_d, Q_b = phi^T P_b and s = r - R_atom.
+constexpr int kNDots = 37;
+
+size_t basis_smem_bytes(int natoms);
+const void* basis_split_kernel_ptr();  // for cudaFuncSetAttribute
+void launch_basis_split(const DevBasis& B, const double* pts, int64_t npts, __half* a_hi, __half* a_lo,
+                        float* inv_scale, cudaStream_t st);
+void launch_basis_fp64(const DevBasis& B, const double* pts, int64_t npts, int64_t ld, double* phi, double* gx,
+                       double* gy, double* gz, double* lap, cudaStream_t st);
+
+// C[M][N] = A[M][K] B[K][N], fp64, row-major with leading dimensions.
+void launch_dgemm(const double* A, int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc, int64_t M,
+                  int64_t N, int64_t K, cudaStream_t st);
+
+// Plain FP64 assembly from W = phi^T [D | C_x C_y C_z | P_x P_y P_z]
+// (row stride ldw, block m at column m * nbf) and fp64 basis values.
+void launch_assemble_fp64(const DevBasis& B, const double* pts, int64_t npts, const double* W, int64_t ldw,
+                          const double* phi, const double* gx, const double* gy, const double* gz, const double* lap,
+                          int64_t ld, Flags fl, Outputs out, cudaStream_t st);
+
+// Split-FP16 tensor-core path: TMA maps are opaque 128-byte CUtensorMap blobs.
+struct TcArgs {
+  const void* tmap_a_hi;
+  const void* tmap_a_lo;
+  const void* tmap_b_hi;
+  const void* tmap_b_lo;
+  const float* inv_row_scale;  // per point
+  const float* inv_col_scale;  // [nchunk * 224]
+  const double* pts;
+  int64_t npts;
+  Flags flags;
+  Outputs out;
+  int* err;                    // device error word (0 = ok)
+};
+int tc_smem_bytes();
+cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st);
+
+// Plane reductions over a (p1 x p2 x p3) product grid of tensors jt.
+struct PlaneArgs {
+  const double* jt;      // p1*p2*p3 x 9, i fastest
+  const double* pts;     // same points (for the radius test)
+  const double* w1;
+  const double* w2;
+  const double* w3;
+  int p1, p2, p3;
+  double center[3];
+  double normal[3];
+  double bb[3];
+  double radius;
+  double* row_out;       // p2*p3 x 7 scratch
+  double* out;           // 7: current tot,+,-; modulus tot,+,-; acid sum
+};
+void launch_plane_reduce(const PlaneArgs& a, cudaStream_t st);
+
+}  // namespace gg

@@ -1,0 +1,152 @@
+// Basis-function evaluation on grid points.
+//
+//  * basis_split_kernel: phi at every point in fp32, scaled per point by a
+//    power of two and written as two fp16 pieces (hi + lo) in the row-major
+//    [point][kpad] layout that the tensor-core GEMM loads with TMA.
+//  * basis_fp64_kernel: phi, grad phi and the Laplacian in fp64 for the plain
+//    FP64 path.
+//
+// Both follow src/libgimic/bfeval.f90:81-122 (bfeval), :295-338 (dfdr) with
+// the per-shell screening of src/libgimic/basis.f90:118-136 (a contraction
+// contributes only when |r - R_A| <= its radius; squared distances are
+// compared here).  One warp handles one point; lanes stride over functions so
+// that stores are coalesced.
+#include "gg_device.cuh"
+#include "gg_kernels.h"
+
+namespace gg {
+
+namespace {
+
+constexpr int kWarps = 8;
+
+// Per-warp scratch: relative position of every atom (fp32) and its squared
+// distance (fp64, for the screening test).
+struct AtomScratch {
+  float* s;     // natoms x 4
+  double* d2;   // natoms
+};
+
+__device__ __forceinline__ AtomScratch atom_scratch(int warp, int natoms) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* d2 = reinterpret_cast<double*>(smem_raw) + static_cast<size_t>(warp) * natoms;
+  float* s = reinterpret_cast<float*>(reinterpret_cast<double*>(smem_raw) + static_cast<size_t>(kWarps) * natoms) +
+             static_cast<size_t>(warp) * natoms * 4;
+  return {s, d2};
+}
+
+__device__ __forceinline__ void fill_atoms(const DevBasis& B, const double r[3], AtomScratch sc, int lane) {
+  for (int a = lane; a < B.natoms; a += 32) {
+    const double dx = r[0] - B.atom_xyz[3 * a], dy = r[1] - B.atom_xyz[3 * a + 1], dz = r[2] - B.atom_xyz[3 * a + 2];
+    sc.d2[a] = dx * dx + dy * dy + dz * dz;
+    sc.s[4 * a] = static_cast<float>(dx);
+    sc.s[4 * a + 1] = static_cast<float>(dy);
+    sc.s[4 * a + 2] = static_cast<float>(dz);
+    sc.s[4 * a + 3] = static_cast<float>(sc.d2[a] - static_cast<double>(static_cast<float>(sc.d2[a])));
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ float phi32(const DevBasis& B, AtomScratch sc, int mu) {
+  const int sh = __ldg(B.f_shell + mu);
+  const int a = __ldg(B.sh_atom + sh);
+  if (!(sc.d2[a] <= __ldg(B.sh_rad2 + sh))) return 0.f;
+  const float x = sc.s[4 * a], y = sc.s[4 * a + 1], z = sc.s[4 * a + 2];
+  const float rh = static_cast<float>(sc.d2[a]), rl = sc.s[4 * a + 3];
+  const int p0 = __ldg(B.sh_prim + sh), np = __ldg(B.sh_npf + sh);
+  float f1 = 0.f;
+  for (int p = 0; p < np; ++p)
+    f1 += __ldg(B.p_cc + p0 + p) * gauss_df(__ldg(B.p_xp + p0 + p), __ldg(B.p_xplo + p0 + p), rh, rl);
+  const int ijk = __ldg(B.f_ijk + mu);
+  return powi(x, ijk & 15) * powi(y, (ijk >> 4) & 15) * powi(z, (ijk >> 8) & 15) * f1;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kWarps * 32) basis_split_kernel(DevBasis B, const double* __restrict__ pts,
+                                                                  int64_t npts, __half* __restrict__ a_hi,
+                                                                  __half* __restrict__ a_lo,
+                                                                  float* __restrict__ inv_scale) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t p = static_cast<int64_t>(blockIdx.x) * kWarps + warp;
+  if (p >= npts) return;
+  AtomScratch sc = atom_scratch(warp, B.natoms);
+  const double r[3] = {pts[3 * p], pts[3 * p + 1], pts[3 * p + 2]};
+  fill_atoms(B, r, sc, lane);
+  float vmax = 0.f;
+  for (int mu = lane; mu < B.nbf; mu += 32) vmax = fmaxf(vmax, fabsf(phi32(B, sc, mu)));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+  // scale = 2^(14 - e) with vmax = m 2^e, m in [0.5, 1): scaled values < 2^14
+  float scale = 1.f;
+  if (vmax > 0.f) {
+    int e;
+    frexpf(vmax, &e);
+    scale = ldexpf(1.f, 14 - e);
+  }
+  __half* hi_row = a_hi + p * B.kpad;
+  __half* lo_row = a_lo + p * B.kpad;
+  for (int mu = lane; mu < B.kpad; mu += 32) {
+    const float v = mu < B.nbf ? phi32(B, sc, mu) * scale : 0.f;
+    const __half h = __float2half_rn(v);
+    hi_row[mu] = h;
+    lo_row[mu] = __float2half_rn(v - __half2float(h));
+  }
+  if (lane == 0) inv_scale[p] = 1.f / scale;
+}
+
+__global__ void __launch_bounds__(kWarps * 32) basis_fp64_kernel(DevBasis B, const double* __restrict__ pts,
+                                                                 int64_t npts, int64_t ld, double* __restrict__ phi,
+                                                                 double* __restrict__ gx, double* __restrict__ gy,
+                                                                 double* __restrict__ gz, double* __restrict__ lap) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t p = static_cast<int64_t>(blockIdx.x) * kWarps + warp;
+  if (p >= npts) return;
+  const double r[3] = {pts[3 * p], pts[3 * p + 1], pts[3 * p + 2]};
+  for (int mu = lane; mu < B.nbf; mu += 32) {
+    const int sh = __ldg(B.f_shell + mu);
+    const int a = __ldg(B.sh_atom + sh);
+    const double x = r[0] - B.atom_xyz[3 * a], y = r[1] - B.atom_xyz[3 * a + 1], z = r[2] - B.atom_xyz[3 * a + 2];
+    const double d2 = x * x + y * y + z * z;
+    double v = 0, dx = 0, dy = 0, dz = 0, l2 = 0;
+    if (d2 <= __ldg(B.sh_rad2 + sh)) {
+      const int p0 = __ldg(B.sh_prim + sh), np = __ldg(B.sh_npf + sh);
+      double f1 = 0, f2 = 0, f3 = 0;
+      for (int q = 0; q < np; ++q) {
+        const double al = __ldg(B.p_xpd + p0 + q);
+        const double e = __ldg(B.p_ccd + p0 + q) * exp(-al * d2);
+        f1 += e;
+        f2 += al * e;
+        f3 += al * al * e;
+      }
+      cart_eval<double>(__ldg(B.f_ijk + mu), x, y, z, f1, f2, f3, &v, &dx, &dy, &dz, &l2);
+    }
+    const int64_t o = p * ld + mu;
+    phi[o] = v;
+    gx[o] = dx;
+    gy[o] = dy;
+    gz[o] = dz;
+    lap[o] = l2;
+  }
+}
+
+const void* basis_split_kernel_ptr() { return reinterpret_cast<const void*>(&basis_split_kernel); }
+
+size_t basis_smem_bytes(int natoms) { return static_cast<size_t>(kWarps) * natoms * (sizeof(double) + 4 * sizeof(float)); }
+
+void launch_basis_split(const DevBasis& B, const double* pts, int64_t npts, __half* a_hi, __half* a_lo,
+                        float* inv_scale, cudaStream_t st) {
+  if (npts <= 0) return;
+  const int64_t blocks = (npts + kWarps - 1) / kWarps;
+  basis_split_kernel<<<static_cast<unsigned>(blocks), kWarps * 32, basis_smem_bytes(B.natoms), st>>>(
+      B, pts, npts, a_hi, a_lo, inv_scale);
+}
+
+void launch_basis_fp64(const DevBasis& B, const double* pts, int64_t npts, int64_t ld, double* phi, double* gx,
+                       double* gy, double* gz, double* lap, cudaStream_t st) {
+  if (npts <= 0) return;
+  const int64_t blocks = (npts + kWarps - 1) / kWarps;
+  basis_fp64_kernel<<<static_cast<unsigned>(blocks), kWarps * 32, 0, st>>>(B, pts, npts, ld, phi, gx, gy, gz, lap);
+}
+
+}  // namespace gg

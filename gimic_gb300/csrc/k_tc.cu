@@ -1,0 +1,268 @@
+// Split-FP16 tensor-core contraction with a fused current-tensor epilogue.
+//
+// Per CTA: 128 grid points (GEMM rows).  The GEMM computes, chunk by chunk,
+//     W[p, (m, nu)] = sum_mu phi_p,mu * M_m[mu, nu],   M = D, C_x, C_y, C_z, P_x, P_y, P_z
+// for 32 functions nu at a time (224 columns), as three fp16 tcgen05 MMAs
+// per K step (hi*hi + hi*lo + lo*hi of power-of-two scaled operands) with
+// fp32 accumulation in TMEM.  The two TMEM accumulators alternate between
+// chunks so that the epilogue of chunk c overlaps the MMAs of chunk c+1.
+//
+// Roles (192 threads):
+//   warp 0      TMA producer (A: phi pieces of the tile, B: matrix pieces)
+//   warp 1      TMEM owner and MMA issuer
+//   warps 2..5  epilogue: for its point (one TMEM lane per thread) it
+//               re-evaluates phi, grad phi and the Laplacian of the chunk's 32
+//               functions in fp32 (src/libgimic/caos.f90:17-110 semantics)
+//               and accumulates the kNDots bilinear forms; fp32 within a
+//               chunk, fp64 across chunks; final fp64 combination as in
+//               gg_combine.cuh (src/libgimic/jtensor.F90:148-237).
+#include <cuda.h>
+
+#include "gg_combine.cuh"
+#include "gg_kernels.h"
+
+namespace gg {
+
+namespace {
+constexpr int kStages = 2;
+constexpr int kTileA = kBlockM * kBlockK * 2;          // 16 KiB
+constexpr int kTileB = kBlockN * kBlockK * 2;          // 28 KiB
+constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;   // 88 KiB
+constexpr int kThreads = 192;
+constexpr uint32_t kTmemCols = 512;
+constexpr int kAccStride = 256;
+constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+}  // namespace
+
+int tc_smem_bytes() { return kSmemBytes; }
+
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_fused_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_constant__ CUtensorMap tm_a_lo,
+                    const __grid_constant__ CUtensorMap tm_b_hi, const __grid_constant__ CUtensorMap tm_b_lo,
+                    DevBasis Bs, const float* __restrict__ inv_row, const float* __restrict__ inv_col,
+                    const double* __restrict__ pts, int64_t npts, Flags fl, Outputs out, int* err) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                         ~static_cast<uintptr_t>(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + kStages * kStageBytes);
+  uint64_t* empty = full + kStages;
+  uint64_t* accfull = empty + kStages;
+  uint64_t* accempty = accfull + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accempty + 2);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBlockM;
+  const int nchunk = Bs.nchunk, nkb = Bs.kpad / kBlockK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accfull[b], 1);
+      mbar_init(&accempty[b], 4);
+    }
+    fence_barrier_init();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, kTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0;
+      for (int c = 0; c < nchunk; ++c) {
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int s = it % kStages, round = it / kStages;
+          if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto done;
+          unsigned char* st = base + s * kStageBytes;
+          mbar_expect_tx(&full[s], kStageBytes);
+          tma_load_2d(st, &tm_a_hi, &full[s], kb * kBlockK, static_cast<int>(m0));
+          tma_load_2d(st + kTileA, &tm_a_lo, &full[s], kb * kBlockK, static_cast<int>(m0));
+          tma_load_2d(st + 2 * kTileA, &tm_b_hi, &full[s], kb * kBlockK, c * kBlockN);
+          tma_load_2d(st + 2 * kTileA + kTileB, &tm_b_lo, &full[s], kb * kBlockK, c * kBlockN);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_f16(kBlockM, kBlockN);
+      int it = 0;
+      for (int c = 0; c < nchunk; ++c) {
+        const int b = c & 1, rb = c >> 1;
+        if (!mbar_wait(&accempty[b], (rb & 1) ^ 1, err, 2)) goto done;
+        tc_fence_after();
+        const uint32_t d_tmem = tmem_base + b * kAccStride;
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int s = it % kStages, round = it / kStages;
+          if (!mbar_wait(&full[s], round & 1, err, 3)) goto done;
+          tc_fence_after();
+          unsigned char* st = base + s * kStageBytes;
+          const uint64_t ah = smem_desc_sw128(st), al = smem_desc_sw128(st + kTileA);
+          const uint64_t bh = smem_desc_sw128(st + 2 * kTileA), bl = smem_desc_sw128(st + 2 * kTileA + kTileB);
+#pragma unroll
+          for (int k = 0; k < kBlockK / 16; ++k) {
+            const uint64_t o = static_cast<uint64_t>(k * 32) >> 4;  // 16 fp16 = 32 bytes along K
+            mma_f16(d_tmem, ah + o, bh + o, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+            mma_f16(d_tmem, ah + o, bl + o, idesc, 1u);
+            mma_f16(d_tmem, al + o, bh + o, idesc, 1u);
+          }
+          mma_commit(&empty[s]);
+        }
+        mma_commit(&accfull[b]);
+      }
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const int64_t p = m0 + row;
+    const bool valid = p < npts;
+    double r[3] = {0.0, 0.0, 0.0};
+    float rscale = 0.f;
+    if (valid) {
+      r[0] = pts[3 * p];
+      r[1] = pts[3 * p + 1];
+      r[2] = pts[3 * p + 2];
+      rscale = inv_row[p];
+    }
+    double tot[kNDots];
+#pragma unroll
+    for (int i = 0; i < kNDots; ++i) tot[i] = 0.0;
+    int cur_shell = -1, cur_atom = -1;
+    float sx = 0.f, sy = 0.f, sz = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f, r2h = 0.f, r2l = 0.f;
+    double d2a = 0.0;
+    bool on = false;
+    for (int c = 0; c < nchunk; ++c) {
+      const int b = c & 1, rb = c >> 1;
+      if (!mbar_wait(&accfull[b], rb & 1, err, 4)) break;
+      tc_fence_after();
+      float part[kNDots];
+#pragma unroll
+      for (int i = 0; i < kNDots; ++i) part[i] = 0.f;
+      const uint32_t tbase = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + b * kAccStride;
+#pragma unroll 1
+      for (int sub = 0; sub < kChunkF / 8; ++sub) {
+        float v[kMats][8];
+#pragma unroll
+        for (int m = 0; m < kMats; ++m) tmem_ld8(tbase + m * kChunkF + sub * 8, v[m]);
+        tmem_ld_wait();
+        if (sub == kChunkF / 8 - 1) {
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&accempty[b]);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int mu = c * kChunkF + sub * 8 + u;
+          if (mu < Bs.nbf) {
+            const int sh = __ldg(Bs.f_shell + mu);
+            if (sh != cur_shell) {
+              cur_shell = sh;
+              const int a = __ldg(Bs.sh_atom + sh);
+              if (a != cur_atom) {
+                cur_atom = a;
+                const double dx = r[0] - Bs.atom_xyz[3 * a], dy = r[1] - Bs.atom_xyz[3 * a + 1],
+                             dz = r[2] - Bs.atom_xyz[3 * a + 2];
+                d2a = dx * dx + dy * dy + dz * dz;
+                sx = static_cast<float>(dx);
+                sy = static_cast<float>(dy);
+                sz = static_cast<float>(dz);
+                r2h = static_cast<float>(d2a);
+                r2l = static_cast<float>(d2a - static_cast<double>(r2h));
+              }
+              on = d2a <= __ldg(Bs.sh_rad2 + sh);
+              f1 = f2 = f3 = 0.f;
+              if (on) {
+                const int p0 = __ldg(Bs.sh_prim + sh), np = __ldg(Bs.sh_npf + sh);
+                for (int k = 0; k < np; ++k) {
+                  const float al = __ldg(Bs.p_xp + p0 + k);
+                  const float e = __ldg(Bs.p_cc + p0 + k) * gauss_df(al, __ldg(Bs.p_xplo + p0 + k), r2h, r2l);
+                  f1 += e;
+                  f2 += al * e;
+                  f3 += al * al * e;
+                }
+              }
+            }
+            if (on) {
+              float ph, gx, gy, gz, lp;
+              cart_eval<float>(__ldg(Bs.f_ijk + mu), sx, sy, sz, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
+              const float* cs = inv_col + c * kBlockN + sub * 8 + u;
+              const float w0 = v[0][u] * __ldg(cs);
+              const float wc0 = v[1][u] * __ldg(cs + 1 * kChunkF), wc1 = v[2][u] * __ldg(cs + 2 * kChunkF),
+                          wc2 = v[3][u] * __ldg(cs + 3 * kChunkF);
+              const float q0 = v[4][u] * __ldg(cs + 4 * kChunkF), q1 = v[5][u] * __ldg(cs + 5 * kChunkF),
+                          q2 = v[6][u] * __ldg(cs + 6 * kChunkF);
+              const float wp = w0 * ph;
+              part[0] = fmaf(w0, ph, part[0]);
+              part[1] = fmaf(wp, sx, part[1]);
+              part[2] = fmaf(wp, sy, part[2]);
+              part[3] = fmaf(wp, sz, part[3]);
+              const float wx = w0 * sx, wy = w0 * sy, wz = w0 * sz;
+              part[4 + 1] = fmaf(wy, gx, part[4 + 1]);  // E[x][y]
+              part[4 + 2] = fmaf(wz, gx, part[4 + 2]);  // E[x][z]
+              part[4 + 3] = fmaf(wx, gy, part[4 + 3]);  // E[y][x]
+              part[4 + 5] = fmaf(wz, gy, part[4 + 5]);  // E[y][z]
+              part[4 + 6] = fmaf(wx, gz, part[4 + 6]);  // E[z][x]
+              part[4 + 7] = fmaf(wy, gz, part[4 + 7]);  // E[z][y]
+              const float wc[3] = {wc0, wc1, wc2}, qq[3] = {q0, q1, q2}, g[3] = {gx, gy, gz};
+#pragma unroll
+              for (int d = 0; d < 3; ++d) {
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                  part[13 + 3 * d + m] = fmaf(wc[d], g[m], part[13 + 3 * d + m]);
+                  part[25 + 3 * d + m] = fmaf(qq[d], g[m], part[25 + 3 * d + m]);
+                }
+                part[22 + d] = fmaf(wc[d], lp, part[22 + d]);
+                part[34 + d] = fmaf(qq[d], lp, part[34 + d]);
+              }
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kNDots; ++i)
+        if (i != 4 && i != 8 && i != 12) tot[i] += static_cast<double>(part[i]);
+    }
+    if (valid) {
+      const double sc = static_cast<double>(rscale);
+#pragma unroll
+      for (int i = 0; i < kNDots; ++i) tot[i] *= sc;
+      double ct[9], dv[3];
+      combine_point(tot, r, fl, ct, dv);
+      if (out.jt)
+        for (int i = 0; i < 9; ++i) out.jt[9 * p + i] = ct[i];
+      if (out.rho) out.rho[p] = tot[0];
+      if (out.divt)
+        for (int i = 0; i < 3; ++i) out.divt[3 * p + i] = dv[i];
+    }
+  }
+done:
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem_base, kTmemCols);
+  }
+}
+
+cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st) {
+  if (a.npts <= 0) return cudaSuccess;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(tc_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const unsigned grid = static_cast<unsigned>((a.npts + kBlockM - 1) / kBlockM);
+  tc_fused_kernel<<<grid, kThreads, kSmemBytes, st>>>(
+      *static_cast<const CUtensorMap*>(a.tmap_a_hi), *static_cast<const CUtensorMap*>(a.tmap_a_lo),
+      *static_cast<const CUtensorMap*>(a.tmap_b_hi), *static_cast<const CUtensorMap*>(a.tmap_b_lo), B,
+      a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err);
+  return cudaGetLastError();
+}
+
+}  // namespace gg

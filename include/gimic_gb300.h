@@ -1,0 +1,125 @@
+/*
+ * gimic_gb300: C ABI of the GB300 (sm_103a) GIMIC current-density path.
+ *
+ * Two layers are exported from libgimic_gb300.so:
+ *
+ *  1. Drop-in replacements of the reference's own C interface, same names
+ *     and argument meaning:
+ *       - src/libgimic/gimic_interface.h:9-17 (gimic_init ... gimic_calc_modj,
+ *         implemented in src/libgimic/gimic_interface.f90:26-163);
+ *       - src/libgimic/gausspoints.h:10-12 (mkgausspoints,
+ *         gimic_get_gauss_points; src/libgimic/gausspoints.f90:12-29).
+ *     Like the reference they keep one module-global molecule and stop the
+ *     process (exit status 1, message on stderr) on fatal input errors.
+ *
+ *  2. A context API (gg_*) with status codes, batched point evaluation on
+ *     device or host buffers, plane integrals and explicit precision control.
+ *     Every gg_* function returns 0 on success or a negative GG_E* code; the
+ *     message is available from gg_last_error().
+ *
+ * Conventions: coordinates in Bohr; current tensors are 3x3 column-major,
+ * t(m,b) = dj_m/dB_b at index m + 3b (src/libgimic/jtensor.F90:148-237);
+ * currents in atomic units (gg_au2si converts to nA/T).
+ */
+#ifndef GIMIC_GB300_H
+#define GIMIC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- reference-compatible interface --------------------------------------
+ * Replaces src/libgimic/gimic_interface.h:9-17.  r is one point (3 doubles),
+ * jt a 3x3 column-major tensor, jv = jt . B with B from gimic_set_magnet. */
+void gimic_init(const char *molfile, const char *densfile);  /* gimic_interface.f90:26-70 */
+void gimic_finalize(void);                                   /* :72-78 */
+void gimic_set_uhf(int *uhf);                                /* :80-86; reloads XDENS if changed after init */
+void gimic_set_magnet(const double *b);                      /* :88-91 */
+void gimic_set_spin(const char *spin);                       /* :93-114 alpha|beta|total|spindens */
+void gimic_set_screening(const double *thrs);                /* :116-119; used by the next gimic_init */
+void gimic_calc_jtensor(const double *r, double *jt);        /* :121-139 */
+void gimic_calc_jvector(const double *r, double *jv);        /* :141-151 */
+void gimic_calc_modj(const double *r, double *mj);           /* :153-163 (stops: not implemented, as in the reference) */
+
+/* Replaces src/libgimic/gausspoints.h:10-12: composite Gauss-Legendre points
+ * and weights, npts/order panels, placed on [0, b - a] exactly as
+ * setup_gauss_data (src/libgimic/gaussint.f90:267-319) does. */
+void gimic_get_gauss_points(double *a, double *b, int *npts, int *order, double *pts, double *wgts);
+void mkgausspoints(double *a, double *b, int *npts, int *order, double *pts, double *wgts);
+
+/* ---- context API ---------------------------------------------------------- */
+#define GG_OK 0
+#define GG_EINVAL (-1)     /* bad argument */
+#define GG_EIO (-2)        /* input file missing or malformed */
+#define GG_ECUDA (-3)      /* CUDA runtime error (no device, launch failure) */
+#define GG_ENOMEM (-4)     /* device allocation failed */
+#define GG_ETIMEDOUT (-5)  /* a device-side wait gave up (kernel reported an error) */
+#define GG_EUNSUPPORTED (-6)
+
+#define GG_PREC_FP64 0     /* plain FP64 path: SIMT DGEMM + FP64 assembly */
+#define GG_PREC_SPLIT16 1  /* split-FP16 x3 tcgen05 GEMM, FP32 accumulate, FP64 combine (default) */
+
+typedef struct gg_ctx gg_ctx;
+
+/* Reads MOL (INTGRL) and XDENS as gimic_init does (basis.f90:29-86,
+ * dens.f90:56-127); screening <= 0 disables screening.  Uses the current CUDA
+ * device.  On failure *out is NULL and gg_last_error(NULL) has the reason. */
+int gg_ctx_create(const char *molfile, const char *xdens, int uhf, double screening, gg_ctx **out);
+int gg_ctx_destroy(gg_ctx *ctx);
+const char *gg_last_error(const gg_ctx *ctx);
+
+int gg_set_spin(gg_ctx *ctx, const char *spin);            /* alpha|beta|total|spindens */
+int gg_set_magnet(gg_ctx *ctx, const double b[3]);
+int gg_get_magnet(const gg_ctx *ctx, double b[3]);
+int gg_set_screening(gg_ctx *ctx, double thrs);            /* takes effect on the next evaluation */
+int gg_set_flags(gg_ctx *ctx, int giao, int diamag, int paramag);  /* Advanced.GIAO/diamag/paramag */
+int gg_set_precision(gg_ctx *ctx, int mode);               /* GG_PREC_* */
+int gg_set_max_batch(gg_ctx *ctx, int64_t npts);           /* points per device pass (scratch size) */
+
+/* nbf: contracted Cartesian functions; turbomole: 1 if the MOL file has the
+ * TURBOMOLE header (component order gtodefs.f90:108-123). */
+int gg_basis_info(const gg_ctx *ctx, int *nbf, int *natoms, int *nshells, int *turbomole);
+int gg_atoms(const gg_ctx *ctx, double *coords /* natoms x 3 */, double *charges);
+
+/* Current tensors at n points.  pts: n x 3; jt: n x 9 (column-major 3x3);
+ * rho: n (electron density of the selected spin case, or null); divt: n x 3,
+ * divt[b] = sum_m d t(m,b)/d r_m (null to skip; needs GIAO, dia and para on).
+ * Buffers may be host or device memory (not mixed host/device for inputs vs
+ * outputs is fine).  stream: a cudaStream_t or null for the default stream.
+ * Returns after the results are complete. */
+int gg_jtensor_batch(gg_ctx *ctx, const double *pts, int64_t n, double *jt, double *rho, double *divt, void *stream);
+
+/* jv = t . B with B the context's magnetic field (jtensor.F90:125-135). */
+int gg_jvector_batch(gg_ctx *ctx, const double *pts, int64_t n, double *jv, void *stream);
+
+/* Product grid r(i,j,k) = origin + x1_i basv1 + x2_j basv2 + x3_k basv3
+ * (src/fgimic/grid.f90:498-511) with quadrature weights per axis. */
+typedef struct {
+  double origin[3];
+  double basv[9];        /* basv[3*d + c]: component c of axis d; axis 2 is the plane normal */
+  int npts[3];
+  const double *pts[3];  /* host arrays, npts[d] each */
+  const double *wgt[3];
+  double radius;         /* points farther than this from the grid centre get weight 0 */
+} gg_grid;
+
+/* Plane integral (integral.f90:50-186, :190-324, :414-511) with the context's
+ * magnetic field.  out[0..2] current (total, positive, negative), out[3..5]
+ * signed modulus (total, positive, negative), out[6] ACID sum (the reference
+ * prints sqrt(out[6])).  All in atomic units. */
+int gg_plane_integral(gg_ctx *ctx, const gg_grid *grid, double out[7], void *stream);
+
+/* Composite quadrature (gaussint.f90:267-319); type 0 Gauss-Legendre,
+ * 1 Gauss-Lobatto.  Returns GG_EINVAL if npts is not a multiple of order or
+ * the Newton iteration fails. */
+int gg_gauss_data(double a, double b, int order, int npts, int type, double *pts, double *wgts);
+
+double gg_au2si(double au);  /* au -> nA/T (globals.f90 au2si) */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GIMIC_GB300_H */
