@@ -1,0 +1,370 @@
+"""Benchmark of the GB300 GIMIC current-density path.
+
+Workload (the split-precision single-GPU configuration): planar C24H24 ring
+(C-C 1.39 A, C-H 1.09 A) with the seeded random basis (3s2p1d1f on C, 2s1p on
+H, Cartesian: nbf = 720), D from 84 occupied orbitals, dD/dB antisymmetric at
+1e-2 ||D||; current tensor + div j + density on a 128^3 cube of half-width 16
+Bohr (2,097,152 points per step).  Synthetic inputs written in the reference's
+MOL/XDENS formats from a fixed seed.
+
+One step = the whole cube through the split-FP16 tensor-core path with the
+points already in HBM (``value``); ``e2e`` = the same through the C ABI with
+pinned host buffers (host->device copy of the points and device->host copy of
+the tensors, densities and divergences inside the timed region).  Also
+reported: plane-integrals/s for a 60x60 Gauss-Lobatto bond plane, the plain
+FP64 GPU path on a subset, the tensor-core kernel's roofline (from the
+library's own CUDA-event timing on its launch stream) and the FP64 CPU oracle
+on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NBF_NOTE = "C24H24, Cartesian 3s2p1d1f/2s1p, nbf=720"
+WORKLOAD = "c24h24 128^3 cube, jtensor+divj+rho"
+CUBE_N = 128
+CUBE_HALF = 16.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--cpu-sample", type=int, default=8192)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu: 65,536 cube points (a z-slab), two passes")
+    ap.add_argument("--data", default=os.environ.get("GIMIC_GB300_DATA",
+                                                     os.path.join(tempfile.gettempdir(), "gimic_gb300_data")))
+    return ap.parse_args()
+
+
+def flops_per_point(n):
+    # 7 n x n mat-vecs + 28 length-n dots per point (reference jtensor.F90:148-237)
+    return 14 * n * n + 56 * n
+
+
+def cube_points_np():
+    ax = np.linspace(-CUBE_HALF, CUBE_HALF, CUBE_N)
+    x, y, z = np.meshgrid(ax, ax, ax, indexing="ij")
+    return np.stack([x, y, z], -1).reshape(-1, 3)
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(tempfile.gettempdir(), "gg_clocks_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except Exception:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        busy = [s for s in sm if mx and s > 0.3 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+def traffic_per_point():
+    """DRAM bytes per point of the tensor-core kernel from the committed ncu
+    summary (profiles/tc_fused_traffic.json), or None."""
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "tc_fused_traffic.json")))["dram_bytes_per_point"]
+    except Exception:
+        return None
+
+
+def cpu_baseline(mp, xp, sample, seed=7):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    o = oracle.Oracle(mp, xp, screening=1e-8)
+    pts = cube_points_np()
+    idx = np.random.default_rng(seed).choice(len(pts), size=sample, replace=False)
+    cores = os.cpu_count() or 1
+    sub = pts[idx]
+    o.jtensor(sub[:64], nthreads=cores)
+    t = time.perf_counter()
+    o.jtensor(sub, nthreads=cores)
+    dt = time.perf_counter() - t
+    return {"value": sample / dt, "unit": "points/s", "cores": cores, "kind": "port",
+            "sample": "%d random points of the 128^3 cube through the FP64 C oracle (OpenMP, %d threads), %.2f s"
+                      % (sample, cores, dt)}
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference's FP64 algorithm on the host cores.  The
+    reference's Fortran cannot be built here (no gfortran), so the arm times
+    the C restatement in oracle/ with all host threads."""
+    if rank != 0:
+        return
+    from gimic_gb300 import synth
+    mp, xp, mol = synth.make_workload("c24h24", args.data, seed=2024)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    o = oracle.Oracle(mp, xp, screening=1e-8)
+    cores = os.cpu_count() or 1
+    pts = cube_points_np()
+    rng = np.random.default_rng(11)
+    sample = max(256, args.cpu_sample // 4)
+    for _ in range(args.warmup):
+        o.jtensor(pts[rng.choice(len(pts), 256, replace=False)], nthreads=cores)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        o.jtensor(pts[rng.choice(len(pts), sample, replace=False)], nthreads=cores)
+    dt = time.perf_counter() - t
+    v = sample * args.steps / dt
+    n = mol.nbf
+    line = {"impl": "reference", "metric": "jtensor points/s (+ plane-integrals/s)", "value": v,
+            "unit": "points/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded MOL/XDENS in the reference's formats)",
+            "config": {"workload": WORKLOAD, "molecule": NBF_NOTE, "nbf": n, "points_per_step": sample,
+                       "sample": "random subset of the cube per step"},
+            "cpu_baseline": {"value": v, "unit": "points/s", "cores": cores, "kind": "port",
+                             "sample": "%d random cube points per step, FP64 C oracle, %d threads" % (sample, cores)},
+            "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_profile_case(args):
+    """65,536 cube points (every 32nd, so that they span the cube) through the
+    split path twice; the second pass is the one to capture."""
+    import torch
+
+    from gimic_gb300 import api, build, synth
+
+    build.build()
+    mp, xp, mol = synth.make_workload("c24h24", args.data, seed=2024)
+    g = api.Gimic(mp, xp, screening=1e-8, precision="split16")
+    P = torch.as_tensor(cube_points_np()[::32].copy(), device="cuda")
+    for _ in range(2):
+        g.jtensor_batch(P, rho=True, divj=True)
+    torch.cuda.synchronize()
+    print("profile case: %d points, nbf=%d" % (P.shape[0], mol.nbf))
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if args.profile_case:
+        run_profile_case(args)
+        return
+    import torch
+
+    from gimic_gb300 import api, build, synth
+    from gimic_gb300 import grid as ggrid
+    from gimic_gb300 import inp as ginp
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+    build.build()
+    mp, xp, mol = synth.make_workload("c24h24", args.data, seed=2024)
+    n = mol.nbf
+    g = api.Gimic(mp, xp, screening=1e-8, precision="split16")
+    g.set_magnet([0.0, 0.0, 1.0])
+    dev = torch.device("cuda", local)
+    pts_np = cube_points_np()
+    npts = len(pts_np)
+    P = torch.as_tensor(pts_np, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def step():
+        return g.jtensor_batch(P, rho=True, divj=True)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    # ---- device-resident timing ------------------------------------------
+    g.profile(False)  # zero the kernel counter
+    barrier()
+    clocks = Clocks(local)
+    with clocks:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    barrier()
+    launches = g.profile_read()["kernels"]
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = npts * world / (ms * 1e-3)
+
+    # ---- per-kernel timing for the roofline (library CUDA events) -----------
+    g.profile(True)
+    for _ in range(args.steps):
+        step()
+    prof = g.profile_read()
+    g.profile(False)
+    tc_ms, tc_n = prof["tc"]
+    basis_ms, basis_n = prof["basis"]
+    per_launch_pts = npts / (tc_n / args.steps)
+    tc_avg = tc_ms / tc_n
+    alg_tflops = flops_per_point(n) * per_launch_pts / (tc_avg * 1e-3) / 1e12
+    pk = peaks()
+    if pk:
+        peak_tf, peak_src = pk["bf16_tflops_sustained"] / 3.0, "measured sustained bf16/3 (fp16 same rate, 3 products)"
+    else:
+        peak_tf, peak_src = 1700.0 / 3.0, "fallback sustained 1.7 PF/3"
+    tpp = traffic_per_point()
+
+    # ---- end-to-end through the C ABI with pinned host buffers ------------
+    hp = torch.empty((npts, 3), dtype=torch.float64, pin_memory=True)
+    hp.copy_(torch.as_tensor(pts_np))
+    hj = torch.empty((npts, 9), dtype=torch.float64, pin_memory=True)
+    hr = torch.empty(npts, dtype=torch.float64, pin_memory=True)
+    hd = torch.empty((npts, 3), dtype=torch.float64, pin_memory=True)
+    import ctypes as C
+
+    def e2e_step():
+        from gimic_gb300._lib import check
+        rc = g._L.gg_jtensor_batch(g._h, C.c_void_p(hp.data_ptr()), npts, C.c_void_p(hj.data_ptr()),
+                                   C.c_void_p(hr.data_ptr()), C.c_void_p(hd.data_ptr()),
+                                   C.c_void_p(stream.cuda_stream))
+        check(rc, g._h)
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": npts * world / e2e_s, "unit": "points/s", "h2d_bytes_per_step": npts * 3 * 8,
+           "d2h_bytes_per_step": npts * (9 + 1 + 3) * 8, "ms_per_step": e2e_s * 1e3}
+
+    # ---- plane integrals: 60x60 Gauss-Lobatto bond plane -------------------
+    text = ("calc=integral\nmagnet_axis=z\nGrid(bond) {\n type=lobatto\n bond=[1,2]\n fixcoord=[0.0,0.0,0.0]\n"
+            " distance=%.6f\n height=[-8.0, 8.0]\n width=[-4.0, 8.0]\n grid_points=[60, 60, 0]\n"
+            " gauss_order=10\n}\n" % (0.5 * np.linalg.norm(mol.coords[1] - mol.coords[0])))
+    pin = ginp.read(text, is_text=True)
+    grd = ggrid.new_grid(pin, mol.coords)
+    bb, _ = ggrid.get_magnet(grd, pin)
+    g.set_magnet(bb)
+    res = g.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)
+    reps = 20
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        g.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)
+    plane_s = (time.perf_counter() - t0) / reps
+
+    # ---- plain FP64 GPU path on a subset (the 10x reference point) --------
+    g64 = api.Gimic(mp, xp, screening=1e-8, precision="fp64")
+    sub = P[:32768].contiguous()
+    g64.jtensor_batch(sub[:1024])
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    g64.jtensor_batch(sub, rho=True, divj=True)
+    torch.cuda.synchronize(dev)
+    fp64_pts_s = len(sub) / (time.perf_counter() - t0)
+
+    if rank != 0:
+        if dist is not None:
+            dist.barrier()
+        return
+    cpu = cpu_baseline(mp, xp, args.cpu_sample)
+    line = {
+        "metric": "jtensor points/s (+ plane-integrals/s) at <=1e-6 rel err vs FP64",
+        "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16x3/f32/f64",
+        "data": "synthetic (seeded MOL/XDENS in the reference's formats)",
+        "config": {"workload": WORKLOAD, "molecule": NBF_NOTE, "nbf": n, "points_per_step_per_gpu": npts,
+                   "precision": "split-FP16 x3 tcgen05, FP32 accumulate, FP64 combine",
+                   "l2": "inputs larger than L2 (points 50 MB, outputs 218 MB, operand scratch 3.2 GB per pass)",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "plane_integrals_per_s": 1.0 / plane_s,
+        "plane": {"points": int(np.prod(grd.npts)), "type": "60x60 Gauss-Lobatto (order 10), bond plane",
+                  "current_nAT": api.au2si(res["current"][0])},
+        "fp64_gpu_points_per_s": fp64_pts_s,
+        "speedup_vs_fp64_gpu": value / world / fp64_pts_s,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "tensor", "achieved": alg_tflops, "peak": peak_tf, "unit": "TFLOP/s",
+                     "frac": alg_tflops / peak_tf, "peak_source": peak_src,
+                     "traffic": (tpp * per_launch_pts) if tpp else None,
+                     "kernel": "tc_fused_kernel", "launch_ms": tc_avg, "points_per_launch": per_launch_pts,
+                     "algorithmic_flops_per_point": flops_per_point(n),
+                     "basis_kernel_ms": basis_ms / max(1, basis_n)},
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+
+
+if __name__ == "__main__":
+    main()

@@ -52,8 +52,11 @@ SIGNATURES = {
                                    C.c_void_p]),
     "gg_jvector_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "gg_plane_integral": (C.c_int, [C.c_void_p, C.POINTER(GridSpec), _dp, C.c_void_p]),
+    "gg_plane_integrals": (C.c_int, [C.c_void_p, C.POINTER(GridSpec), C.c_int, _dp, C.c_void_p]),
     "gg_gauss_data": (C.c_int, [C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "gg_au2si": (C.c_double, [C.c_double]),
+    "gg_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "gg_profile_read": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
 }
 
 

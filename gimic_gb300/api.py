@@ -125,6 +125,22 @@ class Gimic:
         check(self._L.gg_atoms(self._h, _dptr(xyz), _dptr(q)), self._h)
         return xyz, q
 
+    def profile(self, enable=True):
+        """Start (and zero) or stop per-kernel event timing inside the library."""
+        check(self._L.gg_profile(self._h, int(enable)), self._h)
+
+    def profile_read(self):
+        """{group: (milliseconds, launches)} since profile(True), plus the
+        total number of kernels this context launched."""
+        ms = np.zeros(4)
+        n = (C.c_int64 * 4)()
+        tot = C.c_int64()
+        check(self._L.gg_profile_read(self._h, _dptr(ms), n, C.byref(tot)), self._h)
+        names = ("basis", "tc", "fp64", "plane")
+        out = {k: (float(ms[i]), int(n[i])) for i, k in enumerate(names)}
+        out["kernels"] = int(tot.value)
+        return out
+
     # ---- evaluation -----------------------------------------------------
     def jtensor_batch(self, points, rho=False, divj=False, stream=None):
         """Current tensors t(m,b) = dj_m/dB_b at points (N,3), returned as
@@ -183,24 +199,32 @@ class Gimic:
         dict of atomic-unit sums: current (total, positive, negative),
         modulus (total, positive, negative) and acid (sqrt of the sum), as
         printed by src/fgimic/integral.f90."""
-        g = _lib.GridSpec()
-        basv = np.asarray(basv, dtype=np.float64)
+        return self.plane_integrals([(origin, basv, axes, radius)], stream=stream)[0]
+
+    def plane_integrals(self, planes, stream=None):
+        """Many planes (origin, basv, axes, radius) in one device pass, e.g. a
+        bond-current profile scan; returns one dict per plane."""
+        n = len(planes)
+        specs = (_lib.GridSpec * n)()
         keep = []
-        for c in range(3):
-            g.origin[c] = float(origin[c])
-        for d in range(3):
+        for q, (origin, basv, axes, radius) in enumerate(planes):
+            g = specs[q]
+            basv = np.asarray(basv, dtype=np.float64)
             for c in range(3):
-                g.basv[3 * d + c] = float(basv[c, d])
-        for d in range(3):
-            x = np.ascontiguousarray(axes[d][0], dtype=np.float64)
-            w = np.ascontiguousarray(axes[d][1], dtype=np.float64)
-            keep += [x, w]
-            g.npts[d] = len(x)
-            g.pts[d] = _dptr(x)
-            g.wgt[d] = _dptr(w)
-        g.radius = float(radius)
-        out = np.zeros(7)
-        check(self._L.gg_plane_integral(self._h, C.byref(g), _dptr(out), C.c_void_p(stream) if stream else None),
+                g.origin[c] = float(origin[c])
+            for d in range(3):
+                for c in range(3):
+                    g.basv[3 * d + c] = float(basv[c, d])
+            for d in range(3):
+                x = np.ascontiguousarray(axes[d][0], dtype=np.float64)
+                w = np.ascontiguousarray(axes[d][1], dtype=np.float64)
+                keep += [x, w]
+                g.npts[d] = len(x)
+                g.pts[d] = _dptr(x)
+                g.wgt[d] = _dptr(w)
+            g.radius = float(radius)
+        out = np.zeros((n, 7))
+        check(self._L.gg_plane_integrals(self._h, specs, n, _dptr(out), C.c_void_p(stream) if stream else None),
               self._h)
-        return {"current": tuple(out[0:3]), "modulus": tuple(out[3:6]), "acid": float(np.sqrt(max(out[6], 0.0))),
-                "acid_sum": float(out[6])}
+        return [{"current": tuple(o[0:3]), "modulus": tuple(o[3:6]), "acid": float(np.sqrt(max(o[6], 0.0))),
+                 "acid_sum": float(o[6])} for o in out]

@@ -131,7 +131,51 @@ struct gg_ctx {
   DevBuf plane_rows, plane_out;
   int* d_err = nullptr;
 
-  ~gg_ctx() { free_device(); }
+  // optional per-kernel timing with CUDA events on the launching stream
+  struct Prof {
+    bool on = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
+    std::vector<std::pair<int, size_t>> pending;  // (kernel class, pool index)
+    size_t used = 0;
+    double ms[GG_NPROF] = {0};
+    int64_t launches[GG_NPROF] = {0};
+  } prof;
+
+  void prof_begin(int cls, cudaStream_t st, size_t* slot) {
+    if (!prof.on) return;
+    if (prof.used == prof.pool.size()) {
+      cudaEvent_t a, b;
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      prof.pool.emplace_back(a, b);
+    }
+    *slot = prof.used++;
+    prof.pending.emplace_back(cls, *slot);
+    cudaEventRecord(prof.pool[*slot].first, st);
+  }
+  void prof_end(cudaStream_t st, size_t slot) {
+    if (prof.on) cudaEventRecord(prof.pool[slot].second, st);
+  }
+  void prof_collect() {
+    for (auto& pr : prof.pending) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, prof.pool[pr.second].first, prof.pool[pr.second].second) == cudaSuccess) {
+        prof.ms[pr.first] += t;
+        prof.launches[pr.first] += 1;
+      }
+    }
+    cudaGetLastError();
+    prof.pending.clear();
+    prof.used = 0;
+  }
+
+  ~gg_ctx() {
+    for (auto& e : prof.pool) {
+      cudaEventDestroy(e.first);
+      cudaEventDestroy(e.second);
+    }
+    free_device();
+  }
 
   void free_device() {
     for (void* p : table_allocs) cudaFree(p);
@@ -220,7 +264,7 @@ struct gg_ctx {
       if (e == cudaSuccess) e = cudaMemset(d_err, 0, sizeof(int));
       if (e != cudaSuccess) return cuda_fail(e, "allocating error word");
     }
-    const size_t smem = gg::basis_smem_bytes(d.natoms);
+    const size_t smem = gg::basis_smem_bytes(d.natoms, d.nshells);
     if (smem > 48 * 1024) {
       e = cudaFuncSetAttribute(gg::basis_split_kernel_ptr(), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(smem));
@@ -357,12 +401,16 @@ struct gg_ctx {
       }
       e = w64.reserve(static_cast<size_t>(n) * 7 * ld * sizeof(double));
       if (e != cudaSuccess) return cuda_fail(e, "FP64 GEMM scratch");
+      size_t slot = 0;
+      prof_begin(GG_PROF_FP64, st, &slot);
       gg::launch_basis_fp64(dB, d_pts, n, ld, phi.as<double>(), gx.as<double>(), gy.as<double>(), gz.as<double>(),
                             lap.as<double>(), st);
       gg::launch_dgemm(phi.as<double>(), ld, b_fp64.as<double>(), 7 * ld, w64.as<double>(), 7 * ld, n, 7 * ld, ld,
                        st);
       gg::launch_assemble_fp64(dB, d_pts, n, w64.as<double>(), 7 * ld, phi.as<double>(), gx.as<double>(),
                                gy.as<double>(), gz.as<double>(), lap.as<double>(), ld, flags, out, st);
+      prof_end(st, slot);
+      launches += 3;
       e = cudaGetLastError();
       if (e != cudaSuccess) return cuda_fail(e, "FP64 path launch");
       return GG_OK;
@@ -372,21 +420,30 @@ struct gg_ctx {
     if (e == cudaSuccess) e = a_lo.reserve(abytes);
     if (e == cudaSuccess) e = inv_row.reserve(static_cast<size_t>(n) * sizeof(float));
     if (e != cudaSuccess) return cuda_fail(e, "split-path scratch");
+    size_t slot = 0;
+    prof_begin(GG_PROF_BASIS, st, &slot);
     gg::launch_basis_split(dB, d_pts, n, a_hi.as<__half>(), a_lo.as<__half>(), inv_row.as<float>(), st);
+    prof_end(st, slot);
     CUtensorMap tma_hi, tma_lo;
     if (!encode_fp16_2d(&tma_hi, a_hi.p, n, dB.kpad, gg::kBlockM) ||
         !encode_fp16_2d(&tma_lo, a_lo.p, n, dB.kpad, gg::kBlockM))
       return fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
     gg::TcArgs ta{&tma_hi, &tma_lo, &tm_b_hi, &tm_b_lo, inv_row.as<float>(), inv_col.as<float>(),
                   d_pts,   n,       flags,    out,      d_err};
+    prof_begin(GG_PROF_TC, st, &slot);
     e = gg::launch_tc_fused(dB, ta, st);
+    prof_end(st, slot);
     if (e != cudaSuccess) return cuda_fail(e, "tensor-core kernel launch");
+    launches += 2;
     return GG_OK;
   }
+
+  int64_t launches = 0;  // kernels launched by this context
 
   int check_device_error(cudaStream_t st) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "device execution");
+    prof_collect();
     if (d_err) {
       int h = 0;
       e = cudaMemcpy(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost);
@@ -583,73 +640,125 @@ int gg_jvector_batch(gg_ctx* ctx, const double* pts, int64_t n, double* jv, void
   return GG_OK;
 }
 
-int gg_plane_integral(gg_ctx* ctx, const gg_grid* grid, double out[7], void* stream) {
-  if (!ctx || !grid || !out) return GG_EINVAL;
+int gg_plane_integrals(gg_ctx* ctx, const gg_grid* grids, int nplanes, double* out, void* stream) {
+  if (!ctx || !grids || !out || nplanes <= 0) return GG_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
-  const int p1 = grid->npts[0], p2 = grid->npts[1], p3 = grid->npts[2];
-  if (p1 <= 0 || p2 <= 0 || p3 <= 0) return ctx->fail(GG_EINVAL, "empty grid");
-  for (int d = 0; d < 3; ++d)
-    if (!grid->pts[d] || !grid->wgt[d]) return ctx->fail(GG_EINVAL, "missing grid axis");
-  const int64_t n = static_cast<int64_t>(p1) * p2 * p3;
-  // gridpoint (src/fgimic/grid.f90:498-511), i fastest
-  std::vector<double> hp(static_cast<size_t>(n) * 3), hw(static_cast<size_t>(p1 + p2 + p3));
-  for (int k = 0; k < p3; ++k)
-    for (int j = 0; j < p2; ++j)
-      for (int i = 0; i < p1; ++i) {
-        const int64_t idx = i + static_cast<int64_t>(p1) * (j + static_cast<int64_t>(p2) * k);
-        for (int c = 0; c < 3; ++c)
-          hp[3 * idx + c] = grid->origin[c] + grid->pts[0][i] * grid->basv[c] + grid->pts[1][j] * grid->basv[3 + c] +
-                            grid->pts[2][k] * grid->basv[6 + c];
-      }
-  std::copy(grid->wgt[0], grid->wgt[0] + p1, hw.begin());
-  std::copy(grid->wgt[1], grid->wgt[1] + p2, hw.begin() + p1);
-  std::copy(grid->wgt[2], grid->wgt[2] + p3, hw.begin() + p1 + p2);
+  int64_t npts = 0, nrows = 0, nw = 0;
+  for (int q = 0; q < nplanes; ++q) {
+    const gg_grid& gr = grids[q];
+    if (gr.npts[0] <= 0 || gr.npts[1] <= 0 || gr.npts[2] <= 0) return ctx->fail(GG_EINVAL, "empty grid");
+    for (int d = 0; d < 3; ++d)
+      if (!gr.pts[d] || !gr.wgt[d]) return ctx->fail(GG_EINVAL, "missing grid axis");
+    npts += static_cast<int64_t>(gr.npts[0]) * gr.npts[1] * gr.npts[2];
+    nrows += static_cast<int64_t>(gr.npts[1]) * gr.npts[2];
+    nw += gr.npts[0] + gr.npts[1] + gr.npts[2];
+  }
+  // points r(i,j,k) = origin + x1_i basv1 + x2_j basv2 + x3_k basv3, i fastest
+  // (gridpoint, src/fgimic/grid.f90:498-511); centre as grid_center (:529-541)
+  std::vector<double> hp(static_cast<size_t>(npts) * 3), hw(static_cast<size_t>(nw));
+  std::vector<gg::PlaneDesc> desc(nplanes);
+  std::vector<int> row_plane(static_cast<size_t>(nrows));
+  int64_t po = 0, ro = 0, wo = 0;
+  for (int q = 0; q < nplanes; ++q) {
+    const gg_grid& gr = grids[q];
+    const int p1 = gr.npts[0], p2 = gr.npts[1], p3 = gr.npts[2];
+    for (int k = 0; k < p3; ++k)
+      for (int j = 0; j < p2; ++j)
+        for (int i = 0; i < p1; ++i) {
+          const int64_t idx = po + i + static_cast<int64_t>(p1) * (j + static_cast<int64_t>(p2) * k);
+          for (int c = 0; c < 3; ++c)
+            hp[3 * idx + c] = gr.origin[c] + gr.pts[0][i] * gr.basv[c] + gr.pts[1][j] * gr.basv[3 + c] +
+                              gr.pts[2][k] * gr.basv[6 + c];
+        }
+    std::copy(gr.wgt[0], gr.wgt[0] + p1, hw.begin() + wo);
+    std::copy(gr.wgt[1], gr.wgt[1] + p2, hw.begin() + wo + p1);
+    std::copy(gr.wgt[2], gr.wgt[2] + p3, hw.begin() + wo + p1 + p2);
+    gg::PlaneDesc& d = desc[q];
+    d.pt_off = po;
+    d.row_off = ro;
+    d.p1 = p1;
+    d.p2 = p2;
+    d.p3 = p3;
+    d.w_off = static_cast<int>(wo);
+    for (int c = 0; c < 3; ++c) {
+      const double v1 = gr.origin[c] + gr.pts[0][p1 - 1] * gr.basv[c] + gr.pts[1][0] * gr.basv[3 + c] +
+                        gr.pts[2][0] * gr.basv[6 + c];
+      const double v2 = gr.origin[c] + gr.pts[0][0] * gr.basv[c] + gr.pts[1][p2 - 1] * gr.basv[3 + c] +
+                        gr.pts[2][0] * gr.basv[6 + c];
+      d.center[c] = (v1 + v2) * 0.5;
+      d.normal[c] = gr.basv[6 + c];
+    }
+    d.radius = gr.radius;
+    for (int64_t r = 0; r < static_cast<int64_t>(p2) * p3; ++r) row_plane[ro + r] = q;
+    po += static_cast<int64_t>(p1) * p2 * p3;
+    ro += static_cast<int64_t>(p2) * p3;
+    wo += p1 + p2 + p3;
+  }
   int rc = ctx->prepare();
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t aux = hw.size() * sizeof(double) + desc.size() * sizeof(gg::PlaneDesc) + row_plane.size() * sizeof(int) +
+                     static_cast<size_t>(nrows) * 7 * sizeof(double) + static_cast<size_t>(nplanes) * 7 * sizeof(double) + 64;
   cudaError_t e = ctx->pts.reserve(hp.size() * sizeof(double));
-  if (e == cudaSuccess) e = ctx->jt.reserve(static_cast<size_t>(n) * 9 * sizeof(double));
-  if (e == cudaSuccess) e = ctx->plane_rows.reserve(static_cast<size_t>(p2) * p3 * 7 * sizeof(double) + hw.size() * sizeof(double));
-  if (e == cudaSuccess) e = ctx->plane_out.reserve(8 * sizeof(double));
+  if (e == cudaSuccess) e = ctx->jt.reserve(static_cast<size_t>(npts) * 9 * sizeof(double));
+  if (e == cudaSuccess) e = ctx->plane_rows.reserve(aux);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "plane scratch");
-  double* dw = ctx->plane_rows.as<double>() + static_cast<size_t>(p2) * p3 * 7;
+  char* ab = ctx->plane_rows.as<char>();
+  double* dw = reinterpret_cast<double*>(ab);
+  double* drow = dw + hw.size();
+  double* dout = drow + static_cast<size_t>(nrows) * 7;
+  gg::PlaneDesc* ddesc = reinterpret_cast<gg::PlaneDesc*>(dout + static_cast<size_t>(nplanes) * 7);
+  int* drp = reinterpret_cast<int*>(ddesc + nplanes);
   e = cudaMemcpyAsync(ctx->pts.p, hp.data(), hp.size() * sizeof(double), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dw, hw.data(), hw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ddesc, desc.data(), desc.size() * sizeof(gg::PlaneDesc), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(drp, row_plane.data(), row_plane.size() * sizeof(int), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane points");
   const int64_t batch = ctx->precision == GG_PREC_FP64 ? std::min<int64_t>(ctx->max_batch, 16384) : ctx->max_batch;
-  for (int64_t off = 0; off < n; off += batch) {
-    const int64_t m = std::min(batch, n - off);
+  for (int64_t off = 0; off < npts; off += batch) {
+    const int64_t m = std::min(batch, npts - off);
     rc = ctx->run_batch(ctx->pts.as<double>() + 3 * off, m, ctx->jt.as<double>() + 9 * off, nullptr, nullptr, st);
     if (rc) return rc;
   }
-  gg::PlaneArgs pa{};
-  pa.jt = ctx->jt.as<double>();
-  pa.pts = ctx->pts.as<double>();
-  pa.w1 = dw;
-  pa.w2 = dw + p1;
-  pa.w3 = dw + p1 + p2;
-  pa.p1 = p1;
-  pa.p2 = p2;
-  pa.p3 = p3;
-  // grid_center (grid.f90:529-541): midpoint of gridpoint(p1,1,1) and gridpoint(1,p2,1)
-  for (int c = 0; c < 3; ++c) {
-    const double v1 = grid->origin[c] + grid->pts[0][p1 - 1] * grid->basv[c] + grid->pts[1][0] * grid->basv[3 + c] +
-                      grid->pts[2][0] * grid->basv[6 + c];
-    const double v2 = grid->origin[c] + grid->pts[0][0] * grid->basv[c] + grid->pts[1][p2 - 1] * grid->basv[3 + c] +
-                      grid->pts[2][0] * grid->basv[6 + c];
-    pa.center[c] = (v1 + v2) * 0.5;
-    pa.normal[c] = grid->basv[6 + c];
-    pa.bb[c] = ctx->magnet[c];
-  }
-  pa.radius = grid->radius;
-  pa.row_out = ctx->plane_rows.as<double>();
-  pa.out = ctx->plane_out.as<double>();
-  gg::launch_plane_reduce(pa, st);
+  size_t slot = 0;
+  ctx->prof_begin(GG_PROF_PLANE, st, &slot);
+  gg::launch_plane_batch(ctx->jt.as<double>(), ctx->pts.as<double>(), dw, ddesc, nplanes, drp, nrows, ctx->magnet,
+                         drow, dout, st);
+  ctx->prof_end(st, slot);
+  ctx->launches += 2;
   e = cudaGetLastError();
   if (e != cudaSuccess) return ctx->cuda_fail(e, "plane reduction launch");
-  e = cudaMemcpyAsync(out, pa.out, 7 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  e = cudaMemcpyAsync(out, dout, static_cast<size_t>(nplanes) * 7 * sizeof(double), cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane result");
   return ctx->check_device_error(st);
+}
+
+int gg_plane_integral(gg_ctx* ctx, const gg_grid* grid, double out[7], void* stream) {
+  return gg_plane_integrals(ctx, grid, 1, out, stream);
+}
+
+int gg_profile(gg_ctx* ctx, int enable) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->prof.on = enable != 0;
+  for (int i = 0; i < GG_NPROF; ++i) {
+    ctx->prof.ms[i] = 0.0;
+    ctx->prof.launches[i] = 0;
+  }
+  ctx->launches = 0;
+  return GG_OK;
+}
+
+int gg_profile_read(const gg_ctx* ctx, double ms[GG_NPROF], int64_t launches[GG_NPROF], int64_t* total_kernels) {
+  if (!ctx) return GG_EINVAL;
+  for (int i = 0; i < GG_NPROF; ++i) {
+    if (ms) ms[i] = ctx->prof.ms[i];
+    if (launches) launches[i] = ctx->prof.launches[i];
+  }
+  if (total_kernels) *total_kernels = ctx->launches;
+  return GG_OK;
 }
 
 int gg_gauss_data(double a, double b, int order, int npts, int type, double* pts, double* wgts) {

@@ -15,7 +15,7 @@ namespace gg {
 // with W0 = phi^T D, WC_d = phi^T C_d, Q_b = phi^T P_b and s = r - R_atom.
 constexpr int kNDots = 37;
 
-size_t basis_smem_bytes(int natoms);
+size_t basis_smem_bytes(int natoms, int nshells);
 const void* basis_split_kernel_ptr();  // for cudaFuncSetAttribute
 void launch_basis_split(const DevBasis& B, const double* pts, int64_t npts, __half* a_hi, __half* a_lo,
                         float* inv_scale, cudaStream_t st);
@@ -49,21 +49,19 @@ struct TcArgs {
 int tc_smem_bytes();
 cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st);
 
-// Plane reductions over a (p1 x p2 x p3) product grid of tensors jt.
-struct PlaneArgs {
-  const double* jt;      // p1*p2*p3 x 9, i fastest
-  const double* pts;     // same points (for the radius test)
-  const double* w1;
-  const double* w2;
-  const double* w3;
+// Many planes at once: plane q owns points [pt_off, pt_off + p1*p2*p3) of jt
+// and pts, and weights w[w_off ..] (p1 values, then p2, then p3).
+struct PlaneDesc {
+  int64_t pt_off;
+  int64_t row_off;  // first row of this plane in the flattened row list
   int p1, p2, p3;
+  int w_off;
   double center[3];
   double normal[3];
-  double bb[3];
   double radius;
-  double* row_out;       // p2*p3 x 7 scratch
-  double* out;           // 7: current tot,+,-; modulus tot,+,-; acid sum
 };
-void launch_plane_reduce(const PlaneArgs& a, cudaStream_t st);
+void launch_plane_batch(const double* jt, const double* pts, const double* w, const PlaneDesc* planes, int nplanes,
+                        const int* row_plane, int64_t nrows, const double bb[3], double* row_out, double* out,
+                        cudaStream_t st);
 
 }  // namespace gg

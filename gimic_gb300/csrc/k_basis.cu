@@ -20,61 +20,94 @@ namespace {
 
 constexpr int kWarps = 8;
 
-// Per-warp scratch: relative position of every atom (fp32) and its squared
-// distance (fp64, for the screening test).
+// Per-warp scratch: relative position of every atom (fp32, with the fp32
+// residual of |r - R|^2 in the 4th slot), its squared distance (fp64, for the
+// screening test) and the radial factor sum_p c_p exp(-a_p r^2) of every
+// shell (0 when screened).
 struct AtomScratch {
   float* s;     // natoms x 4
   double* d2;   // natoms
+  float* rad;   // nshells
 };
 
-__device__ __forceinline__ AtomScratch atom_scratch(int warp, int natoms) {
+__device__ __forceinline__ AtomScratch atom_scratch(int warp, int natoms, int nshells) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* d2 = reinterpret_cast<double*>(smem_raw) + static_cast<size_t>(warp) * natoms;
   float* s = reinterpret_cast<float*>(reinterpret_cast<double*>(smem_raw) + static_cast<size_t>(kWarps) * natoms) +
              static_cast<size_t>(warp) * natoms * 4;
-  return {s, d2};
+  float* rad = reinterpret_cast<float*>(reinterpret_cast<double*>(smem_raw) + static_cast<size_t>(kWarps) * natoms) +
+               static_cast<size_t>(kWarps) * natoms * 4 + static_cast<size_t>(warp) * nshells;
+  return {s, d2, rad};
 }
 
 __device__ __forceinline__ void fill_atoms(const DevBasis& B, const double r[3], AtomScratch sc, int lane) {
   for (int a = lane; a < B.natoms; a += 32) {
     const double dx = r[0] - B.atom_xyz[3 * a], dy = r[1] - B.atom_xyz[3 * a + 1], dz = r[2] - B.atom_xyz[3 * a + 2];
-    sc.d2[a] = dx * dx + dy * dy + dz * dz;
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    sc.d2[a] = d2;
     sc.s[4 * a] = static_cast<float>(dx);
     sc.s[4 * a + 1] = static_cast<float>(dy);
     sc.s[4 * a + 2] = static_cast<float>(dz);
-    sc.s[4 * a + 3] = static_cast<float>(sc.d2[a] - static_cast<double>(static_cast<float>(sc.d2[a])));
+    sc.s[4 * a + 3] = static_cast<float>(d2 - static_cast<double>(static_cast<float>(d2)));
+  }
+  __syncwarp();
+  for (int sh = lane; sh < B.nshells; sh += 32) {
+    const int a = __ldg(B.sh_atom + sh);
+    float f1 = 0.f;
+    if (sc.d2[a] <= __ldg(B.sh_rad2 + sh)) {
+      const float rh = static_cast<float>(sc.d2[a]), rl = sc.s[4 * a + 3];
+      const int p0 = __ldg(B.sh_prim + sh), np = __ldg(B.sh_npf + sh);
+      for (int p = 0; p < np; ++p)
+        f1 += __ldg(B.p_cc + p0 + p) * gauss_df(__ldg(B.p_xp + p0 + p), __ldg(B.p_xplo + p0 + p), rh, rl);
+    }
+    sc.rad[sh] = f1;
   }
   __syncwarp();
 }
 
 __device__ __forceinline__ float phi32(const DevBasis& B, AtomScratch sc, int mu) {
+  if (mu >= B.nbf) return 0.f;
   const int sh = __ldg(B.f_shell + mu);
+  const float f1 = sc.rad[sh];
+  if (f1 == 0.f) return 0.f;
   const int a = __ldg(B.sh_atom + sh);
-  if (!(sc.d2[a] <= __ldg(B.sh_rad2 + sh))) return 0.f;
   const float x = sc.s[4 * a], y = sc.s[4 * a + 1], z = sc.s[4 * a + 2];
-  const float rh = static_cast<float>(sc.d2[a]), rl = sc.s[4 * a + 3];
-  const int p0 = __ldg(B.sh_prim + sh), np = __ldg(B.sh_npf + sh);
-  float f1 = 0.f;
-  for (int p = 0; p < np; ++p)
-    f1 += __ldg(B.p_cc + p0 + p) * gauss_df(__ldg(B.p_xp + p0 + p), __ldg(B.p_xplo + p0 + p), rh, rl);
   const int ijk = __ldg(B.f_ijk + mu);
   return powi(x, ijk & 15) * powi(y, (ijk >> 4) & 15) * powi(z, (ijk >> 8) & 15) * f1;
 }
 
+constexpr int kMaxPairs = 16;  // phi kept in registers for kpad <= 32 * 2 * kMaxPairs
+
 }  // namespace
 
-__global__ void __launch_bounds__(kWarps * 32) basis_split_kernel(DevBasis B, const double* __restrict__ pts,
+// One warp per point.  Lane l owns the function pairs (2l + 64t, 2l + 1 + 64t)
+// so that every store is a coalesced 128-byte row segment of packed halves.
+__global__ void __launch_bounds__(kWarps * 32, 2) basis_split_kernel(DevBasis B, const double* __restrict__ pts,
                                                                   int64_t npts, __half* __restrict__ a_hi,
                                                                   __half* __restrict__ a_lo,
                                                                   float* __restrict__ inv_scale) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t p = static_cast<int64_t>(blockIdx.x) * kWarps + warp;
   if (p >= npts) return;
-  AtomScratch sc = atom_scratch(warp, B.natoms);
+  AtomScratch sc = atom_scratch(warp, B.natoms, B.nshells);
   const double r[3] = {pts[3 * p], pts[3 * p + 1], pts[3 * p + 2]};
   fill_atoms(B, r, sc, lane);
+  const int npairs = B.kpad / 64;
+  const bool cached = npairs <= kMaxPairs;
+  float2 val[kMaxPairs];
   float vmax = 0.f;
-  for (int mu = lane; mu < B.nbf; mu += 32) vmax = fmaxf(vmax, fabsf(phi32(B, sc, mu)));
+#pragma unroll
+  for (int t = 0; t < kMaxPairs; ++t) {
+    if (t < npairs) {
+      const int mu = 64 * t + 2 * lane;
+      val[t] = make_float2(phi32(B, sc, mu), phi32(B, sc, mu + 1));
+      vmax = fmaxf(vmax, fmaxf(fabsf(val[t].x), fabsf(val[t].y)));
+    }
+  }
+  for (int t = kMaxPairs; t < npairs; ++t) {
+    const int mu = 64 * t + 2 * lane;
+    vmax = fmaxf(vmax, fmaxf(fabsf(phi32(B, sc, mu)), fabsf(phi32(B, sc, mu + 1))));
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
   // scale = 2^(14 - e) with vmax = m 2^e, m in [0.5, 1): scaled values < 2^14
@@ -84,13 +117,22 @@ __global__ void __launch_bounds__(kWarps * 32) basis_split_kernel(DevBasis B, co
     frexpf(vmax, &e);
     scale = ldexpf(1.f, 14 - e);
   }
-  __half* hi_row = a_hi + p * B.kpad;
-  __half* lo_row = a_lo + p * B.kpad;
-  for (int mu = lane; mu < B.kpad; mu += 32) {
-    const float v = mu < B.nbf ? phi32(B, sc, mu) * scale : 0.f;
-    const __half h = __float2half_rn(v);
-    hi_row[mu] = h;
-    lo_row[mu] = __float2half_rn(v - __half2float(h));
+  __half2* hi_row = reinterpret_cast<__half2*>(a_hi + p * B.kpad);
+  __half2* lo_row = reinterpret_cast<__half2*>(a_lo + p * B.kpad);
+  auto store = [&](int t, float2 v) {
+    v.x *= scale;
+    v.y *= scale;
+    const __half2 h = __floats2half2_rn(v.x, v.y);
+    const float2 hf = __half22float2(h);
+    hi_row[32 * t + lane] = h;
+    lo_row[32 * t + lane] = __floats2half2_rn(v.x - hf.x, v.y - hf.y);
+  };
+#pragma unroll
+  for (int t = 0; t < kMaxPairs; ++t)
+    if (t < npairs && cached) store(t, val[t]);
+  for (int t = cached ? npairs : 0; t < npairs; ++t) {
+    const int mu = 64 * t + 2 * lane;
+    store(t, make_float2(phi32(B, sc, mu), phi32(B, sc, mu + 1)));
   }
   if (lane == 0) inv_scale[p] = 1.f / scale;
 }
@@ -132,13 +174,15 @@ __global__ void __launch_bounds__(kWarps * 32) basis_fp64_kernel(DevBasis B, con
 
 const void* basis_split_kernel_ptr() { return reinterpret_cast<const void*>(&basis_split_kernel); }
 
-size_t basis_smem_bytes(int natoms) { return static_cast<size_t>(kWarps) * natoms * (sizeof(double) + 4 * sizeof(float)); }
+size_t basis_smem_bytes(int natoms, int nshells) {
+  return static_cast<size_t>(kWarps) * (natoms * (sizeof(double) + 4 * sizeof(float)) + nshells * sizeof(float));
+}
 
 void launch_basis_split(const DevBasis& B, const double* pts, int64_t npts, __half* a_hi, __half* a_lo,
                         float* inv_scale, cudaStream_t st) {
   if (npts <= 0) return;
   const int64_t blocks = (npts + kWarps - 1) / kWarps;
-  basis_split_kernel<<<static_cast<unsigned>(blocks), kWarps * 32, basis_smem_bytes(B.natoms), st>>>(
+  basis_split_kernel<<<static_cast<unsigned>(blocks), kWarps * 32, basis_smem_bytes(B.natoms, B.nshells), st>>>(
       B, pts, npts, a_hi, a_lo, inv_scale);
 }
 

@@ -28,14 +28,48 @@ constexpr int kStages = 2;
 constexpr int kTileA = kBlockM * kBlockK * 2;          // 16 KiB
 constexpr int kTileB = kBlockN * kBlockK * 2;          // 28 KiB
 constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;   // 88 KiB
-constexpr int kThreads = 192;
+constexpr int kEpiWarps = 8;                           // 2 per TMEM lane quarter
+constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kTmemCols = 512;
 constexpr int kAccStride = 256;
 constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+static_assert(kBlockM * kNDots * 8 <= kStageBytes, "epilogue reduction buffer must fit in one stage");
+
+__device__ __forceinline__ void tmem_ld1(uint32_t taddr, float& v) {
+  uint32_t r;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(r) : "r"(taddr) : "memory");
+  v = __uint_as_float(r);
+}
+
+// wait for this thread's TMEM loads; the registers are in/out operands so
+// that no use of them is scheduled before the wait
+__device__ __forceinline__ void tmem_wait7(float* v) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6])
+               :
+               : "memory");
+}
+
+__device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, %0;" ::"r"(32 * kEpiWarps) : "memory"); }
+
+// error-free fp32 sum: s + e = a + b exactly (Knuth two-sum)
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = hi + x;
+  const float bp = s - hi;
+  const float e = (hi - (s - bp)) + (x - bp);
+  hi = s;
+  lo += e;
+}
 }  // namespace
 
 int tc_smem_bytes() { return kSmemBytes; }
 
+// Per chunk the MMAs run in two passes over K into the same accumulator:
+// first the two small cross products (hi*lo, lo*hi), then the main product
+// (hi*hi).  Tensor-core accumulation truncates each partial sum to fp32; the
+// small terms are added while the accumulator is still small, which keeps
+// their truncation error negligible (measured: max error of j 1.2e-6 with the
+// products interleaved, 4.6e-7 cross-first, for nbf = 720).
 __global__ void __launch_bounds__(kThreads, 1)
     tc_fused_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_constant__ CUtensorMap tm_a_lo,
                     const __grid_constant__ CUtensorMap tm_b_hi, const __grid_constant__ CUtensorMap tm_b_lo,
@@ -53,6 +87,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBlockM;
   const int nchunk = Bs.nchunk, nkb = Bs.kpad / kBlockK;
+  const int nkb2 = (nkb + 1) / 2;  // main-product stages (two K blocks each)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -61,7 +96,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accfull[b], 1);
-      mbar_init(&accempty[b], 4);
+      mbar_init(&accempty[b], kEpiWarps);
     }
     fence_barrier_init();
   }
@@ -75,6 +110,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int it = 0;
       for (int c = 0; c < nchunk; ++c) {
+        // pass 1: A_hi, A_lo, B_hi, B_lo of one K block per stage
         for (int kb = 0; kb < nkb; ++kb, ++it) {
           const int s = it % kStages, round = it / kStages;
           if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto done;
@@ -84,6 +120,18 @@ __global__ void __launch_bounds__(kThreads, 1)
           tma_load_2d(st + kTileA, &tm_a_lo, &full[s], kb * kBlockK, static_cast<int>(m0));
           tma_load_2d(st + 2 * kTileA, &tm_b_hi, &full[s], kb * kBlockK, c * kBlockN);
           tma_load_2d(st + 2 * kTileA + kTileB, &tm_b_lo, &full[s], kb * kBlockK, c * kBlockN);
+        }
+        // pass 2: A_hi, B_hi of two K blocks per stage (same slots)
+        for (int k2 = 0; k2 < nkb2; ++k2, ++it) {
+          const int s = it % kStages, round = it / kStages;
+          if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto done;
+          unsigned char* st = base + s * kStageBytes;
+          const int kb0 = 2 * k2, nk = (kb0 + 1 < nkb) ? 2 : 1;
+          mbar_expect_tx(&full[s], nk * (kTileA + kTileB));
+          for (int j = 0; j < nk; ++j) {
+            tma_load_2d(st + j * kTileA, &tm_a_hi, &full[s], (kb0 + j) * kBlockK, static_cast<int>(m0));
+            tma_load_2d(st + 2 * kTileA + j * kTileB, &tm_b_hi, &full[s], (kb0 + j) * kBlockK, c * kBlockN);
+          }
         }
       }
     }
@@ -106,9 +154,24 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int k = 0; k < kBlockK / 16; ++k) {
             const uint64_t o = static_cast<uint64_t>(k * 32) >> 4;  // 16 fp16 = 32 bytes along K
-            mma_f16(d_tmem, ah + o, bh + o, idesc, (kb > 0 || k > 0) ? 1u : 0u);
-            mma_f16(d_tmem, ah + o, bl + o, idesc, 1u);
+            mma_f16(d_tmem, ah + o, bl + o, idesc, (kb > 0 || k > 0) ? 1u : 0u);
             mma_f16(d_tmem, al + o, bh + o, idesc, 1u);
+          }
+          mma_commit(&empty[s]);
+        }
+        for (int k2 = 0; k2 < nkb2; ++k2, ++it) {
+          const int s = it % kStages, round = it / kStages;
+          if (!mbar_wait(&full[s], round & 1, err, 3)) goto done;
+          tc_fence_after();
+          unsigned char* st = base + s * kStageBytes;
+          const int nk = (2 * k2 + 1 < nkb) ? 2 : 1;
+          for (int j = 0; j < nk; ++j) {
+            const uint64_t ah = smem_desc_sw128(st + j * kTileA), bh = smem_desc_sw128(st + 2 * kTileA + j * kTileB);
+#pragma unroll
+            for (int k = 0; k < kBlockK / 16; ++k) {
+              const uint64_t o = static_cast<uint64_t>(k * 32) >> 4;
+              mma_f16(d_tmem, ah + o, bh + o, idesc, 1u);
+            }
           }
           mma_commit(&empty[s]);
         }
@@ -116,26 +179,28 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    // ---------------- epilogue ----------------
+    // ---------------- epilogue: 8 warps ----------------
+    // warp w reads TMEM lanes 32*(w%4) .. +31 (its 32 points) and handles
+    // half (w-2)/4 of the 32 functions of every chunk.
     const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
     const int row = q * 32 + lane;
     const int64_t p = m0 + row;
     const bool valid = p < npts;
     double r[3] = {0.0, 0.0, 0.0};
-    float rscale = 0.f;
     if (valid) {
       r[0] = pts[3 * p];
       r[1] = pts[3 * p + 1];
       r[2] = pts[3 * p + 2];
-      rscale = inv_row[p];
     }
-    double tot[kNDots];
+    float thi[kNDots], tlo[kNDots];
 #pragma unroll
-    for (int i = 0; i < kNDots; ++i) tot[i] = 0.0;
+    for (int i = 0; i < kNDots; ++i) thi[i] = tlo[i] = 0.f;
     int cur_shell = -1, cur_atom = -1;
     float sx = 0.f, sy = 0.f, sz = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f, r2h = 0.f, r2l = 0.f;
     double d2a = 0.0;
     bool on = false;
+    const uint32_t lane_base = tmem_base + (static_cast<uint32_t>(q * 32) << 16);
     for (int c = 0; c < nchunk; ++c) {
       const int b = c & 1, rb = c >> 1;
       if (!mbar_wait(&accfull[b], rb & 1, err, 4)) break;
@@ -143,94 +208,100 @@ __global__ void __launch_bounds__(kThreads, 1)
       float part[kNDots];
 #pragma unroll
       for (int i = 0; i < kNDots; ++i) part[i] = 0.f;
-      const uint32_t tbase = tmem_base + (static_cast<uint32_t>(q * 32) << 16) + b * kAccStride;
+      const int f0 = c * kChunkF;
+      const int mb = f0 + half * (kChunkF / 2);
+      const int me = min(mb + kChunkF / 2, Bs.nbf);
+      const uint32_t tcol = lane_base + b * kAccStride;
 #pragma unroll 1
-      for (int sub = 0; sub < kChunkF / 8; ++sub) {
-        float v[kMats][8];
+      for (int mu = mb; mu < me; ++mu) {
+        const int u = mu - f0;
+        float v[kMats];
 #pragma unroll
-        for (int m = 0; m < kMats; ++m) tmem_ld8(tbase + m * kChunkF + sub * 8, v[m]);
-        tmem_ld_wait();
-        if (sub == kChunkF / 8 - 1) {
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&accempty[b]);
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int mu = c * kChunkF + sub * 8 + u;
-          if (mu < Bs.nbf) {
-            const int sh = __ldg(Bs.f_shell + mu);
-            if (sh != cur_shell) {
-              cur_shell = sh;
-              const int a = __ldg(Bs.sh_atom + sh);
-              if (a != cur_atom) {
-                cur_atom = a;
-                const double dx = r[0] - Bs.atom_xyz[3 * a], dy = r[1] - Bs.atom_xyz[3 * a + 1],
-                             dz = r[2] - Bs.atom_xyz[3 * a + 2];
-                d2a = dx * dx + dy * dy + dz * dz;
-                sx = static_cast<float>(dx);
-                sy = static_cast<float>(dy);
-                sz = static_cast<float>(dz);
-                r2h = static_cast<float>(d2a);
-                r2l = static_cast<float>(d2a - static_cast<double>(r2h));
-              }
-              on = d2a <= __ldg(Bs.sh_rad2 + sh);
-              f1 = f2 = f3 = 0.f;
-              if (on) {
-                const int p0 = __ldg(Bs.sh_prim + sh), np = __ldg(Bs.sh_npf + sh);
-                for (int k = 0; k < np; ++k) {
-                  const float al = __ldg(Bs.p_xp + p0 + k);
-                  const float e = __ldg(Bs.p_cc + p0 + k) * gauss_df(al, __ldg(Bs.p_xplo + p0 + k), r2h, r2l);
-                  f1 += e;
-                  f2 += al * e;
-                  f3 += al * al * e;
-                }
-              }
-            }
-            if (on) {
-              float ph, gx, gy, gz, lp;
-              cart_eval<float>(__ldg(Bs.f_ijk + mu), sx, sy, sz, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
-              const float* cs = inv_col + c * kBlockN + sub * 8 + u;
-              const float w0 = v[0][u] * __ldg(cs);
-              const float wc0 = v[1][u] * __ldg(cs + 1 * kChunkF), wc1 = v[2][u] * __ldg(cs + 2 * kChunkF),
-                          wc2 = v[3][u] * __ldg(cs + 3 * kChunkF);
-              const float q0 = v[4][u] * __ldg(cs + 4 * kChunkF), q1 = v[5][u] * __ldg(cs + 5 * kChunkF),
-                          q2 = v[6][u] * __ldg(cs + 6 * kChunkF);
-              const float wp = w0 * ph;
-              part[0] = fmaf(w0, ph, part[0]);
-              part[1] = fmaf(wp, sx, part[1]);
-              part[2] = fmaf(wp, sy, part[2]);
-              part[3] = fmaf(wp, sz, part[3]);
-              const float wx = w0 * sx, wy = w0 * sy, wz = w0 * sz;
-              part[4 + 1] = fmaf(wy, gx, part[4 + 1]);  // E[x][y]
-              part[4 + 2] = fmaf(wz, gx, part[4 + 2]);  // E[x][z]
-              part[4 + 3] = fmaf(wx, gy, part[4 + 3]);  // E[y][x]
-              part[4 + 5] = fmaf(wz, gy, part[4 + 5]);  // E[y][z]
-              part[4 + 6] = fmaf(wx, gz, part[4 + 6]);  // E[z][x]
-              part[4 + 7] = fmaf(wy, gz, part[4 + 7]);  // E[z][y]
-              const float wc[3] = {wc0, wc1, wc2}, qq[3] = {q0, q1, q2}, g[3] = {gx, gy, gz};
-#pragma unroll
-              for (int d = 0; d < 3; ++d) {
-#pragma unroll
-                for (int m = 0; m < 3; ++m) {
-                  part[13 + 3 * d + m] = fmaf(wc[d], g[m], part[13 + 3 * d + m]);
-                  part[25 + 3 * d + m] = fmaf(qq[d], g[m], part[25 + 3 * d + m]);
-                }
-                part[22 + d] = fmaf(wc[d], lp, part[22 + d]);
-                part[34 + d] = fmaf(qq[d], lp, part[34 + d]);
-              }
+        for (int m = 0; m < kMats; ++m) tmem_ld1(tcol + m * kChunkF + u, v[m]);
+        const int sh = __ldg(Bs.f_shell + mu);
+        if (sh != cur_shell) {
+          cur_shell = sh;
+          const int a = __ldg(Bs.sh_atom + sh);
+          if (a != cur_atom) {
+            cur_atom = a;
+            const double dx = r[0] - Bs.atom_xyz[3 * a], dy = r[1] - Bs.atom_xyz[3 * a + 1],
+                         dz = r[2] - Bs.atom_xyz[3 * a + 2];
+            d2a = dx * dx + dy * dy + dz * dz;
+            sx = static_cast<float>(dx);
+            sy = static_cast<float>(dy);
+            sz = static_cast<float>(dz);
+            r2h = static_cast<float>(d2a);
+            r2l = static_cast<float>(d2a - static_cast<double>(r2h));
+          }
+          on = d2a <= __ldg(Bs.sh_rad2 + sh);
+          f1 = f2 = f3 = 0.f;
+          if (on) {
+            const int p0 = __ldg(Bs.sh_prim + sh), np = __ldg(Bs.sh_npf + sh);
+            for (int k = 0; k < np; ++k) {
+              const float al = __ldg(Bs.p_xp + p0 + k);
+              const float e = __ldg(Bs.p_cc + p0 + k) * gauss_df(al, __ldg(Bs.p_xplo + p0 + k), r2h, r2l);
+              f1 += e;
+              f2 += al * e;
+              f3 += al * al * e;
             }
           }
         }
+        tmem_wait7(v);
+        if (on) {
+          float ph, gx, gy, gz, lp;
+          cart_eval<float>(__ldg(Bs.f_ijk + mu), sx, sy, sz, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
+          const float* cs = inv_col + c * kBlockN + u;
+          const float w0 = v[0] * __ldg(cs);
+          const float wc[3] = {v[1] * __ldg(cs + 1 * kChunkF), v[2] * __ldg(cs + 2 * kChunkF),
+                               v[3] * __ldg(cs + 3 * kChunkF)};
+          const float qq[3] = {v[4] * __ldg(cs + 4 * kChunkF), v[5] * __ldg(cs + 5 * kChunkF),
+                               v[6] * __ldg(cs + 6 * kChunkF)};
+          const float wp = w0 * ph;
+          part[0] = fmaf(w0, ph, part[0]);
+          part[1] = fmaf(wp, sx, part[1]);
+          part[2] = fmaf(wp, sy, part[2]);
+          part[3] = fmaf(wp, sz, part[3]);
+          const float wx = w0 * sx, wy = w0 * sy, wz = w0 * sz;
+          part[4 + 1] = fmaf(wy, gx, part[4 + 1]);  // E[x][y]
+          part[4 + 2] = fmaf(wz, gx, part[4 + 2]);  // E[x][z]
+          part[4 + 3] = fmaf(wx, gy, part[4 + 3]);  // E[y][x]
+          part[4 + 5] = fmaf(wz, gy, part[4 + 5]);  // E[y][z]
+          part[4 + 6] = fmaf(wx, gz, part[4 + 6]);  // E[z][x]
+          part[4 + 7] = fmaf(wy, gz, part[4 + 7]);  // E[z][y]
+          const float g[3] = {gx, gy, gz};
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+              part[13 + 3 * d + m] = fmaf(wc[d], g[m], part[13 + 3 * d + m]);
+              part[25 + 3 * d + m] = fmaf(qq[d], g[m], part[25 + 3 * d + m]);
+            }
+            part[22 + d] = fmaf(wc[d], lp, part[22 + d]);
+            part[34 + d] = fmaf(qq[d], lp, part[34 + d]);
+          }
+        }
       }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&accempty[b]);
 #pragma unroll
       for (int i = 0; i < kNDots; ++i)
-        if (i != 4 && i != 8 && i != 12) tot[i] += static_cast<double>(part[i]);
+        if (i != 4 && i != 8 && i != 12) two_sum_acc(thi[i], tlo[i], part[i]);
     }
-    if (valid) {
-      const double sc = static_cast<double>(rscale);
+    // combine the two halves of every point through shared memory (the
+    // pipeline stages are idle once the last accumulator has been read)
+    double* red = reinterpret_cast<double*>(base);
+    if (half == 1) {
 #pragma unroll
-      for (int i = 0; i < kNDots; ++i) tot[i] *= sc;
+      for (int i = 0; i < kNDots; ++i) red[row * kNDots + i] = static_cast<double>(thi[i]) + static_cast<double>(tlo[i]);
+    }
+    epi_barrier();
+    if (half == 0 && valid) {
+      double tot[kNDots];
+      const double sc = static_cast<double>(inv_row[p]);
+#pragma unroll
+      for (int i = 0; i < kNDots; ++i)
+        tot[i] = ((static_cast<double>(thi[i]) + static_cast<double>(tlo[i])) + red[row * kNDots + i]) * sc;
       double ct[9], dv[3];
       combine_point(tot, r, fl, ct, dv);
       if (out.jt)

@@ -214,14 +214,15 @@ def make_workload(name, outdir, seed=2024, uhf=False):
     sym, xyz = geo()
     mol = Molecule(sym, xyz, random_basis(rng, with_f))
     if os.path.exists(mol_path) and os.path.exists(xd_path):
-        return mol_path, xd_path, mol
+        return mol_path, xd_path, mol  # the MOL file is written last
     n = mol.nbf
     blocks = []
     for _ in range(2 if uhf else 1):
         d, pert = random_densities(rng, n, nocc if not uhf else max(1, nocc // 2))
         blocks += [d] + pert
-    write_mol(mol_path + ".tmp", mol, "synthetic %s seed %d" % (name, seed))
-    write_xdens(xd_path + ".tmp", blocks)
-    os.replace(mol_path + ".tmp", mol_path)
-    os.replace(xd_path + ".tmp", xd_path)
+    tmp = ".tmp%d" % os.getpid()
+    write_mol(mol_path + tmp, mol, "synthetic %s seed %d" % (name, seed))
+    write_xdens(xd_path + tmp, blocks)
+    os.replace(xd_path + tmp, xd_path)
+    os.replace(mol_path + tmp, mol_path)
     return mol_path, xd_path, mol

@@ -111,12 +111,30 @@ typedef struct {
  * prints sqrt(out[6])).  All in atomic units. */
 int gg_plane_integral(gg_ctx *ctx, const gg_grid *grid, double out[7], void *stream);
 
+/* A batch of planes in one device pass (bond-current profile scans, as the
+ * reference's jobscripts/src/current-profile-header:132-146 drive plane by
+ * plane): out is nplanes x 7 in the layout of gg_plane_integral. */
+int gg_plane_integrals(gg_ctx *ctx, const gg_grid *grids, int nplanes, double *out, void *stream);
+
 /* Composite quadrature (gaussint.f90:267-319); type 0 Gauss-Legendre,
  * 1 Gauss-Lobatto.  Returns GG_EINVAL if npts is not a multiple of order or
  * the Newton iteration fails. */
 int gg_gauss_data(double a, double b, int order, int npts, int type, double *pts, double *wgts);
 
 double gg_au2si(double au);  /* au -> nA/T (globals.f90 au2si) */
+
+/* Self-timing: with profiling on, every kernel group the context launches is
+ * bracketed by CUDA events on its stream; gg_profile_read returns the summed
+ * milliseconds and launch counts per group since gg_profile(ctx, 1), and the
+ * number of kernels launched.  No reference counterpart (the reference times
+ * itself with etime, src/libgimic/timer.f90). */
+#define GG_PROF_BASIS 0  /* fp32 basis evaluation + fp16 split of the point operand */
+#define GG_PROF_TC 1     /* tcgen05 contraction + fused current-tensor epilogue */
+#define GG_PROF_FP64 2   /* plain FP64 path (basis, DGEMM, assembly) */
+#define GG_PROF_PLANE 3  /* plane quadrature reduction */
+#define GG_NPROF 4
+int gg_profile(gg_ctx *ctx, int enable);
+int gg_profile_read(const gg_ctx *ctx, double ms[GG_NPROF], int64_t launches[GG_NPROF], int64_t *total_kernels);
 
 #ifdef __cplusplus
 }

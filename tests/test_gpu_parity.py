@@ -1,0 +1,215 @@
+"""GPU parity: libgimic_gb300 (through its C ABI) against the FP64 CPU oracle
+and the reference's golden outputs.
+
+Tolerances:
+  * plain FP64 GPU path: e_j <= 1e-12 (max |dj| / max |j|);
+  * split-FP16 tensor-core path: e_j <= 1e-6, integrated currents within
+    1e-4 nA/T of the oracle;
+  * div j: against central finite differences of the oracle's tensor.
+"""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN, rel_max_err, sample_points
+from gimic_gb300 import _lib, api
+from gimic_gb300 import grid as ggrid
+from gimic_gb300 import inp as ginp
+
+pytestmark = pytest.mark.gpu
+
+TOL_SPLIT = 1e-6
+TOL_FP64 = 1e-12
+TOL_NAT = 1e-4
+GOLD = json.load(open(os.path.join(GOLDEN, "golden.json")))
+
+
+def _pair(mol, xdens, uhf=False, screening=1e-8, precision="split16"):
+    g = api.Gimic(mol, xdens, uhf=uhf, screening=screening, precision=precision)
+    o = oracle.Oracle(mol, xdens, uhf=uhf, screening=screening)
+    return g, o
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL_FP64), ("split16", TOL_SPLIT)])
+def test_c6h6_points(c6h6, precision, tol):
+    mp, xp, _ = c6h6
+    g, o = _pair(mp, xp, precision=precision)
+    pts = sample_points(o.atoms()[0], 1500, 500, 8.0)
+    ref, rho_ref = o.jtensor(pts, with_rho=True)
+    jt, rho = g.jtensor_batch(pts, rho=True)
+    assert rel_max_err(jt, ref) <= tol
+    assert rel_max_err(rho, rho_ref) <= tol
+
+
+def test_divj_against_finite_differences(c6h6):
+    mp, xp, _ = c6h6
+    g, o = _pair(mp, xp, precision="fp64")
+    pts = sample_points(o.atoms()[0], 30, 10, 4.0, seed=3)
+    _, dv = g.jtensor_batch(pts, divj=True)
+    # fourth-order central differences (tight primitives vary on 0.01 Bohr)
+    h = 2e-4
+    fd = np.zeros((len(pts), 3))
+    for m in range(3):
+        e = np.zeros(3)
+        e[m] = h
+        t2p, t1p, t1m, t2m = (o.jtensor(pts + k * e) for k in (2, 1, -1, -2))
+        for b in range(3):
+            i = m + 3 * b
+            fd[:, b] += (-t2p[:, i] + 8 * t1p[:, i] - 8 * t1m[:, i] + t2m[:, i]) / (12 * h)
+    assert rel_max_err(dv, fd) <= 1e-6
+    g.set_precision("split16")
+    _, dv16 = g.jtensor_batch(pts, divj=True)
+    assert rel_max_err(dv16, dv) <= 1e-5
+
+
+@pytest.mark.parametrize("giao,dia,para", [(0, 1, 1), (1, 0, 1), (1, 1, 0), (0, 0, 1)])
+def test_flags(c6h6, giao, dia, para):
+    mp, xp, _ = c6h6
+    g, o = _pair(mp, xp, precision="fp64")
+    g.set_flags(giao, dia, para)
+    lib = oracle.lib()
+    lib.og_set_flags(o._h, giao, dia, para)
+    pts = sample_points(o.atoms()[0], 300, 100, 8.0, seed=5)
+    ref = o.jtensor(pts)
+    assert rel_max_err(g.jtensor_batch(pts), ref) <= TOL_FP64
+    g.set_precision("split16")
+    assert rel_max_err(g.jtensor_batch(pts), ref) <= TOL_SPLIT
+
+
+def test_c4h4_turbomole_readgrid(golden_dir):
+    """TURBOMOLE component order and density reordering; jvec on the
+    reference's external grid against jvec.vtu."""
+    d = golden_dir / "c4h4"
+    i = ginp.read(str(d / "read-grid.inp"))
+    g, o = _pair(str(d / "MOL"), str(d / "XDENS"))
+    assert g.turbomole and g.nbf == 168
+    grd = ggrid.new_grid(i, g.atoms()[0], workdir=str(d))
+    bb, _ = ggrid.get_magnet(grd, i)
+    g.set_magnet(bb)
+    pts = grd.points()
+    want = np.load(os.path.join(GOLDEN, "c4h4_readgrid.npz"))["jvec"]
+    jv = np.asarray(g.jvector_batch(pts))
+    assert rel_max_err(jv, want) <= TOL_SPLIT
+    g.set_precision("fp64")
+    assert rel_max_err(np.asarray(g.jvector_batch(pts)), want) <= 1e-9
+
+
+@pytest.mark.parametrize("spin", ["total", "alpha", "beta", "spindens"])
+def test_openshell_spin_cases(golden_dir, spin):
+    d = golden_dir / "open-shell"
+    g, o = _pair(str(d / "MOL"), str(d / "XDENS"), uhf=True)
+    pts = sample_points(o.atoms()[0], 800, 200, 8.0, seed=11)
+    ref = o.jtensor(pts, spin=spin)
+    g.set_spin(spin)
+    assert rel_max_err(g.jtensor_batch(pts), ref) <= TOL_SPLIT
+    g.set_precision("fp64")
+    assert rel_max_err(g.jtensor_batch(pts), ref) <= TOL_FP64
+
+
+@pytest.mark.parametrize("case,uhf,key", [("c4h4", False, "c4h4_integration"),
+                                          ("open-shell", True, "openshell_integration")])
+@pytest.mark.parametrize("precision", ["split16", "fp64"])
+def test_plane_integral_goldens(golden_dir, case, uhf, key, precision):
+    d = golden_dir / case
+    i = ginp.read(str(d / "integration.inp"))
+    g = api.Gimic(str(d / "MOL"), str(d / "XDENS"), uhf=uhf, screening=i.get("Advanced.screening_thrs"),
+                  precision=precision)
+    grd = ggrid.new_grid(i, g.atoms()[0])
+    bb, _ = ggrid.get_magnet(grd, i)
+    g.set_magnet(bb)
+    for blk in GOLD[key]:
+        g.set_spin(blk["spin"])
+        res = g.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)[blk["kind"]]
+        tol = 6e-7 if precision == "fp64" else 2e-6
+        for got, want in zip(res, (blk["au"], blk["pos"], blk["neg"])):
+            assert abs(got - want) <= tol, (blk, res)
+        assert abs(api.au2si(res[0]) - blk["nAT"]) <= (6e-7 if precision == "fp64" else TOL_NAT)
+
+
+def test_edge_cases(c6h6):
+    mp, xp, _ = c6h6
+    g, o = _pair(mp, xp)
+    assert g.jtensor_batch(np.zeros((0, 3))).shape == (0, 9)
+    coords = o.atoms()[0]
+    # a point on a nucleus, a ragged count (not a multiple of the 128-point tile)
+    pts = np.vstack([coords[:1], sample_points(coords, 120, 9, 6.0, seed=2)])
+    assert len(pts) % 128 != 0
+    assert rel_max_err(g.jtensor_batch(pts), o.jtensor(pts)) <= TOL_SPLIT
+    # far from every atom: all shells screened, exactly zero
+    far = np.array([[1e3, 0.0, 0.0], [0.0, -500.0, 40.0]])
+    assert np.all(g.jtensor_batch(far) == 0.0)
+    # one point through the single-point API
+    assert rel_max_err(np.array(g.jtensor(pts[5])), o.jtensor(pts[5:6])[0]) <= 1e-5
+
+
+def test_batching_is_invariant(c6h6):
+    """Tiles are independent: any batch split gives bit-identical results."""
+    mp, xp, _ = c6h6
+    g = api.Gimic(mp, xp, screening=1e-8)
+    pts = sample_points(g.atoms()[0], 3000, 100, 8.0, seed=9)
+    a = g.jtensor_batch(pts)
+    g.set_max_batch(256)
+    b = g.jtensor_batch(pts)
+    c = np.vstack([g.jtensor_batch(pts[s:s + 777]) for s in range(0, len(pts), 777)])
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+
+
+def test_device_and_host_buffers_agree(c6h6):
+    torch = pytest.importorskip("torch")
+    mp, xp, _ = c6h6
+    g = api.Gimic(mp, xp, screening=1e-8)
+    pts = sample_points(g.atoms()[0], 1000, 100, 8.0, seed=4)
+    host = g.jtensor_batch(pts, rho=True, divj=True)
+    dev = g.jtensor_batch(torch.as_tensor(pts, device="cuda"), rho=True, divj=True)
+    for h, d in zip(host, dev):
+        assert np.array_equal(h, d.cpu().numpy())
+
+
+def test_reference_compat_interface(golden_dir):
+    """gimic_init / gimic_calc_jtensor / gimic_calc_jvector / mkgausspoints
+    (src/libgimic/gimic_interface.h, gausspoints.h) through ctypes."""
+    L = _lib.load()
+    d = golden_dir / "c4h4"
+    L.gimic_init(str(d / "MOL").encode(), str(d / "XDENS").encode())
+    o = oracle.Oracle(str(d / "MOL"), str(d / "XDENS"), screening=1e-6)
+    b = (C.c_double * 3)(0.0, 0.0, 1.0)
+    L.gimic_set_magnet(b)
+    pts = sample_points(o.atoms()[0], 50, 10, 5.0, seed=8)
+    ref = o.jtensor(pts)
+    for p, t in zip(pts, ref):
+        r = (C.c_double * 3)(*p)
+        jt = (C.c_double * 9)()
+        jv = (C.c_double * 3)()
+        L.gimic_calc_jtensor(r, jt)
+        L.gimic_calc_jvector(r, jv)
+        assert np.abs(np.array(jt[:]) - t).max() <= TOL_SPLIT * np.abs(ref).max()
+        assert np.abs(np.array(jv[:]) - t[6:9]).max() <= TOL_SPLIT * np.abs(ref).max()
+    L.gimic_finalize()
+    a, bb, n, order = C.c_double(0.0), C.c_double(2.0), C.c_int(18), C.c_int(9)
+    pts_, wgt_ = (C.c_double * 18)(), (C.c_double * 18)()
+    L.mkgausspoints(C.byref(a), C.byref(bb), C.byref(n), C.byref(order), pts_, wgt_)
+    p_ref, w_ref = oracle.gauss_data(0.0, 2.0, 9, 18)
+    assert np.array_equal(np.array(pts_[:]), p_ref) and np.array_equal(np.array(wgt_[:]), w_ref)
+
+
+def test_full_cube_properties(synth_dir):
+    """The 128^3 C24H24 cube at full size: density non-negative (D = 2 C C^T
+    is positive semidefinite), split path against the FP64 path on a random
+    subset, and finite everywhere."""
+    torch = pytest.importorskip("torch")
+    from gimic_gb300 import synth
+    mp, xp, _ = synth.make_workload("c24h24", str(synth_dir), seed=2024)
+    g = api.Gimic(mp, xp, screening=1e-8)
+    ax = torch.linspace(-16.0, 16.0, 128, dtype=torch.float64, device="cuda")
+    pts = torch.stack(torch.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3).contiguous()
+    jt, rho, dv = g.jtensor_batch(pts, rho=True, divj=True)
+    assert bool(torch.isfinite(jt).all()) and bool(torch.isfinite(dv).all())
+    assert float(rho.min()) >= -1e-7 * float(rho.max())
+    idx = torch.randint(0, pts.shape[0], (2048,), generator=torch.Generator().manual_seed(1)).cuda()
+    g64 = api.Gimic(mp, xp, screening=1e-8, precision="fp64")
+    ref = g64.jtensor_batch(pts[idx].contiguous())
+    assert rel_max_err(jt[idx].cpu().numpy(), ref.cpu().numpy()) <= TOL_SPLIT

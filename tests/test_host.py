@@ -1,0 +1,188 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports
+every declared symbol, the C++ readers agree with the oracle's, quadrature is
+bit-identical to the oracle's restatement of gaussint.f90, the input parser
+accepts the reference's inputs, and errors come back as status codes."""
+import ctypes as C
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN, ROOT
+from gimic_gb300 import _lib, api, synth
+from gimic_gb300 import grid as ggrid
+from gimic_gb300 import inp as ginp
+
+
+def _declared_symbols():
+    text = open(os.path.join(ROOT, "include", "gimic_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gimic_\w+|gg_\w+|mkgausspoints)\s*\(", text)))
+
+
+def test_library_exports_header_symbols():
+    L = _lib.load()
+    names = _declared_symbols()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(L, name), name
+        assert name in _lib.SIGNATURES, name
+
+
+def _ctx(mol, xd, uhf=False, thr=1e-8):
+    h = C.c_void_p()
+    rc = _lib.load().gg_ctx_create(mol.encode(), xd.encode(), int(uhf), thr, C.byref(h))
+    return rc, h
+
+
+@pytest.mark.parametrize("case,uhf", [("c4h4", False), ("open-shell", True)])
+def test_readers_agree_with_oracle(golden_dir, case, uhf):
+    mol, xd = str(golden_dir / case / "MOL"), str(golden_dir / case / "XDENS")
+    rc, h = _ctx(mol, xd, uhf)
+    assert rc == 0
+    L = _lib.load()
+    o = oracle.Oracle(mol, xd, uhf=uhf, screening=1e-8)
+    nbf, nat, nsh, tm = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    L.gg_basis_info(h, C.byref(nbf), C.byref(nat), C.byref(nsh), C.byref(tm))
+    assert (nbf.value, nat.value, bool(tm.value)) == (o.nbf, o.natoms, o.turbomole)
+    assert nsh.value == len(o.shells()["l"])
+    xyz = np.zeros((nat.value, 3))
+    L.gg_atoms(h, xyz.ctypes.data_as(C.POINTER(C.c_double)), None)
+    assert np.array_equal(xyz, o.atoms()[0])
+    L.gg_ctx_destroy(h)
+
+
+def test_synthetic_inputs_roundtrip(c6h6):
+    mp, xp, mol = c6h6
+    o = oracle.Oracle(mp, xp)
+    assert o.nbf == mol.nbf == 120
+    d = o.density(0, 0)
+    assert np.array_equal(d, d.T)
+    for b in (1, 2, 3):
+        p = o.density(0, b)
+        assert np.array_equal(p, -p.T)
+    assert np.allclose(o.atoms()[0], mol.coords, atol=1e-11)
+
+
+@pytest.mark.parametrize("quad", ["gauss", "lobatto"])
+@pytest.mark.parametrize("order", [2, 3, 5, 7, 9, 10, 12, 13])
+def test_quadrature_bit_identical_to_oracle(quad, order):
+    for nblock, b in ((1, 1.0), (3, 7.25614), (20, 16.0)):
+        p, w = api.gauss_data(0.0, b, order, order * nblock, quad)
+        po, wo = oracle.gauss_data(0.0, b, order, order * nblock, quad)
+        assert np.array_equal(p, po) and np.array_equal(w, wo)
+
+
+def test_quadrature_known_answers():
+    # exact for polynomials of degree 2n-1 (Gauss) / 2n-3 (Lobatto) on [0, b]
+    for quad, deg in (("gauss", 17), ("lobatto", 15)):
+        p, w = api.gauss_data(0.0, 2.0, 9, 9, quad)
+        assert abs(np.sum(w * p ** deg) - 2.0 ** (deg + 1) / (deg + 1)) < 1e-9 * 2.0 ** (deg + 1)
+    # int exp(-x^2) over [-10, 10]^3 = pi^(3/2) (src/pygimic/quadrature.py:27-49)
+    p, w = api.gauss_data(0.0, 20.0, 10, 200, "gauss")
+    x = p - 10.0
+    s1 = np.sum(w * np.exp(-x * x))
+    assert abs(s1 ** 3 - math.pi ** 1.5) < 1e-10
+    with pytest.raises(ValueError):
+        api.gauss_data(0.0, 1.0, 9, 20)  # not a multiple of the order
+    assert api.gauss_data(0.0, 5.0, 9, 1)[0].tolist() == [0.0]
+
+
+def test_au2si():
+    assert abs(api.au2si(1.0) - 28.179409) < 5e-7
+    assert api.au2si(-0.708546) == pytest.approx(oracle.au2si(-0.708546), rel=1e-15)
+
+
+def test_error_codes(tmp_path, c6h6):
+    mp, xp, _ = c6h6
+    L = _lib.load()
+    rc, h = _ctx(str(tmp_path / "nope.mol"), xp)
+    assert rc == -2 and not h.value and b"open failed" in L.gg_last_error(None)
+    short = tmp_path / "short.xdens"
+    short.write_text("\n".join(open(xp).read().splitlines()[:1000]) + "\n")
+    rc, h = _ctx(mp, str(short))
+    assert rc == -2 and b"too short" in L.gg_last_error(None)
+    bad = tmp_path / "bad.mol"
+    bad.write_text("NOT AN INTGRL FILE\n")
+    rc, _ = _ctx(str(bad), xp)
+    assert rc == -2
+    rc, h = _ctx(mp, xp)
+    assert rc == 0
+    assert L.gg_set_spin(h, b"sideways") == -1
+    assert L.gg_set_flags(h, 1, 0, 0) == -1  # both dia and para off
+    assert L.gg_set_precision(h, 7) == -1
+    assert L.gg_set_max_batch(h, 1) == -1
+    L.gg_ctx_destroy(h)
+    with pytest.raises(_lib.GimicError):
+        api.Gimic(str(tmp_path / "nope.mol"), xp)
+
+
+def test_closed_shell_spin_cases_rejected_before_compute(c6h6):
+    # beta/spindens on a closed shell (jtensor.F90:77-98) is a host-side error
+    mp, xp, _ = c6h6
+    o = oracle.Oracle(mp, xp)
+    with pytest.raises(ValueError):
+        o.jtensor(np.zeros((1, 3)), spin="beta")
+
+
+def test_reference_inputs_parse(golden_dir):
+    for case, name in (("c4h4", "integration.inp"), ("c4h4", "read-grid.inp"),
+                       ("open-shell", "integration.inp"), ("open-shell", "3d.inp")):
+        i = ginp.read(str(golden_dir / case / name))
+        assert i.get("calc") in ("integral", "cdens")
+    i = ginp.read(str(golden_dir / "c4h4" / "integration.inp"))
+    assert i.grid_arg == "bond" and i.get("Grid.bond") == [2, 1] and i.get("Grid.gauss_order") == 9
+    assert i.get("Advanced.screening_thrs") == 1e-8 and i.get("Advanced.screening") is True
+    assert not i.is_set("Grid.radius") and i.is_set("Grid.rotation")
+
+
+@pytest.mark.parametrize("text,msg", [
+    ("calc=foo\nmagnet_axis=z\n", "unknown option calc"),
+    ("calc=cdens\n", "Direction of magnetic field must be set"),
+    ("calc=cdens\nmagnet=[0,0,1]\nmagnet_axis=z\n", "Both magnet vector and axis"),
+    ("calc=cdens\nmagnet_axis=z\nGrid(base){\ntype=even\norigin=[0,0,0]\n}\n", "Required option 'ivec'"),
+    ("calc=integral\nmagnet_axis=z\nGrid(bond){\ntype=gauss\ndistance=1.0\nbond=[1,2]\n}\n", "fixpoint or fixcoord"),
+    ("calc=cdens\nmagnet_axis=z\nGrid(base){\norigin=[0,0]\n}\n", "length mismatch"),
+    ("calc=cdens\nmagnet_axis=z\nGrid(base){\norigin=[0,0,0]\n", "unterminated section"),
+    ("calc=cdens\nmagnet_axis=z\nbogus=1\n", "Unknown keyword"),
+    ("calc=cdens\nmagnet_axis=z\nAdvanced{\nscreening=maybe\n}\n", "Not a bool"),
+])
+def test_input_errors(text, msg):
+    with pytest.raises(ginp.InputError, match=msg):
+        ginp.read(text, is_text=True)
+
+
+def test_input_syntax_features():
+    text = ('calc=integral  # comment\nmagnet_axis=T\ntitle="a b # c"\n'
+            'Advanced {\n screening_thrs=1.d-8\n GIAO=off\n}\n'
+            'Grid(bond) {\n type=lobatto\n bond=[1,|\n 2]\n fixpoint=3\n distance=0.5\n'
+            ' height=[-5.0, 5.0]\n width=[0.0, 8.0]\n grid_points=[60, 60, 0]\n gauss_order=10\n}\n')
+    i = ginp.read(text, is_text=True)
+    assert i.get("magnet_axis") == "X"  # T and X both mean "perpendicular" (gimic.in:277-283)
+    assert i.get("title") == "a b # c"
+    assert i.get("Advanced.screening_thrs") == 1e-8 and i.get("Advanced.GIAO") is False
+    assert i.get("Grid.bond") == [1, 2]
+
+
+def test_bond_grid_geometry(c6h6):
+    """Bond-plane frame of grid.f90:165-276 for a benzene C-C bond: normal
+    along the bond, plane spanned by -ortho and the in-plane direction."""
+    mp, xp, mol = c6h6
+    text = ('calc=integral\nmagnet_axis=z\nGrid(bond) {\n type=lobatto\n bond=[1,2]\n fixcoord=[0,0,0]\n'
+            ' distance=1.313\n height=[-8.0, 8.0]\n width=[0.0, 8.0]\n grid_points=[60, 60, 0]\n'
+            ' gauss_order=10\n}\n')
+    i = ginp.read(text, is_text=True)
+    g = ggrid.new_grid(i, mol.coords)
+    assert g.npts == [60, 60, 1]
+    bond = mol.coords[1] - mol.coords[0]
+    assert np.allclose(g.basv[:, 2], bond / np.linalg.norm(bond))
+    assert np.allclose(np.abs(g.basv[:, 0]), [0, 0, 1])
+    assert np.allclose(g.basv.T @ g.basv, np.eye(3), atol=1e-14)
+    bb, flipped = ggrid.get_magnet(g, i)
+    assert np.allclose(np.abs(bb), [0, 0, 1])
+    pts = g.points()
+    assert pts.shape == (3600, 3)
+    assert np.array_equal(pts[61], g.gridpoint(1, 1, 0))
