@@ -56,6 +56,8 @@ SIGNATURES = {
     "gg_gauss_data": (C.c_int, [C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "gg_au2si": (C.c_double, [C.c_double]),
     "gg_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "gg_jtensor_batch_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p]),
     "gg_profile_read": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
 }
 

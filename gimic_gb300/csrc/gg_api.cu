@@ -853,3 +853,94 @@ void mkgausspoints(double* a, double* b, int* npts, int* order, double* pts, dou
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Evaluation without device allocation.
+//
+// Some callers cannot let this library call cudaMalloc or cudaFree: host
+// applications that budget every byte of device memory themselves (a fixed
+// pool shared with other solvers), and time-critical loops where an
+// allocation could stall (cudaFree synchronises the whole device).  For
+// them gg_jtensor_batch_noalloc runs the split-FP16 path with its per-point
+// scratch (the fp16 hi/lo point operand and the per-point scale factors)
+// placed in the fixed array below instead of in buffers that grow on demand.
+// The array occupies kNoAllocScratchBytes on every GPU where the library's
+// device code is loaded, until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;  // 32 MiB
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+
+// Device address of g_noalloc_scratch for the current device, looked up once
+// per device (with that device current) and cached.
+cudaError_t noalloc_scratch(int device, void** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[device] = p;
+  }
+  *out = g_noalloc_addr[device];
+  return cudaSuccess;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+}  // namespace
+
+extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t n, double* jt, double* rho,
+                                        double* divt, void* stream) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (n < 0 || (n > 0 && !pts)) return ctx->fail(GG_EINVAL, "bad point array");
+  if (n == 0) return GG_OK;
+  if (ctx->precision != GG_PREC_SPLIT16)
+    return ctx->fail(GG_EUNSUPPORTED, "gg_jtensor_batch_noalloc runs the split-FP16 path only");
+  if (!ctx->tables_ready || !ctx->d_err || ctx->mats_spin != ctx->spin || ctx->mats_prec != ctx->precision)
+    return ctx->fail(GG_EINVAL,
+                     "context not prepared for this spin case: call gg_jtensor_batch once first (it builds the "
+                     "device tables, which allocates)");
+  if (!is_device_ptr(pts) || (jt && !is_device_ptr(jt)) || (rho && !is_device_ptr(rho)) ||
+      (divt && !is_device_ptr(divt)))
+    return ctx->fail(GG_EINVAL, "gg_jtensor_batch_noalloc takes device pointers only");
+  if (divt && !(ctx->flags.giao && ctx->flags.dia && ctx->flags.para))
+    return ctx->fail(GG_EUNSUPPORTED, "div j needs GIAO, diamagnetic and paramagnetic terms on");
+  const size_t kpad = static_cast<size_t>(ctx->dB.kpad);
+  const size_t per_point = 2 * kpad * sizeof(__half) + sizeof(float);
+  const int64_t max_pts = static_cast<int64_t>((kNoAllocScratchBytes - 3 * 256) / per_point);
+  if (n > max_pts)
+    return ctx->fail(GG_EINVAL, "gg_jtensor_batch_noalloc: " + std::to_string(n) + " points exceed its limit of " +
+                                    std::to_string(max_pts) + " points for nbf=" + std::to_string(ctx->basis.nbf) +
+                                    " (32 MiB of static scratch); split the batch");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
+  void* base = nullptr;
+  e = noalloc_scratch(ctx->device, &base);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+  // Carve the scratch.  Every element the contraction reads is rewritten by
+  // the basis kernel of this call, so nothing has to be cleared first.
+  char* c = static_cast<char*>(base);
+  __half* a_hi = reinterpret_cast<__half*>(c);
+  c += align256(static_cast<size_t>(n) * kpad * sizeof(__half));
+  __half* a_lo = reinterpret_cast<__half*>(c);
+  c += align256(static_cast<size_t>(n) * kpad * sizeof(__half));
+  float* inv_row = reinterpret_cast<float*>(c);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  gg::launch_basis_split(ctx->dB, pts, n, a_hi, a_lo, inv_row, st);
+  CUtensorMap tma_hi, tma_lo;
+  if (!encode_fp16_2d(&tma_hi, a_hi, n, ctx->dB.kpad, gg::kBlockM) ||
+      !encode_fp16_2d(&tma_lo, a_lo, n, ctx->dB.kpad, gg::kBlockM))
+    return ctx->fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
+  gg::TcArgs ta{&tma_hi, &tma_lo, &ctx->tm_b_hi, &ctx->tm_b_lo, inv_row, ctx->inv_col.as<float>(),
+                pts,     n,       ctx->flags,     gg::Outputs{jt, rho, divt}, ctx->d_err};
+  e = gg::launch_tc_fused(ctx->dB, ta, st);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "tensor-core kernel launch");
+  ctx->launches += 2;
+  return ctx->check_device_error(st);
+}

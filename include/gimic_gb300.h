@@ -136,6 +136,24 @@ double gg_au2si(double au);  /* au -> nA/T (globals.f90 au2si) */
 int gg_profile(gg_ctx *ctx, int enable);
 int gg_profile_read(const gg_ctx *ctx, double ms[GG_NPROF], int64_t launches[GG_NPROF], int64_t *total_kernels);
 
+/* Evaluation without device allocation (no counterpart in the reference).
+ * For callers that cannot let a library call cudaMalloc or cudaFree: host
+ * applications that budget all device memory themselves, and time-critical
+ * loops where an allocation would stall the device.  Same results as
+ * gg_jtensor_batch on the split-FP16 path, but the per-point scratch lives in
+ * a fixed 32 MiB static device array (held on every GPU where the library's
+ * device code is loaded, until the process exits), so n is limited to
+ * floor((32 MiB - 768) / (4 * kpad + 4)) points, kpad = nbf rounded up to 64
+ * (10,908 points for nbf 720); larger n is rejected with GG_EINVAL and a
+ * message.  All buffers must be device memory, and the context must already
+ * be prepared for its current spin case by one gg_jtensor_batch call (that
+ * call allocates the device tables).  The first call on a device looks up the
+ * array's address, so make it before any stream capture.  Every call reuses
+ * the same array: calls that overlap on the GPU (other streams, other
+ * contexts, other threads) race on it and must be serialised by the caller. */
+int gg_jtensor_batch_noalloc(gg_ctx *ctx, const double *pts, int64_t n, double *jt, double *rho, double *divt,
+                             void *stream);
+
 #ifdef __cplusplus
 }
 #endif
