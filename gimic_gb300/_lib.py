@@ -46,6 +46,7 @@ SIGNATURES = {
     "gg_set_flags": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "gg_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "gg_set_max_batch": (C.c_int, [C.c_void_p, C.c_int64]),
+    "gg_set_tile_screening": (C.c_int, [C.c_void_p, C.c_int]),
     "gg_basis_info": (C.c_int, [C.c_void_p, _ip, _ip, _ip, _ip]),
     "gg_atoms": (C.c_int, [C.c_void_p, _dp, _dp]),
     "gg_jtensor_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -56,6 +57,7 @@ SIGNATURES = {
     "gg_gauss_data": (C.c_int, [C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "gg_au2si": (C.c_double, [C.c_double]),
     "gg_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "gg_profile_blocks": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "gg_jtensor_batch_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_void_p]),
     "gg_profile_read": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),

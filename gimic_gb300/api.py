@@ -87,6 +87,9 @@ class Gimic:
     def set_flags(self, giao=True, diamag=True, paramag=True):
         check(self._L.gg_set_flags(self._h, int(giao), int(diamag), int(paramag)), self._h)
 
+    def set_tile_screening(self, on=True):
+        check(self._L.gg_set_tile_screening(self._h, int(bool(on))), self._h)
+
     def set_max_batch(self, n):
         check(self._L.gg_set_max_batch(self._h, int(n)), self._h)
 
@@ -132,13 +135,16 @@ class Gimic:
     def profile_read(self):
         """{group: (milliseconds, launches)} since profile(True), plus the
         total number of kernels this context launched."""
-        ms = np.zeros(4)
-        n = (C.c_int64 * 4)()
+        ms = np.zeros(5)
+        n = (C.c_int64 * 5)()
         tot = C.c_int64()
         check(self._L.gg_profile_read(self._h, _dptr(ms), n, C.byref(tot)), self._h)
-        names = ("basis", "tc", "fp64", "plane")
+        names = ("basis", "tc", "fp64", "plane", "order")
         out = {k: (float(ms[i]), int(n[i])) for i, k in enumerate(names)}
         out["kernels"] = int(tot.value)
+        issued, dense = C.c_int64(), C.c_int64()
+        check(self._L.gg_profile_blocks(self._h, C.byref(issued), C.byref(dense)), self._h)
+        out["gemm_blocks"] = (int(issued.value), int(dense.value))
         return out
 
     # ---- evaluation -----------------------------------------------------

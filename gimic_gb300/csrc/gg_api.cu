@@ -111,6 +111,7 @@ struct gg_ctx {
   double magnet[3] = {0, 0, 0};
   gg::Flags flags{1, 1, 1};
   int precision = GG_PREC_SPLIT16;
+  bool tile_screening = true;
   int device = 0;
   int64_t max_batch = 1 << 20;
 
@@ -127,6 +128,7 @@ struct gg_ctx {
 
   // scratch
   DevBuf a_hi, a_lo, inv_row, pts, jt, rho, divt, jv;
+  DevBuf sort_keys, sort_keys2, sort_idx, sort_perm, sort_temp, pts_sorted, tile_lists;
   DevBuf phi, gx, gy, gz, lap, w64;
   DevBuf plane_rows, plane_out;
   int* d_err = nullptr;
@@ -139,6 +141,9 @@ struct gg_ctx {
     size_t used = 0;
     double ms[GG_NPROF] = {0};
     int64_t launches[GG_NPROF] = {0};
+    unsigned long long* d_blocks = nullptr;  // GEMM blocks issued (profiling only)
+    unsigned long long dense_blocks = 0;     // blocks without screening
+    unsigned long long host_blocks = 0;      // blocks of unscreened batches
   } prof;
 
   void prof_begin(int cls, cudaStream_t st, size_t* slot) {
@@ -156,6 +161,11 @@ struct gg_ctx {
   void prof_end(cudaStream_t st, size_t slot) {
     if (prof.on) cudaEventRecord(prof.pool[slot].second, st);
   }
+  void prof_add_blocks(unsigned long long v, cudaStream_t st) {
+    // host-known count (no screening): fold into the device counter later
+    prof.host_blocks += v;
+    (void)st;
+  }
   void prof_collect() {
     for (auto& pr : prof.pending) {
       float t = 0.f;
@@ -170,6 +180,7 @@ struct gg_ctx {
   }
 
   ~gg_ctx() {
+    if (prof.d_blocks) cudaFree(prof.d_blocks);
     for (auto& e : prof.pool) {
       cudaEventDestroy(e.first);
       cudaEventDestroy(e.second);
@@ -182,7 +193,8 @@ struct gg_ctx {
     table_allocs.clear();
     tables_ready = false;
     for (DevBuf* b : {&b_fp64, &b_hi, &b_lo, &inv_col, &a_hi, &a_lo, &inv_row, &pts, &jt, &rho, &divt, &jv, &phi, &gx,
-                      &gy, &gz, &lap, &w64, &plane_rows, &plane_out})
+                      &gy, &gz, &lap, &w64, &plane_rows, &plane_out, &sort_keys, &sort_keys2, &sort_idx, &sort_perm,
+                      &sort_temp, &pts_sorted, &tile_lists})
       b->release();
     if (d_err) cudaFree(d_err);
     d_err = nullptr;
@@ -421,15 +433,59 @@ struct gg_ctx {
     if (e == cudaSuccess) e = inv_row.reserve(static_cast<size_t>(n) * sizeof(float));
     if (e != cudaSuccess) return cuda_fail(e, "split-path scratch");
     size_t slot = 0;
+    // Tile screening: order the points along a Z curve so that tiles are
+    // compact, then list the shells each tile can see (k_tiles.cu).
+    const int stride = gg::tile_stride(dB);
+    const bool screen = tile_screening && stride <= 512;
+    const double* tp = d_pts;
+    const int* tiles = nullptr;
+    const int* perm = nullptr;
+    if (screen) {
+      const int64_t ntiles = (n + gg::kBlockM - 1) / gg::kBlockM;
+      const size_t tb = gg::sort_temp_bytes(n);
+      e = sort_keys.reserve(n * sizeof(uint32_t));
+      if (e == cudaSuccess) e = sort_keys2.reserve(n * sizeof(uint32_t));
+      if (e == cudaSuccess) e = sort_idx.reserve(n * sizeof(int));
+      if (e == cudaSuccess) e = sort_perm.reserve(n * sizeof(int));
+      if (e == cudaSuccess) e = sort_temp.reserve(std::max<size_t>(tb, 16));
+      if (e == cudaSuccess) e = pts_sorted.reserve(static_cast<size_t>(n) * 3 * sizeof(double));
+      if (e == cudaSuccess) e = tile_lists.reserve(static_cast<size_t>(ntiles) * stride * sizeof(int));
+      if (e != cudaSuccess) return cuda_fail(e, "tile-screening scratch");
+      double lo[3] = {0, 0, 0};
+      for (const gg::Atom& a : basis.atoms)
+        for (int d = 0; d < 3; ++d) lo[d] += a.coord[d] / static_cast<double>(basis.atoms.size());
+      for (int d = 0; d < 3; ++d) lo[d] -= 64.0;  // 1024 cells of 0.125 Bohr around the molecule
+      prof_begin(GG_PROF_ORDER, st, &slot);
+      e = gg::launch_spatial_order(d_pts, n, lo, 0.125, sort_keys.as<uint32_t>(), sort_keys2.as<uint32_t>(),
+                                   sort_idx.as<int>(), sort_perm.as<int>(), sort_temp.p, tb,
+                                   pts_sorted.as<double>(), st);
+      if (e != cudaSuccess) return cuda_fail(e, "spatial ordering");
+      gg::launch_tile_screen(dB, pts_sorted.as<double>(), n, tile_lists.as<int>(), st);
+      prof_end(st, slot);
+      if (prof.on && prof.d_blocks) gg::launch_tile_work(tile_lists.as<int>(), ntiles, stride, prof.d_blocks, st);
+      launches += 4;
+      tp = pts_sorted.as<double>();
+      tiles = tile_lists.as<int>();
+      perm = sort_perm.as<int>();
+    }
     prof_begin(GG_PROF_BASIS, st, &slot);
-    gg::launch_basis_split(dB, d_pts, n, a_hi.as<__half>(), a_lo.as<__half>(), inv_row.as<float>(), st);
+    gg::launch_basis_split(dB, tp, n, a_hi.as<__half>(), a_lo.as<__half>(), inv_row.as<float>(), st);
     prof_end(st, slot);
     CUtensorMap tma_hi, tma_lo;
     if (!encode_fp16_2d(&tma_hi, a_hi.p, n, dB.kpad, gg::kBlockM) ||
         !encode_fp16_2d(&tma_lo, a_lo.p, n, dB.kpad, gg::kBlockM))
       return fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
     gg::TcArgs ta{&tma_hi, &tma_lo, &tm_b_hi, &tm_b_lo, inv_row.as<float>(), inv_col.as<float>(),
-                  d_pts,   n,       flags,    out,      d_err};
+                  tp,      n,       flags,    out,      d_err};
+    ta.tiles = tiles;
+    ta.tile_stride = stride;
+    ta.perm = perm;
+    if (prof.on) {
+      const unsigned long long blocks = static_cast<unsigned long long>((n + gg::kBlockM - 1) / gg::kBlockM) *
+                                        dB.nchunk * (dB.kpad / gg::kBlockK);
+      prof.dense_blocks += blocks;
+      if (!screen && prof.d_blocks) prof_add_blocks(blocks, st);
+    }
     prof_begin(GG_PROF_TC, st, &slot);
     e = gg::launch_tc_fused(dB, ta, st);
     prof_end(st, slot);
@@ -595,6 +651,13 @@ int gg_set_precision(gg_ctx* ctx, int mode) {
   return GG_OK;
 }
 
+int gg_set_tile_screening(gg_ctx* ctx, int enable) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->tile_screening = enable != 0;
+  return GG_OK;
+}
+
 int gg_set_max_batch(gg_ctx* ctx, int64_t npts) {
   if (!ctx || npts < 128) return GG_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
@@ -747,6 +810,16 @@ int gg_profile(gg_ctx* ctx, int enable) {
     ctx->prof.ms[i] = 0.0;
     ctx->prof.launches[i] = 0;
   }
+  ctx->prof.dense_blocks = 0;
+  ctx->prof.host_blocks = 0;
+  if (ctx->prof.on) {
+    cudaSetDevice(ctx->device);
+    if (!ctx->prof.d_blocks && cudaMalloc(&ctx->prof.d_blocks, sizeof(unsigned long long)) != cudaSuccess) {
+      ctx->prof.d_blocks = nullptr;
+      return ctx->fail(GG_ENOMEM, "profiling counter");
+    }
+    cudaMemset(ctx->prof.d_blocks, 0, sizeof(unsigned long long));
+  }
   ctx->launches = 0;
   return GG_OK;
 }
@@ -758,6 +831,15 @@ int gg_profile_read(const gg_ctx* ctx, double ms[GG_NPROF], int64_t launches[GG_
     if (launches) launches[i] = ctx->prof.launches[i];
   }
   if (total_kernels) *total_kernels = ctx->launches;
+  return GG_OK;
+}
+
+int gg_profile_blocks(const gg_ctx* ctx, int64_t* issued, int64_t* dense) {
+  if (!ctx) return GG_EINVAL;
+  unsigned long long dev = 0;
+  if (ctx->prof.d_blocks) cudaMemcpy(&dev, ctx->prof.d_blocks, sizeof(dev), cudaMemcpyDeviceToHost);
+  if (issued) *issued = static_cast<int64_t>(dev + ctx->prof.host_blocks);
+  if (dense) *dense = static_cast<int64_t>(ctx->prof.dense_blocks);
   return GG_OK;
 }
 

@@ -45,8 +45,20 @@ struct TcArgs {
   Flags flags;
   Outputs out;
   int* err;                    // device error word (0 = ok)
+  const int* tiles = nullptr;  // per-tile active chunk / K-block lists (null: all)
+  int tile_stride = 0;
+  const int* perm = nullptr;   // output index of each (sorted) point (null: identity)
 };
 int tc_smem_bytes();
+
+// Spatial ordering and tile screening (k_tiles.cu)
+int tile_stride(const DevBasis& B);
+size_t sort_temp_bytes(int64_t n);
+cudaError_t launch_spatial_order(const double* pts, int64_t n, const double lo[3], double cell, uint32_t* keys,
+                                 uint32_t* keys_sorted, int* idx, int* perm, void* temp, size_t temp_bytes,
+                                 double* pts_sorted, cudaStream_t st);
+void launch_tile_screen(const DevBasis& B, const double* pts_sorted, int64_t n, int* tiles, cudaStream_t st);
+void launch_tile_work(const int* tiles, int64_t ntiles, int stride, unsigned long long* acc, cudaStream_t st);
 cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st);
 
 // Many planes at once: plane q owns points [pt_off, pt_off + p1*p2*p3) of jt

@@ -32,7 +32,8 @@ constexpr int kEpiWarps = 8;                           // 2 per TMEM lane quarte
 constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kTmemCols = 512;
 constexpr int kAccStride = 256;
-constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+constexpr int kMaxTileList = 512;  // ints: 2 + column chunks + K blocks of a tile (nbf <= 10,000)
+constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256 + kMaxTileList * 4;
 static_assert(kBlockM * kNDots * 8 <= kStageBytes, "epilogue reduction buffer must fit in one stage");
 
 __device__ __forceinline__ void tmem_ld1(uint32_t taddr, float& v) {
@@ -74,7 +75,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_fused_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_constant__ CUtensorMap tm_a_lo,
                     const __grid_constant__ CUtensorMap tm_b_hi, const __grid_constant__ CUtensorMap tm_b_lo,
                     DevBasis Bs, const float* __restrict__ inv_row, const float* __restrict__ inv_col,
-                    const double* __restrict__ pts, int64_t npts, Flags fl, Outputs out, int* err) {
+                    const double* __restrict__ pts, int64_t npts, Flags fl, Outputs out, int* err,
+                    const int* __restrict__ tiles, int tstride, const int* __restrict__ perm) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                          ~static_cast<uintptr_t>(1023));
@@ -83,11 +85,25 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* accfull = empty + kStages;
   uint64_t* accempty = accfull + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accempty + 2);
+  int* tlist = reinterpret_cast<int*>(tmem_slot + 4);  // {#chunks, #kblocks, chunk ids, kblock ids}
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBlockM;
-  const int nchunk = Bs.nchunk, nkb = Bs.kpad / kBlockK;
-  const int nkb2 = (nkb + 1) / 2;  // main-product stages (two K blocks each)
+  const int nchunk_all = Bs.nchunk, nkb_all = Bs.kpad / kBlockK;
+  // active column chunks and K blocks of this tile (all of them without a
+  // screening list)
+  if (tiles) {
+    for (int i = threadIdx.x; i < tstride; i += blockDim.x) tlist[i] = tiles[static_cast<int64_t>(blockIdx.x) * tstride + i];
+  } else {
+    for (int i = threadIdx.x; i < nchunk_all; i += blockDim.x) tlist[2 + i] = i;
+    for (int i = threadIdx.x; i < nkb_all; i += blockDim.x) tlist[2 + nchunk_all + i] = i;
+    if (threadIdx.x == 0) {
+      tlist[0] = nchunk_all;
+      tlist[1] = nkb_all;
+    }
+  }
+  const int* clist = tlist + 2;
+  const int* klist = tlist + 2 + nchunk_all;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -105,13 +121,18 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
+  const int nkb = tlist[1];
+  const int nchunk = nkb > 0 ? tlist[0] : 0;
+  const int nkb2 = (nkb + 1) / 2;  // main-product stages (two K blocks each)
 
   if (warp == 0) {
     if (lane == 0) {
       int it = 0;
-      for (int c = 0; c < nchunk; ++c) {
+      for (int ci = 0; ci < nchunk; ++ci) {
+        const int c = clist[ci];
         // pass 1: A_hi, A_lo, B_hi, B_lo of one K block per stage
-        for (int kb = 0; kb < nkb; ++kb, ++it) {
+        for (int ki = 0; ki < nkb; ++ki, ++it) {
+          const int kb = klist[ki];
           const int s = it % kStages, round = it / kStages;
           if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto done;
           unsigned char* st = base + s * kStageBytes;
@@ -126,11 +147,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int s = it % kStages, round = it / kStages;
           if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto done;
           unsigned char* st = base + s * kStageBytes;
-          const int kb0 = 2 * k2, nk = (kb0 + 1 < nkb) ? 2 : 1;
+          const int ki0 = 2 * k2, nk = (ki0 + 1 < nkb) ? 2 : 1;
           mbar_expect_tx(&full[s], nk * (kTileA + kTileB));
           for (int j = 0; j < nk; ++j) {
-            tma_load_2d(st + j * kTileA, &tm_a_hi, &full[s], (kb0 + j) * kBlockK, static_cast<int>(m0));
-            tma_load_2d(st + 2 * kTileA + j * kTileB, &tm_b_hi, &full[s], (kb0 + j) * kBlockK, c * kBlockN);
+            const int kb = klist[ki0 + j];
+            tma_load_2d(st + j * kTileA, &tm_a_hi, &full[s], kb * kBlockK, static_cast<int>(m0));
+            tma_load_2d(st + 2 * kTileA + j * kTileB, &tm_b_hi, &full[s], kb * kBlockK, c * kBlockN);
           }
         }
       }
@@ -139,8 +161,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_f16(kBlockM, kBlockN);
       int it = 0;
-      for (int c = 0; c < nchunk; ++c) {
-        const int b = c & 1, rb = c >> 1;
+      for (int ci = 0; ci < nchunk; ++ci) {
+        const int b = ci & 1, rb = ci >> 1;
         if (!mbar_wait(&accempty[b], (rb & 1) ^ 1, err, 2)) goto done;
         tc_fence_after();
         const uint32_t d_tmem = tmem_base + b * kAccStride;
@@ -201,8 +223,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     double d2a = 0.0;
     bool on = false;
     const uint32_t lane_base = tmem_base + (static_cast<uint32_t>(q * 32) << 16);
-    for (int c = 0; c < nchunk; ++c) {
-      const int b = c & 1, rb = c >> 1;
+    for (int ci = 0; ci < nchunk; ++ci) {
+      const int c = clist[ci];
+      const int b = ci & 1, rb = ci >> 1;
       if (!mbar_wait(&accfull[b], rb & 1, err, 4)) break;
       tc_fence_after();
       float part[kNDots];
@@ -304,11 +327,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         tot[i] = ((static_cast<double>(thi[i]) + static_cast<double>(tlo[i])) + red[row * kNDots + i]) * sc;
       double ct[9], dv[3];
       combine_point(tot, r, fl, ct, dv);
+      const int64_t o = perm ? static_cast<int64_t>(perm[p]) : p;  // caller's point order
       if (out.jt)
-        for (int i = 0; i < 9; ++i) out.jt[9 * p + i] = ct[i];
-      if (out.rho) out.rho[p] = tot[0];
+        for (int i = 0; i < 9; ++i) out.jt[9 * o + i] = ct[i];
+      if (out.rho) out.rho[o] = tot[0];
       if (out.divt)
-        for (int i = 0; i < 3; ++i) out.divt[3 * p + i] = dv[i];
+        for (int i = 0; i < 3; ++i) out.divt[3 * o + i] = dv[i];
     }
   }
 done:
@@ -332,7 +356,7 @@ cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st)
   tc_fused_kernel<<<grid, kThreads, kSmemBytes, st>>>(
       *static_cast<const CUtensorMap*>(a.tmap_a_hi), *static_cast<const CUtensorMap*>(a.tmap_a_lo),
       *static_cast<const CUtensorMap*>(a.tmap_b_hi), *static_cast<const CUtensorMap*>(a.tmap_b_lo), B,
-      a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err);
+      a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err, a.tiles, a.tile_stride, a.perm);
   return cudaGetLastError();
 }
 

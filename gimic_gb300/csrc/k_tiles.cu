@@ -1,0 +1,164 @@
+// Tile-level exponent screening for the tensor-core contraction.
+//
+// The reference screens per point and per contraction: a shell contributes
+// to a point only within its screening radius (src/libgimic/basis.f90:90-136,
+// used by bfeval/dfdr).  For a compact tile of points, every shell that is
+// out of range for the whole tile contributes exact zeros both to the GEMM
+// (its rows of the point operand are zero: those K blocks can be skipped) and
+// to the epilogue (its columns are multiplied by zero basis values: those
+// column chunks can be skipped).  Skipping them changes no result.
+//
+//  1. morton_key_kernel + a radix sort order the points along a Z curve so
+//     that 128 consecutive points form a compact tile;
+//  2. gather_kernel copies the points into that order;
+//  3. tile_screen_kernel lists, per tile, the active 32-function column
+//     chunks and 64-function K blocks with a conservative bounding-sphere test.
+#include <cub/device/device_radix_sort.cuh>
+
+#include "gg_kernels.h"
+
+namespace gg {
+
+namespace {
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000ffu;
+  v = (v | (v << 8)) & 0x0300f00fu;
+  v = (v | (v << 4)) & 0x030c30c3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+}  // namespace
+
+__global__ void morton_key_kernel(const double* __restrict__ pts, int64_t n, double lox, double loy, double loz,
+                                  double inv_cell, uint32_t* __restrict__ keys, int* __restrict__ idx) {
+  const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const double lo[3] = {lox, loy, loz};
+  uint32_t c[3];
+  for (int d = 0; d < 3; ++d) {
+    double q = (pts[3 * p + d] - lo[d]) * inv_cell;
+    q = q < 0.0 ? 0.0 : (q > 1023.0 ? 1023.0 : q);  // NaN-free clamp; far points share edge cells
+    c[d] = static_cast<uint32_t>(q);
+  }
+  keys[p] = spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
+  idx[p] = static_cast<int>(p);
+}
+
+__global__ void gather_kernel(const double* __restrict__ pts, const int* __restrict__ perm, int64_t n,
+                              double* __restrict__ out) {
+  const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int64_t s = perm[p];
+  out[3 * p] = pts[3 * s];
+  out[3 * p + 1] = pts[3 * s + 1];
+  out[3 * p + 2] = pts[3 * s + 2];
+}
+
+// One block of 128 threads per tile.  tiles[t * stride] = {#chunks, #kblocks,
+// chunk ids..., kblock ids...}.  A shell is out of range for the tile when
+// |R_A - c| - rho > radius (c, rho: centre and radius of the tile's bounding
+// box), which by the triangle inequality excludes it for every point.
+__global__ void __launch_bounds__(128) tile_screen_kernel(DevBasis B, const double* __restrict__ pts, int64_t n,
+                                                          int stride, int* __restrict__ tiles) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* shell_on = smem_raw;                    // nshells
+  unsigned char* chunk_on = shell_on + B.nshells;        // nchunk
+  unsigned char* kb_on = chunk_on + B.nchunk;            // kpad / 64
+  __shared__ double bmin[3][128], bmax[3][128];
+  const int64_t t = blockIdx.x;
+  const int64_t p = t * kBlockM + threadIdx.x;
+  const int nkb = B.kpad / kBlockK;
+  for (int d = 0; d < 3; ++d) {
+    const double v = p < n ? pts[3 * p + d] : pts[3 * (t * kBlockM) + d];
+    bmin[d][threadIdx.x] = v;
+    bmax[d][threadIdx.x] = v;
+  }
+  for (int i = threadIdx.x; i < B.nchunk; i += 128) chunk_on[i] = 0;
+  for (int i = threadIdx.x; i < nkb; i += 128) kb_on[i] = 0;
+  __syncthreads();
+  for (int s = 64; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int d = 0; d < 3; ++d) {
+        bmin[d][threadIdx.x] = fmin(bmin[d][threadIdx.x], bmin[d][threadIdx.x + s]);
+        bmax[d][threadIdx.x] = fmax(bmax[d][threadIdx.x], bmax[d][threadIdx.x + s]);
+      }
+    __syncthreads();
+  }
+  double c[3], rho2 = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    c[d] = 0.5 * (bmin[d][0] + bmax[d][0]);
+    const double h = 0.5 * (bmax[d][0] - bmin[d][0]);
+    rho2 += h * h;
+  }
+  const double rho = sqrt(rho2);
+  for (int sh = threadIdx.x; sh < B.nshells; sh += 128) {
+    const int a = B.sh_atom[sh];
+    const double dx = B.atom_xyz[3 * a] - c[0], dy = B.atom_xyz[3 * a + 1] - c[1], dz = B.atom_xyz[3 * a + 2] - c[2];
+    const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+    const double rad = sqrt(B.sh_rad2[sh]);
+    shell_on[sh] = !(dist - rho > rad * (1.0 + 1e-12) + 1e-9);
+  }
+  __syncthreads();
+  for (int mu = threadIdx.x; mu < B.nbf; mu += 128)
+    if (shell_on[B.f_shell[mu]]) {
+      chunk_on[mu / kChunkF] = 1;
+      kb_on[mu / kBlockK] = 1;
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int* out = tiles + t * stride;
+    int nc = 0, nk = 0;
+    for (int i = 0; i < B.nchunk; ++i)
+      if (chunk_on[i]) out[2 + nc++] = i;
+    for (int i = 0; i < nkb; ++i)
+      if (kb_on[i]) out[2 + B.nchunk + nk++] = i;
+    out[0] = nc;
+    out[1] = nk;
+  }
+}
+
+// Sum over tiles of (active chunks x active K blocks): the number of
+// (224-column, 64-deep) GEMM blocks the contraction issues, for profiling.
+__global__ void tile_work_kernel(const int* __restrict__ tiles, int64_t ntiles, int stride,
+                                 unsigned long long* __restrict__ acc) {
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  unsigned long long v = 0;
+  if (t < ntiles) v = static_cast<unsigned long long>(tiles[t * stride]) * tiles[t * stride + 1];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(acc, v);
+}
+
+void launch_tile_work(const int* tiles, int64_t ntiles, int stride, unsigned long long* acc, cudaStream_t st) {
+  tile_work_kernel<<<static_cast<unsigned>((ntiles + 255) / 256), 256, 0, st>>>(tiles, ntiles, stride, acc);
+}
+
+int tile_stride(const DevBasis& B) { return 2 + B.nchunk + B.kpad / kBlockK; }
+
+size_t sort_temp_bytes(int64_t n) {
+  size_t bytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, bytes, static_cast<const uint32_t*>(nullptr),
+                                  static_cast<uint32_t*>(nullptr), static_cast<const int*>(nullptr),
+                                  static_cast<int*>(nullptr), static_cast<int>(n), 0, 30);
+  return bytes;
+}
+
+cudaError_t launch_spatial_order(const double* pts, int64_t n, const double lo[3], double cell, uint32_t* keys,
+                                 uint32_t* keys_sorted, int* idx, int* perm, void* temp, size_t temp_bytes,
+                                 double* pts_sorted, cudaStream_t st) {
+  const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
+  morton_key_kernel<<<blocks, 256, 0, st>>>(pts, n, lo[0], lo[1], lo[2], 1.0 / cell, keys, idx);
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys_sorted, idx, perm, static_cast<int>(n),
+                                                  0, 30, st);
+  if (e != cudaSuccess) return e;
+  gather_kernel<<<blocks, 256, 0, st>>>(pts, perm, n, pts_sorted);
+  return cudaGetLastError();
+}
+
+void launch_tile_screen(const DevBasis& B, const double* pts_sorted, int64_t n, int* tiles, cudaStream_t st) {
+  const int64_t ntiles = (n + kBlockM - 1) / kBlockM;
+  const size_t smem = static_cast<size_t>(B.nshells) + B.nchunk + B.kpad / kBlockK;
+  tile_screen_kernel<<<static_cast<unsigned>(ntiles), 128, smem, st>>>(B, pts_sorted, n, tile_stride(B), tiles);
+}
+
+}  // namespace gg

@@ -131,6 +131,64 @@ def benzene():
     return ring(6, cc=1.39, ch=1.09)
 
 
+def honeycomb_patch(ncarbon, rng, cc=1.42, ch=1.09):
+    """Planar sheet of exactly ``ncarbon`` C atoms cut from a honeycomb lattice
+    around a random centre (jittered so that shapes vary), dangling carbons
+    pruned and refilled, one H on every perimeter carbon (two C neighbours)."""
+    a = math.sqrt(3.0) * cc
+    lat = []
+    m = 8
+    for i in range(-m, m + 1):
+        for j in range(-m, m + 1):
+            x = a * (i + 0.5 * j)
+            y = a * (math.sqrt(3.0) / 2.0) * j
+            lat.append((x, y))
+            lat.append((x, y + cc))
+    lat = np.asarray(lat)
+    centre = rng.uniform(-0.5, 0.5, 2) * cc
+    order = np.argsort(np.linalg.norm(lat - centre, axis=1) + rng.uniform(0, 0.3 * cc, len(lat)))
+    chosen = list(order[:ncarbon])
+    rest = list(order[ncarbon:])
+
+    def nbrs(idx, pool):
+        d = np.linalg.norm(lat[pool] - lat[idx], axis=1)
+        return int(np.sum((d > 0.1) & (d < 1.1 * cc)))
+
+    for _ in range(4 * ncarbon):  # replace carbons with fewer than two C neighbours
+        bad = [k for k in chosen if nbrs(k, chosen) < 2]
+        if not bad:
+            break
+        chosen.remove(bad[0])
+        for r in rest:
+            if nbrs(r, chosen) >= 2:
+                chosen.append(r)
+                rest.remove(r)
+                break
+    cpos = lat[chosen]
+    sym, xyz, hxyz = [], [], []
+    for p in cpos:
+        d = np.linalg.norm(cpos - p, axis=1)
+        nb = cpos[(d > 0.1) & (d < cc * 1.1)]
+        sym.append("C")
+        xyz.append((p[0], p[1], 0.0))
+        if len(nb) == 2:
+            out = 2 * p - nb.sum(axis=0)
+            out = out / np.linalg.norm(out)
+            hxyz.append((p[0] + ch * out[0], p[1] + ch * out[1], 0.0))
+    sym += ["H"] * len(hxyz)
+    xyz += hxyz
+    return sym, np.asarray(xyz) * A2AU
+
+
+def random_hydrocarbon(rng, cmin=4, cmax=40):
+    """A planar ring (C <= 30, at random) or honeycomb sheet with a C count
+    drawn uniformly from [cmin, cmax], H on every perimeter carbon."""
+    nc = int(rng.integers(cmin, cmax + 1))
+    if nc <= 30 and rng.uniform() < 0.5:
+        return ring(nc, cc=1.39, ch=1.09)
+    return honeycomb_patch(nc, rng)
+
+
 # ----------------------------------------------------------------------------
 # densities
 # ----------------------------------------------------------------------------
@@ -200,6 +258,27 @@ WORKLOADS = {
     "c24h24": (lambda: ring(24, cc=1.39, ch=1.09), True, 84),
     "c96h24": (lambda: hex_flake(4, cc=1.42, ch=1.09), False, 324),
 }
+
+
+def make_batch_molecule(outdir, index, seed=77):
+    """Molecule ``index`` of the batched-scan generator: a random ring or sheet
+    (C 4..40) with the seeded basis recipe and nocc = number of C atoms x 3.5
+    (rounded).  Returns (mol_path, xdens_path, Molecule)."""
+    rng = np.random.default_rng([seed, index])
+    sym, xyz = random_hydrocarbon(rng)
+    mol = Molecule(sym, xyz, random_basis(rng, with_f=False))
+    os.makedirs(outdir, exist_ok=True)
+    tag = "batch_s%d_%03d" % (seed, index)
+    mol_path, xd_path = os.path.join(outdir, tag + ".mol"), os.path.join(outdir, tag + ".xdens")
+    if not (os.path.exists(mol_path) and os.path.exists(xd_path)):
+        nocc = max(1, int(round(3.5 * sym.count("C"))))
+        d, pert = random_densities(rng, mol.nbf, min(nocc, mol.nbf))
+        tmp = ".tmp%d" % os.getpid()
+        write_mol(mol_path + tmp, mol, "batch molecule %d seed %d" % (index, seed))
+        write_xdens(xd_path + tmp, [d] + pert)
+        os.replace(xd_path + tmp, xd_path)
+        os.replace(mol_path + tmp, mol_path)
+    return mol_path, xd_path, mol
 
 
 def make_workload(name, outdir, seed=2024, uhf=False):

@@ -77,6 +77,10 @@ int gg_set_screening(gg_ctx *ctx, double thrs);            /* takes effect on th
 int gg_set_flags(gg_ctx *ctx, int giao, int diamag, int paramag);  /* Advanced.GIAO/diamag/paramag */
 int gg_set_precision(gg_ctx *ctx, int mode);               /* GG_PREC_* */
 int gg_set_max_batch(gg_ctx *ctx, int64_t npts);           /* points per device pass (scratch size) */
+/* Split path: order the points into compact tiles and skip, per tile, the
+ * shells that are screened for all of its points (on by default; results do
+ * not change, only the work skipped). */
+int gg_set_tile_screening(gg_ctx *ctx, int enable);
 
 /* nbf: contracted Cartesian functions; turbomole: 1 if the MOL file has the
  * TURBOMOLE header (component order gtodefs.f90:108-123). */
@@ -132,9 +136,14 @@ double gg_au2si(double au);  /* au -> nA/T (globals.f90 au2si) */
 #define GG_PROF_TC 1     /* tcgen05 contraction + fused current-tensor epilogue */
 #define GG_PROF_FP64 2   /* plain FP64 path (basis, DGEMM, assembly) */
 #define GG_PROF_PLANE 3  /* plane quadrature reduction */
-#define GG_NPROF 4
+#define GG_PROF_ORDER 4  /* spatial ordering of the points and tile screening */
+#define GG_NPROF 5
 int gg_profile(gg_ctx *ctx, int enable);
 int gg_profile_read(const gg_ctx *ctx, double ms[GG_NPROF], int64_t launches[GG_NPROF], int64_t *total_kernels);
+/* GEMM work since gg_profile(ctx, 1), in blocks of 128 points x 224 columns x
+ * 64 (three fp16 products each): issued after tile screening, and the count
+ * a dense contraction would have issued. */
+int gg_profile_blocks(const gg_ctx *ctx, int64_t *issued, int64_t *dense);
 
 /* Evaluation without device allocation (no counterpart in the reference).
  * For callers that cannot let a library call cudaMalloc or cudaFree: host

@@ -158,6 +158,39 @@ def test_batching_is_invariant(c6h6):
     assert np.array_equal(a, b) and np.array_equal(a, c)
 
 
+def test_tile_screening_is_exact(c6h6):
+    """Tile screening only skips exact zeros: results are bit-identical with
+    and without it, for compact, scattered and far-away points."""
+    mp, xp, _ = c6h6
+    g = api.Gimic(mp, xp, screening=1e-8)
+    rng = np.random.default_rng(12)
+    ax = np.linspace(-12.0, 12.0, 24)
+    cube = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+    pts = np.vstack([cube, sample_points(g.atoms()[0], 2000, 300, 9.0, seed=13),
+                     rng.uniform(-60.0, 60.0, (500, 3))])
+    pts = pts[rng.permutation(len(pts))]
+    a = g.jtensor_batch(pts, rho=True, divj=True)
+    g.set_tile_screening(False)
+    b = g.jtensor_batch(pts, rho=True, divj=True)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    o = oracle.Oracle(mp, xp, screening=1e-8)
+    sel = rng.choice(len(pts), 800, replace=False)
+    assert rel_max_err(a[0][sel], o.jtensor(pts[sel])) <= TOL_SPLIT
+
+
+def test_profile_counts_screened_work(c6h6):
+    mp, xp, _ = c6h6
+    g = api.Gimic(mp, xp, screening=1e-8)
+    ax = np.linspace(-16.0, 16.0, 32)
+    cube = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+    g.profile(True)
+    g.jtensor_batch(cube)
+    issued, dense = g.profile_read()["gemm_blocks"]
+    g.profile(False)
+    assert 0 < issued < dense
+
+
 def test_device_and_host_buffers_agree(c6h6):
     torch = pytest.importorskip("torch")
     mp, xp, _ = c6h6
