@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--cpu-sample", type=int, default=8192)
+    ap.add_argument("--config", default="cube", choices=("cube", "scan"),
+                    help="cube: the C24H24 128^3 cube (default); scan: batched bond-current profile scans")
+    ap.add_argument("--molecules", type=int, default=16, help="molecules of the scan batch")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 65,536 cube points (a z-slab), two passes")
     ap.add_argument("--data", default=os.environ.get("GIMIC_GB300_DATA",
@@ -176,6 +179,60 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_scan(args):
+    """Batched uneven solves: random planar rings/sheets with 4-40 C (H on
+    every perimeter carbon, nbf 40-900), each with a bond-current profile
+    scan of 20-200 strips of 40x40 to 120x120 Gauss-Lobatto points (order
+    10), all strips of a molecule in one device pass."""
+    import torch
+
+    from gimic_gb300 import api, build, scan, synth
+
+    build.build()
+    rng = np.random.default_rng(5)
+    jobs = []
+    for i in range(args.molecules):
+        mp, xp, mol = synth.make_batch_molecule(os.path.join(args.data, "batch"), i)
+        nstrips = int(rng.integers(20, 201))
+        p = int(rng.choice(np.arange(40, 121, 10)))
+        jobs.append((mp, xp, mol, nstrips, p))
+    ctxs = [api.Gimic(mp, xp, screening=1e-8) for mp, xp, _, _, _ in jobs]
+    specs = []
+    for (mp, xp, mol, nstrips, p), g in zip(jobs, ctxs):
+        bond = scan.first_cc_bond(mol.symbols, mol.coords)
+        planes, bb = scan.profile_planes(mol.coords, bond=bond, start=-2.0, out=8.0, nstrips=nstrips, npts=(p, p),
+                                         order=10, quadrature="lobatto",
+                                         fixcoord=tuple(scan.plane_fixcoord(mol.coords, bond)))
+        g.set_magnet(bb)
+        specs.append(planes)
+    for g, planes in zip(ctxs, specs):  # warm-up: device tables, matrices, scratch
+        g.plane_integrals(planes[:2])
+    times, npl, npt = [], 0, 0
+    torch.cuda.synchronize()
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        for (mp, xp, mol, nstrips, p), g, planes in zip(jobs, ctxs, specs):
+            t0 = time.perf_counter()
+            g.plane_integrals(planes)
+            times.append(time.perf_counter() - t0)
+            npl += nstrips
+            npt += nstrips * p * p
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_all
+    nbfs = [m.nbf for _, _, m, _, _ in jobs]
+    line = {"metric": "plane-integrals/s (batched bond-current profile scans)", "value": npl / wall,
+            "unit": "planes/s", "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": wall / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16x3/f32/f64",
+            "data": "synthetic (seeded MOL/XDENS in the reference's formats)",
+            "config": {"workload": "%d random rings/sheets (C 4-40), profile scans of 20-200 Lobatto strips of "
+                                   "40^2-120^2 points" % len(jobs), "nbf_min": min(nbfs), "nbf_max": max(nbfs),
+                       "planes_per_step": npl // args.steps, "points_per_step": npt // args.steps},
+            "points_per_s": npt / wall,
+            "per_molecule_ms": {"p50": float(np.percentile(times, 50) * 1e3),
+                                "p99": float(np.percentile(times, 99) * 1e3)}}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_case(args):
     """65,536 cube points (every 32nd, so that they span the cube) through the
     split path twice; the second pass is the one to capture."""
@@ -203,6 +260,9 @@ def main():
         return
     if args.profile_case:
         run_profile_case(args)
+        return
+    if args.config == "scan":
+        run_scan(args)
         return
     import torch
 

@@ -128,7 +128,7 @@ struct gg_ctx {
 
   // scratch
   DevBuf a_hi, a_lo, inv_row, pts, jt, rho, divt, jv;
-  DevBuf sort_keys, sort_keys2, sort_idx, sort_perm, sort_temp, pts_sorted, tile_lists;
+  DevBuf sort_keys, sort_keys2, sort_idx, sort_perm, sort_temp, pts_sorted, tile_lists, tile_ord;
   DevBuf phi, gx, gy, gz, lap, w64;
   DevBuf plane_rows, plane_out;
   int* d_err = nullptr;
@@ -194,7 +194,7 @@ struct gg_ctx {
     tables_ready = false;
     for (DevBuf* b : {&b_fp64, &b_hi, &b_lo, &inv_col, &a_hi, &a_lo, &inv_row, &pts, &jt, &rho, &divt, &jv, &phi, &gx,
                       &gy, &gz, &lap, &w64, &plane_rows, &plane_out, &sort_keys, &sort_keys2, &sort_idx, &sort_perm,
-                      &sort_temp, &pts_sorted, &tile_lists})
+                      &sort_temp, &pts_sorted, &tile_lists, &tile_ord})
       b->release();
     if (d_err) cudaFree(d_err);
     d_err = nullptr;
@@ -233,6 +233,12 @@ struct gg_ctx {
     std::vector<int> f_shell = b.func_shell, f_ijk(b.nbf), sh_atom, sh_prim, sh_npf;
     std::vector<double> sh_rad2, p_xpd, p_ccd;
     std::vector<float> p_xp, p_xplo, p_cc;
+    std::vector<float2> sh_rad2_df, atom_df;
+    auto split = [](double x) {
+      const float h = static_cast<float>(x);
+      return make_float2(h, static_cast<float>(x - static_cast<double>(h)));
+    };
+    for (double v : axyz) atom_df.push_back(split(v));
     for (int mu = 0; mu < b.nbf; ++mu) {
       int e[3];
       gg::component_exponents(b.shells[f_shell[mu]].l, b.func_comp[mu], b.turbomole, e);
@@ -243,6 +249,7 @@ struct gg_ctx {
       sh_prim.push_back(static_cast<int>(p_xpd.size()));
       sh_npf.push_back(static_cast<int>(s.xp.size()));
       sh_rad2.push_back(s.radius * s.radius);
+      sh_rad2_df.push_back(split(s.radius * s.radius));
       for (size_t i = 0; i < s.xp.size(); ++i) {
         p_xpd.push_back(s.xp[i]);
         p_ccd.push_back(s.ncc[i]);
@@ -265,6 +272,8 @@ struct gg_ctx {
     if (e == cudaSuccess) e = upload(sh_prim, &d.sh_prim);
     if (e == cudaSuccess) e = upload(sh_npf, &d.sh_npf);
     if (e == cudaSuccess) e = upload(sh_rad2, &d.sh_rad2);
+    if (e == cudaSuccess) e = upload(sh_rad2_df, &d.sh_rad2_df);
+    if (e == cudaSuccess) e = upload(atom_df, &d.atom_df);
     if (e == cudaSuccess) e = upload(p_xp, &d.p_xp);
     if (e == cudaSuccess) e = upload(p_xplo, &d.p_xplo);
     if (e == cudaSuccess) e = upload(p_cc, &d.p_cc);
@@ -442,7 +451,7 @@ struct gg_ctx {
     const int* perm = nullptr;
     if (screen) {
       const int64_t ntiles = (n + gg::kBlockM - 1) / gg::kBlockM;
-      const size_t tb = gg::sort_temp_bytes(n);
+      const size_t tb = std::max(gg::sort_temp_bytes(n), gg::tile_order_temp_bytes(ntiles));
       e = sort_keys.reserve(n * sizeof(uint32_t));
       if (e == cudaSuccess) e = sort_keys2.reserve(n * sizeof(uint32_t));
       if (e == cudaSuccess) e = sort_idx.reserve(n * sizeof(int));
@@ -450,6 +459,7 @@ struct gg_ctx {
       if (e == cudaSuccess) e = sort_temp.reserve(std::max<size_t>(tb, 16));
       if (e == cudaSuccess) e = pts_sorted.reserve(static_cast<size_t>(n) * 3 * sizeof(double));
       if (e == cudaSuccess) e = tile_lists.reserve(static_cast<size_t>(ntiles) * stride * sizeof(int));
+      if (e == cudaSuccess) e = tile_ord.reserve(static_cast<size_t>(ntiles) * sizeof(int));
       if (e != cudaSuccess) return cuda_fail(e, "tile-screening scratch");
       double lo[3] = {0, 0, 0};
       for (const gg::Atom& a : basis.atoms)
@@ -461,9 +471,14 @@ struct gg_ctx {
                                    pts_sorted.as<double>(), st);
       if (e != cudaSuccess) return cuda_fail(e, "spatial ordering");
       gg::launch_tile_screen(dB, pts_sorted.as<double>(), n, tile_lists.as<int>(), st);
+      // heaviest tiles first; the key/index scratch of the point sort is reused
+      e = gg::launch_tile_order(tile_lists.as<int>(), ntiles, stride, sort_keys.as<uint32_t>(),
+                                sort_keys2.as<uint32_t>(), sort_idx.as<int>(), tile_ord.as<int>(), sort_temp.p, tb,
+                                st);
+      if (e != cudaSuccess) return cuda_fail(e, "tile ordering");
       prof_end(st, slot);
       if (prof.on && prof.d_blocks) gg::launch_tile_work(tile_lists.as<int>(), ntiles, stride, prof.d_blocks, st);
-      launches += 4;
+      launches += 6;
       tp = pts_sorted.as<double>();
       tiles = tile_lists.as<int>();
       perm = sort_perm.as<int>();
@@ -480,6 +495,7 @@ struct gg_ctx {
     ta.tiles = tiles;
     ta.tile_stride = stride;
     ta.perm = perm;
+    ta.tile_order = screen ? tile_ord.as<int>() : nullptr;
     if (prof.on) {
       const unsigned long long blocks = static_cast<unsigned long long>((n + gg::kBlockM - 1) / gg::kBlockM) *
                                         dB.nchunk * (dB.kpad / gg::kBlockK);
@@ -932,6 +948,65 @@ void gimic_get_gauss_points(double* a, double* b, int* npts, int* order, double*
 
 void mkgausspoints(double* a, double* b, int* npts, int* order, double* pts, double* wgts) {
   gimic_get_gauss_points(a, b, npts, order, pts, wgts);
+}
+
+// ---------------------------------------------------------------------------
+// Integration proposal network (no reference counterpart).  All arrays are
+// device arrays; the network is the 5 -> 64 -> 64 -> 1 SiLU MLP of k_mlp.cu.
+// ---------------------------------------------------------------------------
+int gg_mlp_nparams(void) { return gg::kMlpParams; }
+
+int gg_mlp_features(gg_ctx* ctx, const double* pts, const double* uv, int64_t n, float* feats, void* stream) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (n < 0 || (n > 0 && (!pts || !uv || !feats))) return ctx->fail(GG_EINVAL, "bad feature arrays");
+  if (n == 0) return GG_OK;
+  if (!is_device_ptr(pts) || !is_device_ptr(uv) || !is_device_ptr(feats))
+    return ctx->fail(GG_EINVAL, "gg_mlp_features takes device pointers only");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
+  int rc = ctx->build_tables();
+  if (rc) return rc;
+  gg::launch_mlp_features(ctx->dB, pts, uv, n, feats, static_cast<cudaStream_t>(stream));
+  ctx->launches += 1;
+  e = cudaGetLastError();
+  return e == cudaSuccess ? GG_OK : ctx->cuda_fail(e, "feature kernel launch");
+}
+
+static int mlp_check(const void* const* ptrs, int count) {
+  for (int i = 0; i < count; ++i)
+    if (ptrs[i] && !is_device_ptr(ptrs[i])) return GG_EINVAL;
+  return GG_OK;
+}
+
+int gg_mlp_grad(const float* params, const float* x, const float* target, int64_t n, float* grad, float* loss,
+                void* stream) {
+  if (n < 0 || n > INT32_MAX || !params || !grad || (n > 0 && (!x || !target))) return GG_EINVAL;
+  const void* p[] = {params, x, target, grad, loss};
+  if (mlp_check(p, 5)) return GG_EINVAL;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(grad, 0, sizeof(float) * gg::kMlpParams, st);
+  if (e == cudaSuccess && loss) e = cudaMemsetAsync(loss, 0, sizeof(float), st);
+  if (e != cudaSuccess) return GG_ECUDA;
+  gg::launch_mlp_train(params, x, target, static_cast<int>(n), grad, loss, st);
+  return cudaGetLastError() == cudaSuccess ? GG_OK : GG_ECUDA;
+}
+
+int gg_mlp_adam(float* params, const float* grad, float* m, float* v, float lr, float beta1, float beta2, float eps,
+                int step, void* stream) {
+  if (!params || !grad || !m || !v || step < 1) return GG_EINVAL;
+  const void* p[] = {params, grad, m, v};
+  if (mlp_check(p, 4)) return GG_EINVAL;
+  gg::launch_mlp_adam(params, grad, m, v, lr, beta1, beta2, eps, step, static_cast<cudaStream_t>(stream));
+  return cudaGetLastError() == cudaSuccess ? GG_OK : GG_ECUDA;
+}
+
+int gg_mlp_infer(const float* params, const float* x, int64_t n, float* y, void* stream) {
+  if (n < 0 || n > INT32_MAX || !params || (n > 0 && (!x || !y))) return GG_EINVAL;
+  const void* p[] = {params, x, y};
+  if (mlp_check(p, 3)) return GG_EINVAL;
+  gg::launch_mlp_infer(params, x, static_cast<int>(n), y, static_cast<cudaStream_t>(stream));
+  return cudaGetLastError() == cudaSuccess ? GG_OK : GG_ECUDA;
 }
 
 }  // extern "C"

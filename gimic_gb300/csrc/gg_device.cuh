@@ -23,6 +23,8 @@ struct DevBasis {
   const int* sh_prim;      // first primitive
   const int* sh_npf;
   const double* sh_rad2;   // squared screening radius
+  const float2* sh_rad2_df;  // the same as a double-float (hi, lo)
+  const float2* atom_df;     // natoms x 3 coordinates as double-floats (hi, lo)
   const float* p_xp;       // primitive exponents (fp32, rounded)
   const float* p_xplo;     // exponent residuals: p_xpd - p_xp (fp32)
   const float* p_cc;       // normalised contraction coefficients (fp32)
@@ -59,6 +61,67 @@ __device__ __forceinline__ float gauss_df(float ah, float al, float rh, float rl
   const float xe = fmaf(ah, rh, -xh);
   const float xl = xe + fmaf(ah, rl, al * rh);
   return expf(-xh) * (1.0f - xl);
+}
+
+// Double-float arithmetic (value = hi + lo, |lo| <= ulp(hi) / 2) in fp32.
+// The FP64 pipe of this GPU issues 64 times fewer operations per cycle than
+// the fp32 pipe, so per-function and per-shell geometry (r - R_A, |r - R_A|^2
+// and the screening test) is carried this way, with about 44 significant
+// bits, and fp64 is kept for per-point work.
+struct DFloat {
+  float h, l;
+};
+
+__device__ __forceinline__ DFloat df_split(double x) {
+  const float h = static_cast<float>(x);
+  return {h, static_cast<float>(x - static_cast<double>(h))};
+}
+
+// Knuth's two-sum: s + e == a + b exactly
+__device__ __forceinline__ DFloat two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+
+// Dekker's fast two-sum, |a| >= |b|
+__device__ __forceinline__ DFloat fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ DFloat df_sub(DFloat a, float2 b) {
+  const DFloat s = two_sum(a.h, -b.x);
+  return fast_two_sum(s.h, __fadd_rn(s.l, __fsub_rn(a.l, b.y)));
+}
+
+__device__ __forceinline__ DFloat df_add(DFloat a, DFloat b) {
+  const DFloat s = two_sum(a.h, b.h);
+  return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+
+// (h + l)^2 with the product error recovered by an fma
+__device__ __forceinline__ DFloat df_sqr(DFloat a) {
+  const float p = __fmul_rn(a.h, a.h);
+  const float e = fmaf(a.h, a.h, -p);
+  return fast_two_sum(p, fmaf(2.0f * a.h, a.l, e));
+}
+
+// a <= b for normalised double-floats
+__device__ __forceinline__ bool df_le(DFloat a, float2 b) { return a.h < b.x || (a.h == b.x && a.l <= b.y); }
+
+// Position of a point relative to atom a and its squared distance, from the
+// point as double-floats and the atom table.
+__device__ __forceinline__ DFloat atom_offset(const DFloat r[3], const float2* __restrict__ atom_df, int a, float s[3]) {
+  DFloat d2{0.f, 0.f};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const DFloat dc = df_sub(r[c], __ldg(atom_df + 3 * a + c));
+    s[c] = dc.h;
+    d2 = df_add(d2, df_sqr(dc));
+  }
+  return d2;
 }
 
 __device__ __forceinline__ int ipow_exp(int packed, int axis) { return (packed >> (4 * axis)) & 15; }

@@ -19,6 +19,7 @@ size_t basis_smem_bytes(int natoms, int nshells);
 const void* basis_split_kernel_ptr();  // for cudaFuncSetAttribute
 void launch_basis_split(const DevBasis& B, const double* pts, int64_t npts, __half* a_hi, __half* a_lo,
                         float* inv_scale, cudaStream_t st);
+// Tile-ordered points; only the K blocks active in each tile's screening list.
 void launch_basis_fp64(const DevBasis& B, const double* pts, int64_t npts, int64_t ld, double* phi, double* gx,
                        double* gy, double* gz, double* lap, cudaStream_t st);
 
@@ -48,6 +49,7 @@ struct TcArgs {
   const int* tiles = nullptr;  // per-tile active chunk / K-block lists (null: all)
   int tile_stride = 0;
   const int* perm = nullptr;   // output index of each (sorted) point (null: identity)
+  const int* tile_order = nullptr;  // tile processed by each CTA (null: CTA i -> tile i)
 };
 int tc_smem_bytes();
 
@@ -59,6 +61,11 @@ cudaError_t launch_spatial_order(const double* pts, int64_t n, const double lo[3
                                  double* pts_sorted, cudaStream_t st);
 void launch_tile_screen(const DevBasis& B, const double* pts_sorted, int64_t n, int* tiles, cudaStream_t st);
 void launch_tile_work(const int* tiles, int64_t ntiles, int stride, unsigned long long* acc, cudaStream_t st);
+// Tiles ordered by decreasing GEMM work (blocks = chunks x K blocks), so that
+// the heaviest tiles start first and the tail of the launch is short.
+size_t tile_order_temp_bytes(int64_t ntiles);
+cudaError_t launch_tile_order(const int* tiles, int64_t ntiles, int stride, uint32_t* work, uint32_t* work_sorted,
+                              int* ids, int* order, void* temp, size_t temp_bytes, cudaStream_t st);
 cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st);
 
 // Many planes at once: plane q owns points [pt_off, pt_off + p1*p2*p3) of jt
@@ -75,5 +82,17 @@ struct PlaneDesc {
 void launch_plane_batch(const double* jt, const double* pts, const double* w, const PlaneDesc* planes, int nplanes,
                         const int* row_plane, int64_t nrows, const double bb[3], double* row_out, double* out,
                         cudaStream_t st);
+
+// Integration proposal network (k_mlp.cu): 5 -> 64 -> 64 -> 1, SiLU.
+constexpr int kMlpIn = 5;
+constexpr int kMlpHidden = 64;
+constexpr int kMlpParams = kMlpHidden * kMlpIn + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;
+void launch_mlp_train(const float* params, const float* x, const float* t, int n, float* grad, float* loss,
+                      cudaStream_t st);
+void launch_mlp_adam(float* params, const float* grad, float* m, float* v, float lr, float b1, float b2, float eps, int step,
+                     cudaStream_t st);
+void launch_mlp_infer(const float* params, const float* x, int n, float* y, cudaStream_t st);
+void launch_mlp_features(const DevBasis& B, const double* pts, const double* uv, int64_t n, float* feats,
+                         cudaStream_t st);
 
 }  // namespace gg

@@ -20,45 +20,57 @@ namespace {
 
 constexpr int kWarps = 8;
 
-// Per-warp scratch: relative position of every atom (fp32, with the fp32
-// residual of |r - R|^2 in the 4th slot), its squared distance (fp64, for the
-// screening test) and the radial factor sum_p c_p exp(-a_p r^2) of every
-// shell (0 when screened).
+// Per-warp scratch: position of the point relative to every atom (fp32 x,
+// y, z), its squared distance as a double-float (hi, lo) and the radial
+// factor sum_p c_p exp(-a_p r^2) of every shell (0 when screened).  All
+// per-atom and per-shell arithmetic is fp32 / double-float: none of it runs
+// on the FP64 pipe.
 struct AtomScratch {
-  float* s;     // natoms x 4
-  double* d2;   // natoms
+  float* s;     // natoms x 4 (x, y, z, unused)
+  float2* d2;   // natoms
   float* rad;   // nshells
 };
 
 __device__ __forceinline__ AtomScratch atom_scratch(int warp, int natoms, int nshells) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* d2 = reinterpret_cast<double*>(smem_raw) + static_cast<size_t>(warp) * natoms;
-  float* s = reinterpret_cast<float*>(reinterpret_cast<double*>(smem_raw) + static_cast<size_t>(kWarps) * natoms) +
+  float2* d2 = reinterpret_cast<float2*>(smem_raw) + static_cast<size_t>(warp) * natoms;
+  float* s = reinterpret_cast<float*>(reinterpret_cast<float2*>(smem_raw) + static_cast<size_t>(kWarps) * natoms) +
              static_cast<size_t>(warp) * natoms * 4;
-  float* rad = reinterpret_cast<float*>(reinterpret_cast<double*>(smem_raw) + static_cast<size_t>(kWarps) * natoms) +
+  float* rad = reinterpret_cast<float*>(reinterpret_cast<float2*>(smem_raw) + static_cast<size_t>(kWarps) * natoms) +
                static_cast<size_t>(kWarps) * natoms * 4 + static_cast<size_t>(warp) * nshells;
   return {s, d2, rad};
 }
 
-__device__ __forceinline__ void fill_atoms(const DevBasis& B, const double r[3], AtomScratch sc, int lane) {
+// The point as double-floats: lanes 0-2 split one coordinate each and the
+// warp shares them.
+__device__ __forceinline__ void point_df(const double* __restrict__ pts, int64_t p, int lane, DFloat r[3]) {
+  DFloat mine{0.f, 0.f};
+  if (lane < 3) mine = df_split(pts[3 * p + lane]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    r[c].h = __shfl_sync(0xffffffffu, mine.h, c);
+    r[c].l = __shfl_sync(0xffffffffu, mine.l, c);
+  }
+}
+
+__device__ __forceinline__ void fill_atoms(const DevBasis& B, const DFloat r[3], AtomScratch sc, int lane) {
   for (int a = lane; a < B.natoms; a += 32) {
-    const double dx = r[0] - B.atom_xyz[3 * a], dy = r[1] - B.atom_xyz[3 * a + 1], dz = r[2] - B.atom_xyz[3 * a + 2];
-    const double d2 = dx * dx + dy * dy + dz * dz;
-    sc.d2[a] = d2;
-    sc.s[4 * a] = static_cast<float>(dx);
-    sc.s[4 * a + 1] = static_cast<float>(dy);
-    sc.s[4 * a + 2] = static_cast<float>(dz);
-    sc.s[4 * a + 3] = static_cast<float>(d2 - static_cast<double>(static_cast<float>(d2)));
+    float s3[3];
+    const DFloat d2 = atom_offset(r, B.atom_df, a, s3);
+    sc.d2[a] = make_float2(d2.h, d2.l);
+    sc.s[4 * a] = s3[0];
+    sc.s[4 * a + 1] = s3[1];
+    sc.s[4 * a + 2] = s3[2];
   }
   __syncwarp();
   for (int sh = lane; sh < B.nshells; sh += 32) {
     const int a = __ldg(B.sh_atom + sh);
+    const float2 d2 = sc.d2[a];
     float f1 = 0.f;
-    if (sc.d2[a] <= __ldg(B.sh_rad2 + sh)) {
-      const float rh = static_cast<float>(sc.d2[a]), rl = sc.s[4 * a + 3];
+    if (df_le(DFloat{d2.x, d2.y}, __ldg(B.sh_rad2_df + sh))) {
       const int p0 = __ldg(B.sh_prim + sh), np = __ldg(B.sh_npf + sh);
       for (int p = 0; p < np; ++p)
-        f1 += __ldg(B.p_cc + p0 + p) * gauss_df(__ldg(B.p_xp + p0 + p), __ldg(B.p_xplo + p0 + p), rh, rl);
+        f1 += __ldg(B.p_cc + p0 + p) * gauss_df(__ldg(B.p_xp + p0 + p), __ldg(B.p_xplo + p0 + p), d2.x, d2.y);
     }
     sc.rad[sh] = f1;
   }
@@ -90,7 +102,8 @@ __global__ void __launch_bounds__(kWarps * 32, 2) basis_split_kernel(DevBasis B,
   const int64_t p = static_cast<int64_t>(blockIdx.x) * kWarps + warp;
   if (p >= npts) return;
   AtomScratch sc = atom_scratch(warp, B.natoms, B.nshells);
-  const double r[3] = {pts[3 * p], pts[3 * p + 1], pts[3 * p + 2]};
+  DFloat r[3];
+  point_df(pts, p, lane, r);
   fill_atoms(B, r, sc, lane);
   const int npairs = B.kpad / 64;
   const bool cached = npairs <= kMaxPairs;
@@ -175,7 +188,7 @@ __global__ void __launch_bounds__(kWarps * 32) basis_fp64_kernel(DevBasis B, con
 const void* basis_split_kernel_ptr() { return reinterpret_cast<const void*>(&basis_split_kernel); }
 
 size_t basis_smem_bytes(int natoms, int nshells) {
-  return static_cast<size_t>(kWarps) * (natoms * (sizeof(double) + 4 * sizeof(float)) + nshells * sizeof(float));
+  return static_cast<size_t>(kWarps) * (natoms * (sizeof(float2) + 4 * sizeof(float)) + nshells * sizeof(float));
 }
 
 void launch_basis_split(const DevBasis& B, const double* pts, int64_t npts, __half* a_hi, __half* a_lo,

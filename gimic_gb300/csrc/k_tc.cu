@@ -76,7 +76,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const __grid_constant__ CUtensorMap tm_b_hi, const __grid_constant__ CUtensorMap tm_b_lo,
                     DevBasis Bs, const float* __restrict__ inv_row, const float* __restrict__ inv_col,
                     const double* __restrict__ pts, int64_t npts, Flags fl, Outputs out, int* err,
-                    const int* __restrict__ tiles, int tstride, const int* __restrict__ perm) {
+                    const int* __restrict__ tiles, int tstride, const int* __restrict__ perm,
+                    const int* __restrict__ tile_order) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                          ~static_cast<uintptr_t>(1023));
@@ -88,12 +89,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   int* tlist = reinterpret_cast<int*>(tmem_slot + 4);  // {#chunks, #kblocks, chunk ids, kblock ids}
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBlockM;
+  const int64_t tile = tile_order ? static_cast<int64_t>(tile_order[blockIdx.x]) : static_cast<int64_t>(blockIdx.x);
+  const int64_t m0 = tile * kBlockM;
   const int nchunk_all = Bs.nchunk, nkb_all = Bs.kpad / kBlockK;
   // active column chunks and K blocks of this tile (all of them without a
   // screening list)
   if (tiles) {
-    for (int i = threadIdx.x; i < tstride; i += blockDim.x) tlist[i] = tiles[static_cast<int64_t>(blockIdx.x) * tstride + i];
+    for (int i = threadIdx.x; i < tstride; i += blockDim.x) tlist[i] = tiles[tile * tstride + i];
   } else {
     for (int i = threadIdx.x; i < nchunk_all; i += blockDim.x) tlist[2 + i] = i;
     for (int i = threadIdx.x; i < nkb_all; i += blockDim.x) tlist[2 + nchunk_all + i] = i;
@@ -215,12 +217,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       r[1] = pts[3 * p + 1];
       r[2] = pts[3 * p + 2];
     }
+    const DFloat rdf[3] = {df_split(r[0]), df_split(r[1]), df_split(r[2])};
     float thi[kNDots], tlo[kNDots];
 #pragma unroll
     for (int i = 0; i < kNDots; ++i) thi[i] = tlo[i] = 0.f;
     int cur_shell = -1, cur_atom = -1;
-    float sx = 0.f, sy = 0.f, sz = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f, r2h = 0.f, r2l = 0.f;
-    double d2a = 0.0;
+    float sx = 0.f, sy = 0.f, sz = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
+    DFloat d2a{0.f, 0.f};
     bool on = false;
     const uint32_t lane_base = tmem_base + (static_cast<uint32_t>(q * 32) << 16);
     for (int ci = 0; ci < nchunk; ++ci) {
@@ -238,37 +241,36 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll 1
       for (int mu = mb; mu < me; ++mu) {
         const int u = mu - f0;
-        float v[kMats];
-#pragma unroll
-        for (int m = 0; m < kMats; ++m) tmem_ld1(tcol + m * kChunkF + u, v[m]);
         const int sh = __ldg(Bs.f_shell + mu);
         if (sh != cur_shell) {
           cur_shell = sh;
           const int a = __ldg(Bs.sh_atom + sh);
           if (a != cur_atom) {
             cur_atom = a;
-            const double dx = r[0] - Bs.atom_xyz[3 * a], dy = r[1] - Bs.atom_xyz[3 * a + 1],
-                         dz = r[2] - Bs.atom_xyz[3 * a + 2];
-            d2a = dx * dx + dy * dy + dz * dz;
-            sx = static_cast<float>(dx);
-            sy = static_cast<float>(dy);
-            sz = static_cast<float>(dz);
-            r2h = static_cast<float>(d2a);
-            r2l = static_cast<float>(d2a - static_cast<double>(r2h));
+            float s3[3];
+            d2a = atom_offset(rdf, Bs.atom_df, a, s3);
+            sx = s3[0];
+            sy = s3[1];
+            sz = s3[2];
           }
-          on = d2a <= __ldg(Bs.sh_rad2 + sh);
+          on = df_le(d2a, __ldg(Bs.sh_rad2_df + sh));
           f1 = f2 = f3 = 0.f;
           if (on) {
             const int p0 = __ldg(Bs.sh_prim + sh), np = __ldg(Bs.sh_npf + sh);
             for (int k = 0; k < np; ++k) {
               const float al = __ldg(Bs.p_xp + p0 + k);
-              const float e = __ldg(Bs.p_cc + p0 + k) * gauss_df(al, __ldg(Bs.p_xplo + p0 + k), r2h, r2l);
+              const float e = __ldg(Bs.p_cc + p0 + k) * gauss_df(al, __ldg(Bs.p_xplo + p0 + k), d2a.h, d2a.l);
               f1 += e;
               f2 += al * e;
               f3 += al * al * e;
             }
           }
         }
+        // functions screened for all 32 points of the warp contribute nothing
+        if (!__any_sync(0xffffffffu, on)) continue;
+        float v[kMats];
+#pragma unroll
+        for (int m = 0; m < kMats; ++m) tmem_ld1(tcol + m * kChunkF + u, v[m]);
         tmem_wait7(v);
         if (on) {
           float ph, gx, gy, gz, lp;
@@ -356,7 +358,8 @@ cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st)
   tc_fused_kernel<<<grid, kThreads, kSmemBytes, st>>>(
       *static_cast<const CUtensorMap*>(a.tmap_a_hi), *static_cast<const CUtensorMap*>(a.tmap_a_lo),
       *static_cast<const CUtensorMap*>(a.tmap_b_hi), *static_cast<const CUtensorMap*>(a.tmap_b_lo), B,
-      a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err, a.tiles, a.tile_stride, a.perm);
+      a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err, a.tiles, a.tile_stride, a.perm,
+      a.tile_order);
   return cudaGetLastError();
 }
 

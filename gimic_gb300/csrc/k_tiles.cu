@@ -135,6 +135,29 @@ void launch_tile_work(const int* tiles, int64_t ntiles, int stride, unsigned lon
 
 int tile_stride(const DevBasis& B) { return 2 + B.nchunk + B.kpad / kBlockK; }
 
+__global__ void tile_work_keys_kernel(const int* __restrict__ tiles, int64_t ntiles, int stride,
+                                      uint32_t* __restrict__ work, int* __restrict__ ids) {
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  work[t] = static_cast<uint32_t>(tiles[t * stride]) * static_cast<uint32_t>(tiles[t * stride + 1]);
+  ids[t] = static_cast<int>(t);
+}
+
+size_t tile_order_temp_bytes(int64_t ntiles) {
+  size_t bytes = 0;
+  cub::DeviceRadixSort::SortPairsDescending(nullptr, bytes, static_cast<const uint32_t*>(nullptr),
+                                            static_cast<uint32_t*>(nullptr), static_cast<const int*>(nullptr),
+                                            static_cast<int*>(nullptr), static_cast<int>(ntiles), 0, 20);
+  return bytes;
+}
+
+cudaError_t launch_tile_order(const int* tiles, int64_t ntiles, int stride, uint32_t* work, uint32_t* work_sorted,
+                              int* ids, int* order, void* temp, size_t temp_bytes, cudaStream_t st) {
+  tile_work_keys_kernel<<<static_cast<unsigned>((ntiles + 255) / 256), 256, 0, st>>>(tiles, ntiles, stride, work, ids);
+  return cub::DeviceRadixSort::SortPairsDescending(temp, temp_bytes, work, work_sorted, ids, order,
+                                                   static_cast<int>(ntiles), 0, 20, st);
+}
+
 size_t sort_temp_bytes(int64_t n) {
   size_t bytes = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, bytes, static_cast<const uint32_t*>(nullptr),

@@ -14,6 +14,35 @@ from . import grid as ggrid
 from . import inp as ginp
 
 
+def first_cc_bond(symbols, coords, cutoff=3.0):
+    """1-based atoms of the first carbon and its nearest carbon (a bond when
+    closer than ``cutoff`` Bohr)."""
+    c = np.asarray(coords, dtype=np.float64)
+    ci = [i for i, s in enumerate(symbols) if s.upper() == "C"]
+    a = ci[0]
+    d = [np.linalg.norm(c[j] - c[a]) if j != a else np.inf for j in ci]
+    b = ci[int(np.argmin(d))]
+    if d[int(np.argmin(d))] > cutoff:
+        raise ValueError("no C-C bond shorter than %g Bohr" % cutoff)
+    return a + 1, b + 1
+
+
+def plane_fixcoord(coords, bond):
+    """A fixcoord for a bond plane: the molecule's centroid, or, when the
+    centroid lies on the bond's line (the bond grid then has no "up"
+    direction, src/fgimic/grid.f90:236-241), the point 2 Bohr from the bond
+    midpoint in the molecular plane, perpendicular to the bond."""
+    c = np.asarray(coords, dtype=np.float64)
+    a1, a2 = c[bond[0] - 1], c[bond[1] - 1]
+    cen = c.mean(axis=0)
+    if np.linalg.norm(np.cross(a1 - cen, a2 - cen)) > 1e-3 * max(1.0, np.linalg.norm(a2 - a1) ** 2):
+        return cen
+    _, _, vt = np.linalg.svd(c - cen)
+    nrm = vt[-1]
+    perp = np.cross(nrm, a2 - a1)
+    return 0.5 * (a1 + a2) + 2.0 * perp / np.linalg.norm(perp)
+
+
 def strip_inputs(bond, start, out, nstrips, up=8.0, down=8.0, npts=(60, 60), order=10, quadrature="lobatto",
                  magnet_axis="z", fixpoint=None, fixcoord=(0.0, 0.0, 0.0), distance=None, coords=None):
     """gimic.inp texts for the strips of one profile (1-based atom numbers in
@@ -21,7 +50,9 @@ def strip_inputs(bond, start, out, nstrips, up=8.0, down=8.0, npts=(60, 60), ord
     if distance is None:
         a1, a2 = bond
         distance = 0.5 * float(np.linalg.norm(np.asarray(coords[a2 - 1]) - np.asarray(coords[a1 - 1])))
-    fix = ("fixpoint=%d" % fixpoint) if fixpoint is not None else ("fixcoord=[%r, %r, %r]" % tuple(fixcoord))
+    fix = (("fixpoint=%d" % fixpoint) if fixpoint is not None
+           else ("fixcoord=[%r, %r, %r]" % tuple(float(v) for v in fixcoord)))
+    distance, up, down, start, out = (float(v) for v in (distance, up, down, start, out))
     delta = (out - start) / float(nstrips)
     texts = []
     for k in range(nstrips):

@@ -134,7 +134,9 @@ def benzene():
 def honeycomb_patch(ncarbon, rng, cc=1.42, ch=1.09):
     """Planar sheet of exactly ``ncarbon`` C atoms cut from a honeycomb lattice
     around a random centre (jittered so that shapes vary), dangling carbons
-    pruned and refilled, one H on every perimeter carbon (two C neighbours)."""
+    pruned and refilled, one H on every perimeter carbon (two C neighbours).
+    Returns None when no carbon set of that size with at least two C
+    neighbours per carbon was found."""
     a = math.sqrt(3.0) * cc
     lat = []
     m = 8
@@ -164,6 +166,8 @@ def honeycomb_patch(ncarbon, rng, cc=1.42, ch=1.09):
                 chosen.append(r)
                 rest.remove(r)
                 break
+    if len(chosen) != ncarbon or any(nbrs(k, chosen) < 2 for k in chosen):
+        return None  # no such patch near this centre (e.g. 4, 5 or 7 carbons)
     cpos = lat[chosen]
     sym, xyz, hxyz = [], [], []
     for p in cpos:
@@ -186,7 +190,10 @@ def random_hydrocarbon(rng, cmin=4, cmax=40):
     nc = int(rng.integers(cmin, cmax + 1))
     if nc <= 30 and rng.uniform() < 0.5:
         return ring(nc, cc=1.39, ch=1.09)
-    return honeycomb_patch(nc, rng)
+    sheet = honeycomb_patch(nc, rng)
+    if sheet is None:
+        return ring(nc, cc=1.39, ch=1.09) if nc <= 30 else random_hydrocarbon(rng, cmin, cmax)
+    return sheet
 
 
 # ----------------------------------------------------------------------------

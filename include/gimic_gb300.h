@@ -145,6 +145,33 @@ int gg_profile_read(const gg_ctx *ctx, double ms[GG_NPROF], int64_t launches[GG_
  * a dense contraction would have issued. */
 int gg_profile_blocks(const gg_ctx *ctx, int64_t *issued, int64_t *dense);
 
+/* Integration proposal network (no counterpart in the reference, which
+ * integrates on fixed grids, src/fgimic/integral.f90:50-511).  A 5 -> 64 ->
+ * 64 -> 1 multilayer perceptron with SiLU activations predicts ln|j| at a
+ * point of an integration plane; the adaptive plane integrator refines a
+ * quadtree of Gauss-Lobatto panels where it predicts large, fast-varying
+ * currents.  Parameters are gg_mlp_nparams() fp32 values laid out as
+ * W1[64][5] b1[64] W2[64][64] b2[64] W3[64] b3.  Every array is device
+ * memory; non-device pointers are rejected with GG_EINVAL.
+ *
+ * gg_mlp_features: the five inputs for n points pts (n x 3, Bohr) with
+ *   in-plane coordinates uv (n x 2, Bohr): u/8, v/8, ln of the distances to
+ *   the nearest and second-nearest nucleus, and the local shell-exponent
+ *   density log10(1e-6 + sum_s sqrt(a_s) exp(-a_s d_s^2)) / 3 (a_s: smallest
+ *   exponent of shell s); feats is n x 5 fp32.
+ * gg_mlp_grad: gradient of the mean squared error (1/n) sum (y_i - t_i)^2
+ *   over the n samples x (n x 5) with targets t, written to grad (overwritten),
+ *   and the loss itself when loss is not null.
+ * gg_mlp_adam: one Adam step (bias-corrected, step counted from 1).
+ * gg_mlp_infer: predictions y (n) with bf16-rounded weights and activations. */
+int gg_mlp_nparams(void);
+int gg_mlp_features(gg_ctx *ctx, const double *pts, const double *uv, int64_t n, float *feats, void *stream);
+int gg_mlp_grad(const float *params, const float *x, const float *target, int64_t n, float *grad, float *loss,
+                void *stream);
+int gg_mlp_adam(float *params, const float *grad, float *m, float *v, float lr, float beta1, float beta2, float eps,
+                int step, void *stream);
+int gg_mlp_infer(const float *params, const float *x, int64_t n, float *y, void *stream);
+
 /* Evaluation without device allocation (no counterpart in the reference).
  * For callers that cannot let a library call cudaMalloc or cudaFree: host
  * applications that budget all device memory themselves, and time-critical

@@ -1,0 +1,202 @@
+"""Integration proposal network: the CPU oracle pinned by finite differences,
+the CUDA kernels (features, gradient, Adam, bf16 inference) against it, and
+the quadtree integrator against the uniform Gauss-Lobatto judge."""
+import numpy as np
+import pytest
+
+import mlp_oracle as MO
+
+
+def _rand_params(rng, scale=0.4):
+    return rng.standard_normal(MO.N_PARAMS) * scale
+
+
+# ---------------------------------------------------------------------------
+# CPU: the oracle itself
+# ---------------------------------------------------------------------------
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    p = _rand_params(rng)
+    x = rng.standard_normal((37, 5))
+    t = rng.standard_normal(37)
+    _, g = MO.loss_and_grad(p, x, t)
+    idx = rng.choice(MO.N_PARAMS, 60, replace=False)
+    idx = np.concatenate([idx, [0, 319, 320, 383, 384, 4479, 4480, 4543, 4544, 4607, 4608]])
+    h = 1e-6
+    for i in idx:
+        e = np.zeros_like(p)
+        e[i] = h
+        fd = (MO.loss_and_grad(p + e, x, t)[0] - MO.loss_and_grad(p - e, x, t)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(fd)), (i, fd, g[i])
+
+
+def test_oracle_layout_and_bf16():
+    assert MO.N_PARAMS == 4609
+    # bf16 keeps 7 fraction bits: the spacing above 1.0 is 2^-7
+    v = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, 1.0 + 3 * 2 ** -9, -3.14159, 0.0], dtype=np.float32)
+    r = MO.bf16(v)
+    assert r[0] == 1.0
+    assert r[1] == 1.0  # halfway: to the even neighbour 1.0
+    assert r[2] == np.float32(1.0 + 2 ** -6)  # halfway: to the even neighbour 1 + 2^-6
+    assert r[3] == np.float32(1.0 + 2 ** -7)  # nearest
+    assert r[4] == np.float32(-3.140625) and r[5] == 0.0
+
+
+def test_oracle_adam_first_step_is_signed_lr():
+    g = np.array([0.5, -2.0, 1e-3])
+    p, m, v = MO.adam(np.zeros(3), g, np.zeros(3), np.zeros(3), 0.01, 0.9, 0.999, 1e-12, 1)
+    assert np.allclose(p, -0.01 * np.sign(g), rtol=1e-6)
+
+
+def test_quadtree_panels_cover_the_plane():
+    from gimic_gb300 import proposal as P
+
+    reg = P.Region(np.zeros(3), [1, 0, 0], [0, 1, 0], [0, 0, 1], 16.0, 10.0, [8.0, 5.0, 0.0])
+    m = np.full((64, 64), 1e-6)
+    m[30:34, 20:28] = 1.0
+    pan = P.panels_from_mass(m, reg, dict(tau=2.0, max_depth=4, q_hi=10, q_lo=4, frac=0.02))
+    area = sum((x1 - x0) * (y1 - y0) for x0, x1, y0, y1, _ in pan)
+    assert abs(area - 160.0) < 1e-9
+    assert {q for *_, q in pan} == {4, 10}
+    # panels over the massive cells (x 7.5-8.5, y 3.125-4.375 Bohr) are
+    # refined to depth 4 (1 x 0.625 Bohr) and get the high order
+    hot = [p for p in pan if p[0] < 8.5 and p[1] > 7.5 and p[2] < 4.375 and p[3] > 3.125]
+    assert hot and all(p[4] == 10 and abs(p[1] - p[0] - 1.0) < 1e-12 for p in hot)
+    # nothing to refine: one coarse panel
+    pan = P.panels_from_mass(np.full((64, 64), 1e-9), reg, dict(tau=2.0))
+    assert len(pan) == 1 and pan[0][4] == P.DEFAULT_RULE["q_lo"]
+
+
+# ---------------------------------------------------------------------------
+# GPU: kernels against the oracle
+# ---------------------------------------------------------------------------
+def _cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    from gimic_gb300 import _lib
+    return torch, _lib.load()
+
+
+def _ptr(t):
+    import ctypes as C
+    return C.c_void_p(t.data_ptr())
+
+
+@pytest.mark.gpu
+def test_mlp_gradient_matches_oracle():
+    torch, L = _cuda()
+    rng = np.random.default_rng(1)
+    for n in (1, 31, 128, 1000, 4099):
+        p = _rand_params(rng, 0.25).astype(np.float32)
+        x = rng.standard_normal((n, 5)).astype(np.float32)
+        # targets away from the outputs, so that y - t is well conditioned
+        y0 = MO.forward(p.astype(np.float64), x.astype(np.float64))[0]
+        t = (y0 + np.where(rng.uniform(size=n) < 0.5, -1.0, 1.0) * rng.uniform(0.5, 2.0, n)).astype(np.float32)
+        loss_ref, g_ref = MO.loss_and_grad(p.astype(np.float64), x.astype(np.float64), t.astype(np.float64))
+        dp, dx, dt = (torch.as_tensor(a, device="cuda") for a in (p, x, t))
+        grad = torch.full((MO.N_PARAMS,), 7.0, device="cuda")  # overwritten, not accumulated
+        loss = torch.zeros(1, device="cuda")
+        assert L.gg_mlp_grad(_ptr(dp), _ptr(dx), _ptr(dt), n, _ptr(grad), _ptr(loss), None) == 0
+        torch.cuda.synchronize()
+        g = grad.cpu().numpy().astype(np.float64)
+        # fp32 kernel vs fp64 oracle: relative to the gradient's scale
+        assert np.max(np.abs(g - g_ref)) <= 2e-5 * np.max(np.abs(g_ref)), n
+        assert abs(float(loss) - loss_ref) <= 1e-5 * max(1.0, loss_ref)
+
+
+@pytest.mark.gpu
+def test_mlp_adam_matches_oracle():
+    torch, L = _cuda()
+    rng = np.random.default_rng(2)
+    p = _rand_params(rng)
+    m = rng.standard_normal(MO.N_PARAMS) * 1e-2
+    v = np.abs(rng.standard_normal(MO.N_PARAMS)) * 1e-4
+    g = rng.standard_normal(MO.N_PARAMS) * 1e-2
+    dp, dg, dm, dv = (torch.as_tensor(a.astype(np.float32), device="cuda") for a in (p, g, m, v))
+    p32, g32, m32, v32 = (a.astype(np.float32).astype(np.float64) for a in (p, g, m, v))
+    for step in (1, 2, 3):
+        assert L.gg_mlp_adam(_ptr(dp), _ptr(dg), _ptr(dm), _ptr(dv), 1e-3, 0.9, 0.999, 1e-8, step, None) == 0
+        p32, m32, v32 = MO.adam(p32, g32, m32, v32, 1e-3, 0.9, 0.999, 1e-8, step)
+    torch.cuda.synchronize()
+    # fp32 kernel vs fp64 oracle, tolerances relative to each array's scale
+    for got, ref in ((dp, p32), (dm, m32), (dv, v32)):
+        got = got.cpu().numpy().astype(np.float64)
+        assert np.max(np.abs(got - ref)) <= 1e-6 * np.max(np.abs(ref))
+
+
+@pytest.mark.gpu
+def test_mlp_bf16_inference_matches_oracle():
+    torch, L = _cuda()
+    rng = np.random.default_rng(3)
+    p = _rand_params(rng).astype(np.float32)
+    x = rng.standard_normal((5000, 5)).astype(np.float32)
+    dp, dx = torch.as_tensor(p, device="cuda"), torch.as_tensor(x, device="cuda")
+    y = torch.empty(5000, device="cuda")
+    assert L.gg_mlp_infer(_ptr(dp), _ptr(dx), 5000, _ptr(y), None) == 0
+    torch.cuda.synchronize()
+    ref = MO.infer_bf16(p, x)
+    full = MO.forward(p.astype(np.float64), x.astype(np.float64))[0]
+    err = np.abs(y.cpu().numpy() - ref)
+    # fp32 accumulation may flip the bf16 rounding of an activation now and then
+    assert np.median(err) < 1e-5 * np.max(np.abs(ref))
+    assert np.max(err) < 2e-2 * np.max(np.abs(ref))
+    # bf16 inference stays close to the fp32 network
+    assert np.max(np.abs(ref - full)) < 0.05 * np.max(np.abs(full))
+
+
+@pytest.mark.gpu
+def test_mlp_rejects_host_pointers_and_bad_sizes():
+    torch, L = _cuda()
+    p = torch.zeros(MO.N_PARAMS, device="cuda")
+    x = np.zeros((4, 5), dtype=np.float32)
+    y = torch.empty(4, device="cuda")
+    import ctypes as C
+    assert L.gg_mlp_infer(_ptr(p), C.c_void_p(x.ctypes.data), 4, _ptr(y), None) != 0
+    assert L.gg_mlp_infer(_ptr(p), _ptr(p), -1, _ptr(y), None) != 0
+    assert L.gg_mlp_adam(_ptr(p), _ptr(p), _ptr(p), _ptr(p), 1e-3, 0.9, 0.999, 1e-8, 0, None) != 0
+    assert L.gg_mlp_infer(_ptr(p), _ptr(p), 0, _ptr(y), None) == 0
+
+
+@pytest.mark.gpu
+def test_features_match_oracle(c6h6):
+    torch, L = _cuda()
+    from gimic_gb300 import api
+    from oracle import Oracle
+    from gimic_gb300 import proposal as P
+
+    mol, xdens, _ = c6h6
+    o = Oracle(mol, xdens)
+    xyz, _ = o.atoms()
+    sh = o.shells()
+    amin = np.array([sh["xp"][s, :sh["npf"][s]].min() for s in range(len(sh["atom"]))])
+    rng = np.random.default_rng(4)
+    pts = rng.uniform(-6, 6, (3000, 3))
+    pts[:3] = xyz[:3]  # on nuclei: distance floor
+    uv = rng.uniform(-8, 8, (3000, 2))
+    g = api.Gimic(mol, xdens)
+    f = P.features(g, pts, uv).cpu().numpy()
+    ref = MO.features(xyz, sh["atom"], amin, pts, uv)
+    assert np.allclose(f, ref, rtol=2e-6, atol=2e-6)
+
+
+@pytest.mark.gpu
+def test_training_reduces_loss_and_matches_oracle_step():
+    torch, L = _cuda()
+    from gimic_gb300 import proposal as P
+
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((20000, 5)).astype(np.float32)
+    t = (np.sin(2 * x[:, 0]) + x[:, 1] * x[:, 2] - 0.5 * x[:, 3] ** 2 + 0.3 * x[:, 4]).astype(np.float32)
+    net = P.ProposalNet(seed=3)
+    p0 = net.params.cpu().numpy().astype(np.float64)
+    dx, dt = torch.as_tensor(x, device="cuda"), torch.as_tensor(t, device="cuda")
+    # one step by hand against the oracle
+    tt = (t - t.mean()) / t.std(ddof=1)
+    _, g = net.loss_grad(dx[:4096], torch.as_tensor(tt[:4096].astype(np.float32), device="cuda"))
+    _, g_ref = MO.loss_and_grad(p0, x[:4096].astype(np.float64), tt[:4096].astype(np.float64))
+    assert np.max(np.abs(g.cpu().numpy() - g_ref)) <= 2e-5 * np.max(np.abs(g_ref))
+    hist = net.fit(dx, dt, epochs=20, batch=2048, lr=3e-3)
+    assert hist[-1] < 0.2 * hist[0], hist
+    pred = net.predict(dx).cpu().numpy()
+    assert np.sqrt(np.mean((pred - t) ** 2)) < 0.4 * t.std()
