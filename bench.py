@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--cpu-sample", type=int, default=8192)
-    ap.add_argument("--config", default="cube", choices=("cube", "scan"),
+    ap.add_argument("--config", default="cube", choices=("cube", "scan", "large", "proposal"),
                     help="cube: the C24H24 128^3 cube (default); scan: batched bond-current profile scans")
     ap.add_argument("--molecules", type=int, default=16, help="molecules of the scan batch")
     ap.add_argument("--profile-case", action="store_true",
@@ -233,6 +233,166 @@ def run_scan(args):
     print(json.dumps(line), flush=True)
 
 
+def run_large(args):
+    """The large single instance: C96H24 hexagonal flake (C-C 1.42 A, nbf
+    1560), 256^3 cube with 0.1 Bohr spacing (16.8 M points) streamed through
+    the split path in batches of 2^20 points; tensor, div j and density
+    written in fp32.  Accuracy against the FP64 oracle on 1024 cube points."""
+    import torch
+
+    from gimic_gb300 import api, build, synth
+
+    build.build()
+    mp, xp, mol = synth.make_workload("c96h24", args.data, seed=2024)
+    g = api.Gimic(mp, xp, screening=1e-8, precision="split16")
+    dev = torch.device("cuda", 0)
+    ax = torch.arange(256, dtype=torch.float64, device=dev) * 0.1 - 12.75
+    Z, Y, X = torch.meshgrid(ax, ax, ax, indexing="ij")
+    P = torch.stack([X.reshape(-1), Y.reshape(-1), Z.reshape(-1)], 1).contiguous()
+    del X, Y, Z
+    n = P.shape[0]
+    step = lambda: g.jtensor_batch(P, rho=True, divj=True, dtype=np.float32)  # noqa: E731
+    for _ in range(max(1, args.warmup)):
+        step()
+    stream = torch.cuda.current_stream(dev)
+    clocks = Clocks(0)
+    g.profile(False)
+    torch.cuda.synchronize(dev)
+    with clocks:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            out = step()
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = g.profile_read()["kernels"]
+    g.profile(True)
+    step()
+    prof = g.profile_read()
+    g.profile(False)
+    # accuracy on a sample of the cube against the FP64 oracle
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    idx = torch.as_tensor(np.random.default_rng(3).choice(n, 1024, replace=False), device=dev)
+    sub = P[idx].cpu().numpy()
+    ref = orc.Oracle(mp, xp, screening=1e-8).jtensor(sub)
+    got64 = g.jtensor_batch(sub)
+    got32 = out[0][idx].double().cpu().numpy()
+    err = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))  # noqa: E731
+    line = {"metric": "jtensor points/s, large single instance", "value": n / (ms * 1e-3), "unit": "points/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16x3/f32/f64",
+            "data": "synthetic (seeded MOL/XDENS in the reference's formats)",
+            "config": {"workload": "c96h24 256^3 cube (0.1 Bohr spacing), jtensor+divj+rho in fp32",
+                       "nbf": mol.nbf, "points_per_step": n, "batch_points": 1 << 20},
+            "gpu_launches": int(launches),
+            "kernel_ms_per_step": {k: prof[k][0] for k in ("order", "basis", "tc")},
+            "gemm_blocks_issued_fraction": prof["gemm_blocks"][0] / max(1, prof["gemm_blocks"][1]),
+            "rel_err_vs_fp64_oracle": {"fp64_outputs": err(got64, ref), "fp32_outputs": err(got32, ref),
+                                       "sample_points": 1024},
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def run_proposal(args):
+    """Learned-proposal adaptive plane integration.  Training: bond planes
+    of 32 generated rings/sheets (2 planes each) give 10^6 (point, |j|)
+    samples from the GPU path; the network is trained with the library's
+    forward/backward/Adam kernels.  Evaluation: one bond plane of each of 16
+    held-out molecules (another seed); the judge is the uniform 200 x 200
+    Gauss-Lobatto grid (order 10), and the uniform baseline is the smallest
+    uniform grid (order-10 panels) from which every finer one stays within
+    0.01 nA/T of the judge."""
+    import torch
+
+    from gimic_gb300 import api, build, scan, synth
+    from gimic_gb300 import proposal as P
+
+    build.build()
+    dev = torch.device("cuda", 0)
+
+    def planes(seed, n, per):
+        out = []
+        for i in range(n):
+            mp, xp, mol = synth.make_batch_molecule(os.path.join(args.data, "proposal"), i, seed=seed)
+            g = api.Gimic(mp, xp, screening=1e-8)
+            c = mol.coords
+            ci = [k for k, s_ in enumerate(mol.symbols) if s_ == "C"]
+            bonds = [(a + 1, b + 1) for a in ci for b in ci if b > a and np.linalg.norm(c[a] - c[b]) < 3.0]
+            rng = np.random.default_rng([seed, i, 7])
+            pick = [bonds[0]] + [bonds[k] for k in rng.choice(len(bonds), min(per - 1, len(bonds)), replace=False)]
+            for bd in pick[:per]:
+                reg, bb = P.Region.bond_plane(c, bd)
+                out.append((g, reg, bb, mol.nbf))
+        return out
+
+    train, held = planes(1077, 32, 2), planes(2077, 16, 1)
+    rng = np.random.default_rng(5)
+    nsamp = 1000000
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    F, T = [], []
+    for g, reg, bb, _ in train:
+        g.set_magnet(bb)
+        f, t = P.sample_plane(g, reg, nsamp // len(train), rng)
+        F.append(f)
+        T.append(t)
+    x, t = torch.cat(F), torch.cat(T)
+    torch.cuda.synchronize(dev)
+    t_samp = time.perf_counter() - t0
+    net = P.ProposalNet(seed=1)
+    epochs = 20
+    t0 = time.perf_counter()
+    hist = net.fit(x, t, epochs=epochs, batch=4096, lr=3e-3)
+    torch.cuda.synchronize(dev)
+    t_train = time.perf_counter() - t0
+    net0 = P.ProposalNet(seed=1)  # the same network untrained
+    net0.t_mean, net0.t_std, net0.box = net.t_mean, net.t_std, net.box
+    # bf16 inference throughput on the training features
+    net.infer(x[:65536])
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(10):
+        net.infer(x)
+    torch.cuda.synchronize(dev)
+    infer_s = (time.perf_counter() - t0) / 10
+    rows = []
+    t_adapt = 0.0
+    for g, reg, bb, nbf in held:
+        g.set_magnet(bb)
+        judge = P.integrate_uniform(g, reg, 200)
+        upts, _ = P.uniform_points_to_reach(g, reg, judge)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        res = P.integrate_adaptive(g, net, reg)
+        torch.cuda.synchronize(dev)
+        t_adapt += time.perf_counter() - t0
+        res0 = P.integrate_adaptive(g, net0, reg, min_inside=0.0)
+        rows.append({"nbf": nbf, "judge_nAT": judge, "uniform_points": upts, "adaptive_points": res["points"],
+                     "adaptive_err_nAT": res["current"] - judge, "method": res["method"],
+                     "untrained_points": res0["points"], "untrained_err_nAT": res0["current"] - judge})
+    u = sum(r["uniform_points"] or 40000 for r in rows)
+    a = sum(r["adaptive_points"] for r in rows)
+    errs = [abs(r["adaptive_err_nAT"]) for r in rows]
+    line = {"metric": "points evaluated to reach 0.01 nA/T: uniform grid / learned adaptive (16 held-out planes)",
+            "value": u / a, "unit": "x fewer points", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 train / bf16 infer",
+            "data": "synthetic (seeded rings/sheets, C 4-40)",
+            "config": {"workload": "bond planes (height +-8, width out 8 Bohr), judge 200x200 Gauss-Lobatto order 10",
+                       "train_planes": len(train), "held_out_planes": len(held), "samples": int(x.shape[0]),
+                       "rule": P.DEFAULT_RULE},
+            "uniform_points_total": u, "adaptive_points_total": a,
+            "adaptive_max_err_nAT": max(errs), "planes_within_0.01": int(sum(e <= 0.01 for e in errs)),
+            "untrained_max_err_nAT": max(abs(r["untrained_err_nAT"]) for r in rows),
+            "untrained_planes_within_0.01": int(sum(abs(r["untrained_err_nAT"]) <= 0.01 for r in rows)),
+            "sample_generation_s": t_samp, "training_s": t_train, "training_samples_per_s": epochs * x.shape[0] / t_train,
+            "final_loss": hist[-1], "inference_points_per_s": x.shape[0] / infer_s,
+            "adaptive_ms_per_plane": t_adapt / len(held) * 1e3, "planes": rows}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_case(args):
     """65,536 cube points (every 32nd, so that they span the cube) through the
     split path twice; the second pass is the one to capture."""
@@ -263,6 +423,12 @@ def main():
         return
     if args.config == "scan":
         run_scan(args)
+        return
+    if args.config == "large":
+        run_large(args)
+        return
+    if args.config == "proposal":
+        run_proposal(args)
         return
     import torch
 

@@ -148,32 +148,35 @@ class Gimic:
         return out
 
     # ---- evaluation -----------------------------------------------------
-    def jtensor_batch(self, points, rho=False, divj=False, stream=None):
+    def jtensor_batch(self, points, rho=False, divj=False, stream=None, dtype=np.float64):
         """Current tensors t(m,b) = dj_m/dB_b at points (N,3), returned as
         (N,9) column-major (index m + 3b); optionally the density (N,) and
         the tensor divergence (N,3).  numpy in -> numpy out; CUDA torch
-        tensors in -> CUDA torch tensors out (no host round trip)."""
+        tensors in -> CUDA torch tensors out (no host round trip).  dtype
+        float32 stores the outputs in fp32 (gg_jtensor_batch_f32)."""
+        f32 = np.dtype(dtype) == np.float32
+        fn = self._L.gg_jtensor_batch_f32 if f32 else self._L.gg_jtensor_batch
         if _is_cuda(points):
             p = points.to(torch.float64).contiguous().reshape(-1, 3)
             n = p.shape[0]
-            jt = torch.empty((n, 9), dtype=torch.float64, device=p.device)
-            rh = torch.empty(n, dtype=torch.float64, device=p.device) if rho else None
-            dv = torch.empty((n, 3), dtype=torch.float64, device=p.device) if divj else None
+            tdt = torch.float32 if f32 else torch.float64
+            jt = torch.empty((n, 9), dtype=tdt, device=p.device)
+            rh = torch.empty(n, dtype=tdt, device=p.device) if rho else None
+            dv = torch.empty((n, 3), dtype=tdt, device=p.device) if divj else None
             st = stream if stream is not None else torch.cuda.current_stream(p.device).cuda_stream
-            rc = self._L.gg_jtensor_batch(self._h, C.c_void_p(p.data_ptr()), n, C.c_void_p(jt.data_ptr()),
-                                          C.c_void_p(rh.data_ptr()) if rh is not None else None,
-                                          C.c_void_p(dv.data_ptr()) if dv is not None else None,
-                                          C.c_void_p(st))
+            rc = fn(self._h, C.c_void_p(p.data_ptr()), n, C.c_void_p(jt.data_ptr()),
+                    C.c_void_p(rh.data_ptr()) if rh is not None else None,
+                    C.c_void_p(dv.data_ptr()) if dv is not None else None, C.c_void_p(st))
         else:
             p = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
             n = p.shape[0]
-            jt = np.zeros((n, 9))
-            rh = np.zeros(n) if rho else None
-            dv = np.zeros((n, 3)) if divj else None
-            rc = self._L.gg_jtensor_batch(self._h, C.c_void_p(p.ctypes.data), n, C.c_void_p(jt.ctypes.data),
-                                          C.c_void_p(rh.ctypes.data) if rh is not None else None,
-                                          C.c_void_p(dv.ctypes.data) if dv is not None else None,
-                                          C.c_void_p(stream) if stream else None)
+            ndt = np.float32 if f32 else np.float64
+            jt = np.zeros((n, 9), dtype=ndt)
+            rh = np.zeros(n, dtype=ndt) if rho else None
+            dv = np.zeros((n, 3), dtype=ndt) if divj else None
+            rc = fn(self._h, C.c_void_p(p.ctypes.data), n, C.c_void_p(jt.ctypes.data),
+                    C.c_void_p(rh.ctypes.data) if rh is not None else None,
+                    C.c_void_p(dv.ctypes.data) if dv is not None else None, C.c_void_p(stream) if stream else None)
         check(rc, self._h)
         out = [jt]
         if rho:

@@ -230,7 +230,9 @@ struct gg_ctx {
     const gg::Basis& b = basis;
     std::vector<double> axyz;
     for (const gg::Atom& a : b.atoms) axyz.insert(axyz.end(), a.coord, a.coord + 3);
-    std::vector<int> f_shell = b.func_shell, f_ijk(b.nbf), sh_atom, sh_prim, sh_npf;
+    std::vector<int> f_shell = b.func_shell, f_ijk(b.nbf), sh_atom, sh_prim, sh_npf, sh_l, sh_f0, sh_ncomp;
+    std::vector<int4> sh_pack;
+    std::vector<float2> sh_bound, p_bound;
     std::vector<double> sh_rad2, p_xpd, p_ccd;
     std::vector<float> p_xp, p_xplo, p_cc;
     std::vector<float2> sh_rad2_df, atom_df;
@@ -244,7 +246,19 @@ struct gg_ctx {
       gg::component_exponents(b.shells[f_shell[mu]].l, b.func_comp[mu], b.turbomole, e);
       f_ijk[mu] = e[0] | (e[1] << 4) | (e[2] << 8);
     }
+    // functions of every shell must be contiguous and in shell order (the
+    // shell-blocked basis kernel walks them so)
+    sh_f0.assign(b.shells.size(), -1);
+    sh_ncomp.assign(b.shells.size(), 0);
+    for (int mu = 0; mu < b.nbf; ++mu) {
+      const int s = f_shell[mu];
+      if (sh_f0[s] < 0) sh_f0[s] = mu;
+      if (sh_f0[s] + sh_ncomp[s] != mu || (s > 0 && sh_f0[s - 1] > sh_f0[s]))
+        return fail(GG_EUNSUPPORTED, "basis functions are not grouped by shell");
+      ++sh_ncomp[s];
+    }
     for (const gg::Shell& s : b.shells) {
+      sh_l.push_back(s.l);
       sh_atom.push_back(s.atom);
       sh_prim.push_back(static_cast<int>(p_xpd.size()));
       sh_npf.push_back(static_cast<int>(s.xp.size()));
@@ -257,6 +271,19 @@ struct gg_ctx {
         p_xplo.push_back(static_cast<float>(s.xp[i] - static_cast<double>(static_cast<float>(s.xp[i]))));
         p_cc.push_back(static_cast<float>(s.ncc[i]));
       }
+    }
+    // per-shell and per-primitive records of the shell-blocked basis kernel;
+    // the row-scale bound is |phi| <= d^l npf max_p |c_p| exp(-a_p d^2)
+    for (size_t si = 0; si < b.shells.size(); ++si) {
+      const gg::Shell& sh = b.shells[si];
+      sh_pack.push_back(make_int4(sh.atom, sh_f0[si],
+                                  sh_ncomp[si] | (static_cast<int>(sh.xp.size()) << 8) | (sh.l << 16), sh_prim[si]));
+      sh_bound.push_back(make_float2(static_cast<float>(sh.radius * sh.radius * (1.0 + 1e-4)),
+                                     static_cast<float>(sh.l)));
+      for (size_t i = 0; i < sh.xp.size(); ++i)
+        p_bound.push_back(make_float2(static_cast<float>(sh.xp[i] * 1.4426950408889634 * (1.0 - 1e-6)),
+                                      static_cast<float>(std::log2(std::max(std::fabs(sh.ncc[i]), 1e-300)) +
+                                                         std::log2(static_cast<double>(sh.xp.size())) + 1e-4)));
     }
     gg::DevBasis d{};
     d.nbf = b.nbf;
@@ -271,6 +298,12 @@ struct gg_ctx {
     if (e == cudaSuccess) e = upload(sh_atom, &d.sh_atom);
     if (e == cudaSuccess) e = upload(sh_prim, &d.sh_prim);
     if (e == cudaSuccess) e = upload(sh_npf, &d.sh_npf);
+    if (e == cudaSuccess) e = upload(sh_l, &d.sh_l);
+    if (e == cudaSuccess) e = upload(sh_f0, &d.sh_f0);
+    if (e == cudaSuccess) e = upload(sh_ncomp, &d.sh_ncomp);
+    if (e == cudaSuccess) e = upload(sh_pack, &d.sh_pack);
+    if (e == cudaSuccess) e = upload(sh_bound, &d.sh_bound);
+    if (e == cudaSuccess) e = upload(p_bound, &d.p_bound);
     if (e == cudaSuccess) e = upload(sh_rad2, &d.sh_rad2);
     if (e == cudaSuccess) e = upload(sh_rad2_df, &d.sh_rad2_df);
     if (e == cudaSuccess) e = upload(atom_df, &d.atom_df);
@@ -284,12 +317,6 @@ struct gg_ctx {
       e = cudaMalloc(&d_err, sizeof(int));
       if (e == cudaSuccess) e = cudaMemset(d_err, 0, sizeof(int));
       if (e != cudaSuccess) return cuda_fail(e, "allocating error word");
-    }
-    const size_t smem = gg::basis_smem_bytes(d.natoms, d.nshells);
-    if (smem > 48 * 1024) {
-      e = cudaFuncSetAttribute(gg::basis_split_kernel_ptr(), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               static_cast<int>(smem));
-      if (e != cudaSuccess) return cuda_fail(e, "basis kernel shared memory");
     }
     dB = d;
     tables_ready = true;
@@ -407,10 +434,13 @@ struct gg_ctx {
 
   // One device-resident batch: pts, outputs all device pointers.
   int run_batch(const double* d_pts, int64_t n, double* d_jt, double* d_rho, double* d_divt, cudaStream_t st) {
+    return run_batch(d_pts, n, gg::Outputs{d_jt, d_rho, d_divt}, st);
+  }
+
+  int run_batch(const double* d_pts, int64_t n, gg::Outputs out, cudaStream_t st) {
     if (n <= 0) return GG_OK;
-    if (d_divt && !(flags.giao && flags.dia && flags.para))
+    if ((out.divt || out.divt32) && !(flags.giao && flags.dia && flags.para))
       return fail(GG_EUNSUPPORTED, "div j needs GIAO, diamagnetic and paramagnetic terms on");
-    gg::Outputs out{d_jt, d_rho, d_divt};
     cudaError_t e;
     if (precision == GG_PREC_FP64) {
       const int nb = basis.nbf;
@@ -483,13 +513,14 @@ struct gg_ctx {
       tiles = tile_lists.as<int>();
       perm = sort_perm.as<int>();
     }
-    prof_begin(GG_PROF_BASIS, st, &slot);
-    gg::launch_basis_split(dB, tp, n, a_hi.as<__half>(), a_lo.as<__half>(), inv_row.as<float>(), st);
-    prof_end(st, slot);
     CUtensorMap tma_hi, tma_lo;
     if (!encode_fp16_2d(&tma_hi, a_hi.p, n, dB.kpad, gg::kBlockM) ||
         !encode_fp16_2d(&tma_lo, a_lo.p, n, dB.kpad, gg::kBlockM))
       return fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
+    prof_begin(GG_PROF_BASIS, st, &slot);
+    e = gg::launch_basis_tile(dB, &tma_hi, &tma_lo, tp, n, tiles, stride, inv_row.as<float>(), st);
+    prof_end(st, slot);
+    if (e != cudaSuccess) return cuda_fail(e, "basis kernel launch");
     gg::TcArgs ta{&tma_hi, &tma_lo, &tm_b_hi, &tm_b_lo, inv_row.as<float>(), inv_col.as<float>(),
                   tp,      n,       flags,    out,      d_err};
     ta.tiles = tiles;
@@ -528,7 +559,8 @@ struct gg_ctx {
     return GG_OK;
   }
 
-  int jtensor(const double* p, int64_t n, double* jto, double* rhoo, double* divo, cudaStream_t st) {
+  template <typename T>
+  int jtensor(const double* p, int64_t n, T* jto, T* rhoo, T* divo, cudaStream_t st) {
     if (n < 0 || (n > 0 && !p)) return fail(GG_EINVAL, "bad point array");
     if (n == 0) return GG_OK;
     int rc = prepare();
@@ -549,38 +581,51 @@ struct gg_ctx {
         if (e != cudaSuccess) return cuda_fail(e, "copying points");
         dp = pts.as<double>();
       }
-      double *dj = jto ? jto + 9 * off : nullptr, *dr = rhoo ? rhoo + off : nullptr,
-             *dd = divo ? divo + 3 * off : nullptr;
+      T *dj = jto ? jto + 9 * off : nullptr, *dr = rhoo ? rhoo + off : nullptr, *dd = divo ? divo + 3 * off : nullptr;
       if (!dev_out) {
         if (jto) {
-          if ((e = jt.reserve(static_cast<size_t>(m) * 9 * sizeof(double))) != cudaSuccess)
+          if ((e = jt.reserve(static_cast<size_t>(m) * 9 * sizeof(T))) != cudaSuccess)
             return cuda_fail(e, "output scratch");
-          dj = jt.as<double>();
+          dj = jt.as<T>();
         }
         if (rhoo) {
-          if ((e = rho.reserve(static_cast<size_t>(m) * sizeof(double))) != cudaSuccess)
+          if ((e = rho.reserve(static_cast<size_t>(m) * sizeof(T))) != cudaSuccess)
             return cuda_fail(e, "output scratch");
-          dr = rho.as<double>();
+          dr = rho.as<T>();
         }
         if (divo) {
-          if ((e = divt.reserve(static_cast<size_t>(m) * 3 * sizeof(double))) != cudaSuccess)
+          if ((e = divt.reserve(static_cast<size_t>(m) * 3 * sizeof(T))) != cudaSuccess)
             return cuda_fail(e, "output scratch");
-          dd = divt.as<double>();
+          dd = divt.as<T>();
         }
       }
-      rc = run_batch(dp, m, dj, dr, dd, st);
+      gg::Outputs out{nullptr, nullptr, nullptr};
+      set_outputs(&out, dj, dr, dd);
+      rc = run_batch(dp, m, out, st);
       if (rc) return rc;
       if (!dev_out) {
-        if (jto) e = cudaMemcpyAsync(jto + 9 * off, dj, m * 9 * sizeof(double), cudaMemcpyDeviceToHost, st);
-        if (rhoo && e == cudaSuccess) e = cudaMemcpyAsync(rhoo + off, dr, m * sizeof(double), cudaMemcpyDeviceToHost, st);
+        e = cudaSuccess;
+        if (jto) e = cudaMemcpyAsync(jto + 9 * off, dj, m * 9 * sizeof(T), cudaMemcpyDeviceToHost, st);
+        if (rhoo && e == cudaSuccess) e = cudaMemcpyAsync(rhoo + off, dr, m * sizeof(T), cudaMemcpyDeviceToHost, st);
         if (divo && e == cudaSuccess)
-          e = cudaMemcpyAsync(divo + 3 * off, dd, m * 3 * sizeof(double), cudaMemcpyDeviceToHost, st);
+          e = cudaMemcpyAsync(divo + 3 * off, dd, m * 3 * sizeof(T), cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) return cuda_fail(e, "copying results");
         // host staging buffers are reused by the next batch
         if ((rc = check_device_error(st))) return rc;
       }
     }
     return check_device_error(st);
+  }
+
+  static void set_outputs(gg::Outputs* o, double* j, double* r, double* d) {
+    o->jt = j;
+    o->rho = r;
+    o->divt = d;
+  }
+  static void set_outputs(gg::Outputs* o, float* j, float* r, float* d) {
+    o->jt32 = j;
+    o->rho32 = r;
+    o->divt32 = d;
   }
 };
 
@@ -701,6 +746,13 @@ int gg_atoms(const gg_ctx* ctx, double* coords, double* charges) {
 }
 
 int gg_jtensor_batch(gg_ctx* ctx, const double* pts, int64_t n, double* jt, double* rho, double* divt, void* stream) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  return ctx->jtensor(pts, n, jt, rho, divt, static_cast<cudaStream_t>(stream));
+}
+
+int gg_jtensor_batch_f32(gg_ctx* ctx, const double* pts, int64_t n, float* jt, float* rho, float* divt,
+                         void* stream) {
   if (!ctx) return GG_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   return ctx->jtensor(pts, n, jt, rho, divt, static_cast<cudaStream_t>(stream));
@@ -1089,11 +1141,12 @@ extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t 
   c += align256(static_cast<size_t>(n) * kpad * sizeof(__half));
   float* inv_row = reinterpret_cast<float*>(c);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  gg::launch_basis_split(ctx->dB, pts, n, a_hi, a_lo, inv_row, st);
   CUtensorMap tma_hi, tma_lo;
   if (!encode_fp16_2d(&tma_hi, a_hi, n, ctx->dB.kpad, gg::kBlockM) ||
       !encode_fp16_2d(&tma_lo, a_lo, n, ctx->dB.kpad, gg::kBlockM))
     return ctx->fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
+  e = gg::launch_basis_tile(ctx->dB, &tma_hi, &tma_lo, pts, n, nullptr, 0, inv_row, st);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "basis kernel launch");
   gg::TcArgs ta{&tma_hi, &tma_lo, &ctx->tm_b_hi, &ctx->tm_b_lo, inv_row, ctx->inv_col.as<float>(),
                 pts,     n,       ctx->flags,     gg::Outputs{jt, rho, divt}, ctx->d_err};
   e = gg::launch_tc_fused(ctx->dB, ta, st);

@@ -22,12 +22,18 @@ struct DevBasis {
   const int* sh_atom;
   const int* sh_prim;      // first primitive
   const int* sh_npf;
+  const int* sh_l;         // angular momentum
+  const int* sh_f0;        // first function (functions of a shell are contiguous)
+  const int* sh_ncomp;     // number of Cartesian components
   const double* sh_rad2;   // squared screening radius
   const float2* sh_rad2_df;  // the same as a double-float (hi, lo)
   const float2* atom_df;     // natoms x 3 coordinates as double-floats (hi, lo)
   const float* p_xp;       // primitive exponents (fp32, rounded)
   const float* p_xplo;     // exponent residuals: p_xpd - p_xp (fp32)
   const float* p_cc;       // normalised contraction coefficients (fp32)
+  const int4* sh_pack;     // {atom, first function, ncomp | npf << 8 | l << 16, first primitive}
+  const float2* sh_bound;  // {squared radius (fp32, rounded up), l}
+  const float2* p_bound;   // {a log2(e) (rounded down), log2 |c| + log2(npf of the shell) (rounded up)}
   const double* p_xpd;     // same in fp64
   const double* p_ccd;
 };
@@ -37,12 +43,30 @@ struct Flags {
   int giao, dia, para;
 };
 
-// Per-point outputs; any pointer may be null.
+// Per-point outputs; any pointer may be null.  The fp32 set receives the
+// same values rounded once from fp64 (for large grids stored in fp32).
 struct Outputs {
   double* jt;    // N x 9, column-major 3x3 (t(m,b) at m + 3b)
   double* rho;   // N
   double* divt;  // N x 3: sum_m d/dm t(m,b)
+  float* jt32 = nullptr;
+  float* rho32 = nullptr;
+  float* divt32 = nullptr;
 };
+
+__device__ __forceinline__ void store_outputs(const Outputs& out, int64_t o, const double ct[9], double rho,
+                                              const double dv[3]) {
+  if (out.jt)
+    for (int i = 0; i < 9; ++i) out.jt[9 * o + i] = ct[i];
+  if (out.rho) out.rho[o] = rho;
+  if (out.divt)
+    for (int i = 0; i < 3; ++i) out.divt[3 * o + i] = dv[i];
+  if (out.jt32)
+    for (int i = 0; i < 9; ++i) out.jt32[9 * o + i] = static_cast<float>(ct[i]);
+  if (out.rho32) out.rho32[o] = static_cast<float>(rho);
+  if (out.divt32)
+    for (int i = 0; i < 3; ++i) out.divt32[3 * o + i] = static_cast<float>(dv[i]);
+}
 
 // Split-FP16 GEMM geometry
 constexpr int kChunkF = 32;              // functions per column chunk

@@ -15,11 +15,15 @@ namespace gg {
 // with W0 = phi^T D, WC_d = phi^T C_d, Q_b = phi^T P_b and s = r - R_atom.
 constexpr int kNDots = 37;
 
-size_t basis_smem_bytes(int natoms, int nshells);
-const void* basis_split_kernel_ptr();  // for cudaFuncSetAttribute
-void launch_basis_split(const DevBasis& B, const double* pts, int64_t npts, __half* a_hi, __half* a_lo,
-                        float* inv_scale, cudaStream_t st);
-// Tile-ordered points; only the K blocks active in each tile's screening list.
+// Shell-blocked basis evaluation for the split-FP16 point operand
+// (k_basis_tile.cu): one thread per point, the row scale from a log-domain
+// bound, K blocks staged in shared memory and written with TMA tensor stores
+// through the point operand's own tensor maps; with tile lists, inactive K
+// blocks are skipped.
+int basis_tile_smem_bytes();
+cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* tm_lo, const double* pts,
+                              int64_t npts, const int* tiles, int stride, float* inv_scale, cudaStream_t st);
+// phi, grad phi and the Laplacian in fp64 for the plain FP64 path.
 void launch_basis_fp64(const DevBasis& B, const double* pts, int64_t npts, int64_t ld, double* phi, double* gx,
                        double* gy, double* gz, double* lap, cudaStream_t st);
 

@@ -1,0 +1,232 @@
+// Shell-blocked basis evaluation for the split-FP16 point operand.
+//
+// One CTA handles one tile of 128 consecutive points (the M tile of the
+// tensor-core contraction), one thread per point.  All threads walk the
+// shells in the same order (uniform control flow, shell data broadcast), so
+// each thread evaluates the radial factor of a shell once and then its
+// Cartesian components (bfeval.f90:81-122 with the per-shell screening of
+// basis.f90:118-136).  Geometry is double-float fp32 (no FP64 pipe work per
+// shell).
+//
+// The row's power-of-two scale has to be known before the first value is
+// written, so a first pass computes an upper bound of max_mu |phi_mu| in the
+// log domain, without exponentials:
+//   |x^i y^j z^k sum_p c_p e^{-a_p d^2}| <= d^l npf max_p |c_p| e^{-a_p d^2}.
+// The scale puts that bound just under 2^14.  When the bound exceeds the
+// true row maximum by 2^k, the values whose fp16 lo part is subnormal are
+// stored with an absolute error of at most 2^(k-38) times the row maximum;
+// k stays below 4 for the seeded bases (checked against the oracle's basis
+// values), i.e. far below 1e-9 of the maximum.
+//
+// Values go to a shared-memory tile laid out in the 128-byte swizzle that the
+// contraction's TMA loads expect, and every finished 128 x 64 K block is
+// written to HBM with a TMA tensor store.  With tile screening on, K blocks
+// that are inactive for the tile (all their shells out of range for every
+// point) are neither staged nor stored: the contraction never reads them.
+#include <cuda.h>
+
+#include "gg_device.cuh"
+#include "gg_kernels.h"
+
+namespace gg {
+
+namespace {
+
+constexpr int kTileThreads = kBlockM;                   // one thread per point of the tile
+constexpr int kStageBytes = kBlockM * kBlockK * 2;      // one 128 x 64 fp16 tile: 16 KiB
+constexpr int kBufBytes = 2 * kStageBytes;              // hi + lo
+constexpr int kTileSmem = kBufBytes + 1024;             // one buffer + alignment slack
+
+__device__ __forceinline__ void tma_store_2d(const void* tmap, const void* src, int c0, int c1) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(tmap)),
+               "r"(smem_u32(src)), "r"(c0), "r"(c1)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// wait until no committed group still reads shared memory
+__device__ __forceinline__ void bulk_wait_read_0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// byte offset of column pair (col, col + 1) of row `row` in a 128B-swizzled
+// 128 x 64 fp16 tile: 16-byte chunk c of row r sits at chunk c ^ (r & 7)
+__device__ __forceinline__ uint32_t swz(int row, int col) {
+  const int byte = col * 2;
+  return static_cast<uint32_t>(row * 128 + ((((byte >> 4) ^ (row & 7)) << 4) | (byte & 15)));
+}
+
+struct Stager {
+  unsigned char* buf;  // current buffer: hi tile then lo tile
+  int row;
+  __half ph, pl;       // pending even column
+  __device__ __forceinline__ void put_pair(int col, __half h0, __half l0, __half h1, __half l1) {
+    const uint32_t o = swz(row, col);
+    *reinterpret_cast<__half2*>(buf + o) = __halves2half2(h0, h1);
+    *reinterpret_cast<__half2*>(buf + kStageBytes + o) = __halves2half2(l0, l1);
+  }
+};
+
+}  // namespace
+
+__global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_constant__ CUtensorMap tm_hi,
+                                                                  const __grid_constant__ CUtensorMap tm_lo,
+                                                                  DevBasis B, const double* __restrict__ pts,
+                                                                  int64_t npts, const int* __restrict__ tiles,
+                                                                  int stride, float* __restrict__ inv_scale) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int row = threadIdx.x;
+  const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBlockM;
+  const int64_t p = min(m0 + row, npts - 1);  // rows past the end compute a copy; the TMA store clips them
+  const int nkb = B.kpad / kBlockK;
+
+  // active K blocks of this tile (all when no screening lists are given)
+  uint64_t kb_on = ~0ull;
+  if (tiles) {
+    const int* tl = tiles + blockIdx.x * static_cast<int64_t>(stride);
+    const int nk = tl[1];
+    const int* kl = tl + 2 + B.nchunk;
+    kb_on = 0;
+    for (int i = 0; i < nk; ++i) kb_on |= 1ull << kl[i];
+  }
+
+  DFloat r[3];
+  for (int c = 0; c < 3; ++c) r[c] = df_split(pts[3 * p + c]);
+
+  // ---- pass 1: log2 of an upper bound of |phi| over the row -------------
+  float lb = -INFINITY;
+  {
+    int cur_atom = -1;
+    float d2 = 0.f, hl2d = 0.f;
+    for (int sh = 0; sh < B.nshells; ++sh) {
+      const int a = __ldg(&B.sh_pack[sh].x);
+      if (a != cur_atom) {
+        cur_atom = a;
+        const float dx = r[0].h - __ldg(&B.atom_df[3 * a].x), dy = r[1].h - __ldg(&B.atom_df[3 * a + 1].x),
+                    dz = r[2].h - __ldg(&B.atom_df[3 * a + 2].x);
+        d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        hl2d = 0.5f * __log2f(fmaxf(d2, 1e-30f));
+      }
+      const float2 bd = __ldg(B.sh_bound + sh);  // radius^2 (rounded up), l
+      if (d2 > bd.x) continue;                   // screened
+      const int4 pk = __ldg(B.sh_pack + sh);
+      const int np = (pk.z >> 8) & 0xff;
+      float m = -INFINITY;
+      for (int k = 0; k < np; ++k) {
+        const float2 pb = __ldg(B.p_bound + pk.w + k);  // a log2 e, log2 |c| + log2 npf
+        m = fmaxf(m, fmaf(-pb.x, d2, pb.y));
+      }
+      lb = fmaxf(lb, bd.y > 0.f ? fmaf(bd.y, hl2d, m) : m);
+    }
+  }
+  float scale = 1.f;
+  if (lb > -INFINITY) {
+    // bound < 2^e with e = floor(lb + margin) + 1; scale = 2^(14 - e)
+    const int e = static_cast<int>(floorf(lb + 0.05f)) + 1;
+    scale = ldexpf(1.f, max(-120, min(120, 14 - e)));
+  }
+  if (m0 + row < npts) inv_scale[m0 + row] = 1.f / scale;
+
+  // ---- pass 2: values, staged per K block and stored with TMA -------------
+  Stager st{base, row, __float2half_rn(0.f), __float2half_rn(0.f)};
+  int kb = 0;
+  bool active = (kb_on & 1ull) != 0;
+  auto flush = [&](int k) {  // all threads: the K block k is complete in the buffer
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store_2d(&tm_hi, base, k * kBlockK, static_cast<int>(m0));
+      tma_store_2d(&tm_lo, base + kStageBytes, k * kBlockK, static_cast<int>(m0));
+      bulk_commit();
+      bulk_wait_read_0();  // the buffer may be written again
+    }
+    __syncthreads();
+  };
+  auto advance_to = [&](int k) {  // close K blocks before k (zeros never need staging: they are written in order)
+    while (kb < k) {
+      if (active) flush(kb);
+      ++kb;
+      active = kb < nkb && ((kb_on >> kb) & 1ull);
+    }
+  };
+  auto emit = [&](int mu, float v) {
+    const int k = mu >> 6;
+    if (k != kb) advance_to(k);
+    if (!active) return;
+    const __half h = __float2half_rn(v);
+    const __half l = __float2half_rn(v - __half2float(h));
+    if ((mu & 1) == 0) {
+      st.ph = h;
+      st.pl = l;
+    } else {
+      st.put_pair((mu & 63) - 1, st.ph, st.pl, h, l);
+    }
+  };
+  {
+    int cur_atom = -1;
+    float px[4] = {1.f, 0.f, 0.f, 0.f}, py[4] = {1.f, 0.f, 0.f, 0.f}, pz[4] = {1.f, 0.f, 0.f, 0.f};
+    DFloat d2{0.f, 0.f};
+    for (int sh = 0; sh < B.nshells; ++sh) {
+      const int4 pk = __ldg(B.sh_pack + sh);  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
+      const int mu0 = pk.y, ncomp = pk.z & 0xff, np = (pk.z >> 8) & 0xff;
+      const int k_first = mu0 >> 6, k_last = (mu0 + ncomp - 1) >> 6;
+      // skip whole shells whose K blocks are inactive for the tile
+      if (!((kb_on >> k_first) & 1ull) && !((kb_on >> k_last) & 1ull)) continue;
+      if (pk.x != cur_atom) {
+        cur_atom = pk.x;
+        float s3[3];
+        d2 = atom_offset(r, B.atom_df, pk.x, s3);
+        px[1] = s3[0];
+        py[1] = s3[1];
+        pz[1] = s3[2];
+        px[2] = px[1] * px[1];
+        py[2] = py[1] * py[1];
+        pz[2] = pz[1] * pz[1];
+        px[3] = px[2] * px[1];
+        py[3] = py[2] * py[1];
+        pz[3] = pz[2] * pz[1];
+      }
+      float f1 = 0.f;
+      if (df_le(d2, __ldg(B.sh_rad2_df + sh))) {
+        for (int k = 0; k < np; ++k)
+          f1 += __ldg(B.p_cc + pk.w + k) * gauss_df(__ldg(B.p_xp + pk.w + k), __ldg(B.p_xplo + pk.w + k), d2.h, d2.l);
+        f1 *= scale;
+      }
+      for (int c = 0; c < ncomp; ++c) {
+        const int ijk = __ldg(B.f_ijk + mu0 + c);
+        const int i = ijk & 15, j = (ijk >> 4) & 15, k = (ijk >> 8) & 15;  // each <= 3
+        const float xi = i == 0 ? 1.f : (i == 1 ? px[1] : (i == 2 ? px[2] : px[3]));
+        const float yj = j == 0 ? 1.f : (j == 1 ? py[1] : (j == 2 ? py[2] : py[3]));
+        const float zk = k == 0 ? 1.f : (k == 1 ? pz[1] : (k == 2 ? pz[2] : pz[3]));
+        emit(mu0 + c, xi * yj * zk * f1);
+      }
+    }
+    // padding columns nbf .. kpad-1 of the last K block are zero
+    for (int mu = B.nbf; mu < B.kpad; ++mu) emit(mu, 0.f);
+    advance_to(nkb);
+  }
+  if (threadIdx.x == 0) bulk_wait_all();
+}
+
+int basis_tile_smem_bytes() { return kTileSmem; }
+
+cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* tm_lo, const double* pts,
+                              int64_t npts, const int* tiles, int stride, float* inv_scale, cudaStream_t st) {
+  if (npts <= 0) return cudaSuccess;
+  if (B.kpad / kBlockK > 64) return cudaErrorInvalidValue;  // K-block mask is 64 bits
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(basis_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const unsigned grid = static_cast<unsigned>((npts + kBlockM - 1) / kBlockM);
+  basis_tile_kernel<<<grid, kTileThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
+                                                            *static_cast<const CUtensorMap*>(tm_lo), B, pts, npts,
+                                                            tiles, stride, inv_scale);
+  return cudaGetLastError();
+}
+
+}  // namespace gg

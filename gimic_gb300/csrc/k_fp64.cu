@@ -117,11 +117,7 @@ __global__ void __launch_bounds__(256) assemble_fp64_kernel(DevBasis Bs, const d
   if (lane == 0) {
     double ct[9], dv[3];
     combine_point(d, r, fl, ct, dv);
-    if (out.jt)
-      for (int i = 0; i < 9; ++i) out.jt[9 * p + i] = ct[i];
-    if (out.rho) out.rho[p] = d[0];
-    if (out.divt)
-      for (int b = 0; b < 3; ++b) out.divt[3 * p + b] = dv[b];
+    store_outputs(out, p, ct, d[0], dv);
   }
 }
 

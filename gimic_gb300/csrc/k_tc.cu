@@ -330,11 +330,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       double ct[9], dv[3];
       combine_point(tot, r, fl, ct, dv);
       const int64_t o = perm ? static_cast<int64_t>(perm[p]) : p;  // caller's point order
-      if (out.jt)
-        for (int i = 0; i < 9; ++i) out.jt[9 * o + i] = ct[i];
-      if (out.rho) out.rho[o] = tot[0];
-      if (out.divt)
-        for (int i = 0; i < 3; ++i) out.divt[3 * o + i] = dv[i];
+      store_outputs(out, o, ct, tot[0], dv);
     }
   }
 done:

@@ -27,7 +27,7 @@ from . import grid as ggrid
 from . import inp as ginp
 
 N_IN = 5
-J_FLOOR = 1e-9  # au; targets are ln(|j| + J_FLOOR)
+J_FLOOR = 1e-6  # au; targets are ln(|j| + J_FLOOR): the network need not resolve currents far below the plane's
 
 
 def _ptr(t):
@@ -133,7 +133,7 @@ def features(gimic, pts, uv):
 
 
 class ProposalNet:
-    """5 -> 64 -> 64 -> 1 SiLU network predicting ln(|j| + 1e-9) (|j| in au).
+    """5 -> 64 -> 64 -> 1 SiLU network predicting ln(|j| + 1e-6) (|j| in au).
 
     Weights are fp32 on the device; targets are standardised with the
     training set's mean and deviation.  ``box`` is the per-feature range seen
@@ -187,7 +187,7 @@ class ProposalNet:
 
     # -- training and prediction ---------------------------------------------
     def fit(self, x, target, epochs=20, batch=4096, lr=3e-3, lr_min=1e-4, seed=0):
-        """Train on features x (N, 5) and targets ln(|j| + 1e-9) (N,), both
+        """Train on features x (N, 5) and targets ln(|j| + 1e-6) (N,), both
         device tensors.  Returns the mean training loss of each epoch."""
         target = target.to(torch.float32)
         self.t_mean = float(target.mean())
@@ -216,7 +216,7 @@ class ProposalNet:
         return hist
 
     def predict(self, x):
-        """ln(|j| + 1e-9) predicted for features x (device tensor)."""
+        """ln(|j| + 1e-6) predicted for features x (device tensor)."""
         return self.infer(x) * self.t_std + self.t_mean
 
     def in_box(self, x, margin=0.1):
@@ -253,9 +253,9 @@ class ProposalNet:
 # ---------------------------------------------------------------------------
 # training data produced by the method itself
 # ---------------------------------------------------------------------------
-def sample_plane(gimic, region, n, rng, core_frac=0.5):
-    """n points on the plane with their features and targets ln(|j| + 1e-9)
-    (|j| from the GPU path).  A fraction ``core_frac`` is drawn within 3 Bohr
+def sample_plane(gimic, region, n, rng, core_frac=0.5, floor=J_FLOOR):
+    """n points on the plane with their features and targets ln(|j| + floor)
+    (|j| in au, from the GPU path).  A fraction ``core_frac`` is drawn within 3 Bohr
     of the molecular plane, where the current lives; the rest uniformly."""
     nc = int(n * core_frac)
     xy = np.empty((n, 2))
@@ -267,17 +267,188 @@ def sample_plane(gimic, region, n, rng, core_frac=0.5):
     pts = torch.as_tensor(region.points(xy), device=dev)
     f = features(gimic, pts, torch.as_tensor(region.uv(xy), device=dev))
     j = gimic.jvector_batch(pts)
-    t = torch.log(torch.linalg.norm(j, dim=1) + J_FLOOR).to(torch.float32)
+    t = torch.log(torch.linalg.norm(j, dim=1) + floor).to(torch.float32)
     return f, t
 
 
 # ---------------------------------------------------------------------------
 # adaptive integration
 # ---------------------------------------------------------------------------
-DEFAULT_RULE = {"tau": 0.25, "q_hi": 10, "q_lo": 4, "frac": 0.02, "max_depth": 4, "lattice": 64}
+# Calibrated on 64 bond planes of 32 training molecules (see bench.py
+# --config proposal): the cheapest rule with every training plane within
+# 0.01 nA/T of its 200 x 200 uniform judge.
+DEFAULT_RULE = {"mode": "mass", "kappa_u": 2.0, "kappa_v": 2.0, "tau": 1.0, "q_hi": 7, "q_lo": 4, "frac": 0.02,
+                "max_depth": 1, "n0u": 3, "n0v": 3, "lattice": 96, "tau_s": 1e-3}
 
 
-def predict_mass(net, gimic, region, lattice=64):
+class AxisMap:
+    """Smooth monotone map x(t) = c + s sinh(t) of t in [t0, t1] onto [0, L]:
+    Gauss-Lobatto nodes equally spaced in t crowd around x = c, on the
+    length scale s; s = None is the identity (t = x)."""
+
+    def __init__(self, L, c=None, s=None):
+        self.L, self.c, self.s = float(L), c, s
+        if s is None:
+            self.t0, self.t1 = 0.0, self.L
+        else:
+            self.t0, self.t1 = float(np.arcsinh((0.0 - c) / s)), float(np.arcsinh((self.L - c) / s))
+
+    def x(self, t):
+        t = np.asarray(t, dtype=np.float64)
+        if self.s is None:
+            return t
+        return np.clip(self.c + self.s * np.sinh(t), 0.0, self.L)
+
+    def nodes(self, ta, tb, q):
+        """Gauss-Lobatto nodes of order q on [ta, tb] mapped to x, with the
+        weights times dx/dt."""
+        t, w = api.gauss_data(0.0, tb - ta, q, q, "lobatto")
+        t = t + ta
+        if self.s is None:
+            return t, w
+        return self.x(t), w * self.s * np.cosh(t)
+
+
+def _weighted_quantiles(centres, w, qs):
+    cw = np.cumsum(w)
+    if cw[-1] <= 0.0:
+        return [float(np.quantile(centres, q)) for q in qs]
+    return [float(np.interp(q * cw[-1], cw, centres)) for q in qs]
+
+
+def estimate_maps(mass, region, rule=None):
+    """The two axis maps from the predicted mass lattice: centred on the
+    mass-weighted median of each marginal, with s = kappa times the
+    interquartile range of that marginal (at least 0.25 Bohr)."""
+    r = dict(DEFAULT_RULE, **(rule or {}))
+    G = mass.shape[0]
+    maps = []
+    for axis, L, kappa in ((0, region.lx, r["kappa_u"]), (1, region.ly, r["kappa_v"])):
+        marg = np.abs(mass).sum(axis=1 - axis)
+        centres = (np.arange(G) + 0.5) / G * L
+        q25, q50, q75 = _weighted_quantiles(centres, marg, (0.25, 0.5, 0.75))
+        maps.append(AxisMap(L, q50, max(kappa * (q75 - q25), 0.25)) if kappa is not None else AxisMap(L))
+    return maps
+
+
+class _MassTable:
+    """Predicted mass of any rectangle [x0, x1] x [y0, y1] from the lattice,
+    by interpolating its 2-D cumulative sums."""
+
+    def __init__(self, mass, region):
+        G = mass.shape[0]
+        self.S = np.zeros((G + 1, G + 1))
+        self.S[1:, 1:] = mass.cumsum(0).cumsum(1)
+        self.gx = np.linspace(0.0, region.lx, G + 1)
+        self.gy = np.linspace(0.0, region.ly, G + 1)
+
+    def _cum(self, x, y):
+        fx = np.interp(x, self.gx, np.arange(len(self.gx)))
+        fy = np.interp(y, self.gy, np.arange(len(self.gy)))
+        i, j = min(int(fx), len(self.gx) - 2), min(int(fy), len(self.gy) - 2)
+        ax, ay = fx - i, fy - j
+        S = self.S
+        return ((1 - ax) * (1 - ay) * S[i, j] + ax * (1 - ay) * S[i + 1, j] + (1 - ax) * ay * S[i, j + 1]
+                + ax * ay * S[i + 1, j + 1])
+
+    def __call__(self, x0, x1, y0, y1):
+        return self._cum(x1, y1) - self._cum(x0, y1) - self._cum(x1, y0) + self._cum(x0, y0)
+
+
+def propose_panels(mass, region, rule=None):
+    """The proposal: axis maps from the predicted mass, then a quadtree in the
+    mapped coordinates.  The mapped domain starts as n0u x n0v panels; a
+    panel is split in four while its predicted current mass exceeds ``tau``
+    (nA/T) and it is shallower than ``max_depth``; a leaf gets ``q_hi``
+    Gauss-Lobatto points per axis when its mass exceeds frac * tau, else
+    ``q_lo``.  Returns (map_u, map_v, [(ta, tb, wa, wb, q)])."""
+    r = dict(DEFAULT_RULE, **(rule or {}))
+    mu, mv = estimate_maps(mass, region, r)
+    table = _MassTable(mass, region)
+    tu = np.linspace(mu.t0, mu.t1, int(r["n0u"]) + 1)
+    tv = np.linspace(mv.t0, mv.t1, int(r["n0v"]) + 1)
+    stack = [(tu[i], tu[i + 1], tv[j], tv[j + 1], 0) for i in range(len(tu) - 1) for j in range(len(tv) - 1)]
+    panels = []
+    while stack:
+        ta, tb, wa, wb, d = stack.pop()
+        m = table(float(mu.x(ta)), float(mu.x(tb)), float(mv.x(wa)), float(mv.x(wb)))
+        if m > r["tau"] and d < r["max_depth"]:
+            tm, wm = 0.5 * (ta + tb), 0.5 * (wa + wb)
+            stack += [(ta, tm, wa, wm, d + 1), (tm, tb, wa, wm, d + 1), (ta, tm, wm, wb, d + 1),
+                      (tm, tb, wm, wb, d + 1)]
+        else:
+            panels.append((ta, tb, wa, wb, r["q_hi"] if m > r["frac"] * r["tau"] else r["q_lo"]))
+    return mu, mv, panels
+
+
+def predict_at(net, gimic, region, xy):
+    """Predicted |j| (au) at in-plane points xy (N, 2)."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    f = features(gimic, torch.as_tensor(region.points(xy), device=dev), torch.as_tensor(region.uv(xy), device=dev))
+    return np.exp(net.predict(f).double().cpu().numpy())
+
+
+def _panel_rule(mu, mv, ta, tb, wa, wb, q):
+    x, wx = mu.nodes(ta, tb, q)
+    y, wy = mv.nodes(wa, wb, q)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    return np.stack([X.reshape(-1), Y.reshape(-1)], axis=1), np.outer(wx, wy).reshape(-1)
+
+
+def propose_panels_surrogate(net, gimic, region, mass, rule=None):
+    """Quadtree driven by the network as a surrogate integrand: a mapped
+    panel is split in four while its order-q rule and an order-2q rule
+    applied to the predicted |j| differ by more than ``tau_s`` (nA/T), up to
+    ``max_depth``.  Returns (map_u, map_v, panels) as propose_panels."""
+    r = dict(DEFAULT_RULE, **(rule or {}))
+    mu, mv = estimate_maps(mass, region, r)
+    q = int(r["q_hi"])
+    tu = np.linspace(mu.t0, mu.t1, int(r["n0u"]) + 1)
+    tv = np.linspace(mv.t0, mv.t1, int(r["n0v"]) + 1)
+    todo = [(tu[i], tu[i + 1], tv[j], tv[j + 1]) for i in range(len(tu) - 1) for j in range(len(tv) - 1)]
+    leaves = []
+    conv = api.au2si(1.0)
+    for depth in range(int(r["max_depth"]) + 1):
+        if not todo:
+            break
+        if depth == int(r["max_depth"]):
+            leaves += todo
+            break
+        rules = [(_panel_rule(mu, mv, *pn, q), _panel_rule(mu, mv, *pn, 2 * q)) for pn in todo]
+        xy = np.concatenate([a[0] for pair in rules for a in pair])
+        g = predict_at(net, gimic, region, xy) * conv
+        nxt, off = [], 0
+        for pn, (lo, hi) in zip(todo, rules):
+            n1, n2 = len(lo[1]), len(hi[1])
+            e = abs(np.dot(g[off:off + n1], lo[1]) - np.dot(g[off + n1:off + n1 + n2], hi[1]))
+            off += n1 + n2
+            if e > r["tau_s"]:
+                ta, tb, wa, wb = pn
+                tm, wm = 0.5 * (ta + tb), 0.5 * (wa + wb)
+                nxt += [(ta, tm, wa, wm), (tm, tb, wa, wm), (ta, tm, wm, wb), (tm, tb, wm, wb)]
+            else:
+                leaves.append(pn)
+        todo = nxt
+    return mu, mv, [(ta, tb, wa, wb, q) for ta, tb, wa, wb in leaves]
+
+
+def panel_planes(region, mu, mv, panels):
+    """Each mapped panel as a plane for Gimic.plane_integrals."""
+    out = []
+    for ta, tb, wa, wb, q in panels:
+        ax = [mu.nodes(ta, tb, q), mv.nodes(wa, wb, q), (np.zeros(1), np.ones(1))]
+        out.append((region.origin, region.basis(), ax, region.radius))
+    return out
+
+
+def integrate_panels(gimic, region, mu, mv, panels):
+    """Current (nA/T) summed over the mapped Gauss-Lobatto panels, all in
+    one device pass."""
+    res = gimic.plane_integrals(panel_planes(region, mu, mv, panels))
+    return sum(api.au2si(r["current"][0]) for r in res)
+
+
+def predict_mass(net, gimic, region, lattice=96):
     """Predicted current mass per cell of a lattice x lattice partition of
     the plane (|j| predicted at the cell centre times the cell area, nA/T),
     and the fraction of those cells whose features lie in the training
@@ -294,36 +465,6 @@ def predict_mass(net, gimic, region, lattice=64):
     return np.exp(lnj) * api.au2si(1.0) * (region.lx / G) * (region.ly / G), inside
 
 
-def panels_from_mass(mass, region, rule=None):
-    """Quadtree of panels over the lattice of predicted cell masses.  A panel
-    is split in four while its predicted current mass exceeds ``tau`` (nA/T)
-    and it is shallower than ``max_depth``; a leaf gets ``q_hi``
-    Gauss-Lobatto points per axis when its mass exceeds frac * tau, else
-    ``q_lo``.  Returns [(x0, x1, y0, y1, q)]."""
-    r = dict(DEFAULT_RULE, **(rule or {}))
-    G = mass.shape[0]
-    S = np.zeros((G + 1, G + 1))
-    S[1:, 1:] = mass.cumsum(0).cumsum(1)
-    panels, stack = [], [(0, G, 0, G, 0)]
-    while stack:
-        i0, i1, j0, j1, d = stack.pop()
-        m = S[i1, j1] - S[i0, j1] - S[i1, j0] + S[i0, j0]
-        if m > r["tau"] and d < r["max_depth"] and i1 - i0 >= 2 and j1 - j0 >= 2:
-            im, jm = (i0 + i1) // 2, (j0 + j1) // 2
-            stack += [(i0, im, j0, jm, d + 1), (im, i1, j0, jm, d + 1), (i0, im, jm, j1, d + 1),
-                      (im, i1, jm, j1, d + 1)]
-        else:
-            q = r["q_hi"] if m > r["frac"] * r["tau"] else r["q_lo"]
-            panels.append((i0 / G * region.lx, i1 / G * region.lx, j0 / G * region.ly, j1 / G * region.ly, q))
-    return panels
-
-
-def integrate_panels(gimic, region, panels):
-    """Current (nA/T) summed over Gauss-Lobatto panels, all in one pass."""
-    res = gimic.plane_integrals([region.panel(x0, x1, y0, y1, q, q) for x0, x1, y0, y1, q in panels])
-    return sum(api.au2si(r["current"][0]) for r in res)
-
-
 def integrate_adaptive(gimic, net, region, rule=None, min_inside=0.99, fallback_npts=200):
     """Current (nA/T) through the plane on the proposed panels.  When fewer
     than ``min_inside`` of the lattice features lie in the training range
@@ -334,10 +475,13 @@ def integrate_adaptive(gimic, net, region, rule=None, min_inside=0.99, fallback_
         r = dict(DEFAULT_RULE, **(rule or {}))
         mass, inside = predict_mass(net, gimic, region, r["lattice"])
         if inside >= min_inside:
-            panels = panels_from_mass(mass, region, r)
-            cur = integrate_panels(gimic, region, panels)
-            return {"current": cur, "points": int(sum(q * q for *_, q in panels)), "panels": panels,
-                    "method": "adaptive", "inside": inside}
+            if r["mode"] == "surrogate":
+                mu, mv, panels = propose_panels_surrogate(net, gimic, region, mass, r)
+            else:
+                mu, mv, panels = propose_panels(mass, region, r)
+            cur = integrate_panels(gimic, region, mu, mv, panels)
+            return {"current": cur, "points": int(sum(p[4] ** 2 for p in panels)), "panels": panels,
+                    "maps": (mu, mv), "method": "adaptive", "inside": inside}
     cur = integrate_uniform(gimic, region, fallback_npts)
     return {"current": cur, "points": fallback_npts * fallback_npts, "panels": None, "method": "uniform-fallback",
             "inside": inside}

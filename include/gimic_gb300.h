@@ -94,6 +94,11 @@ int gg_atoms(const gg_ctx *ctx, double *coords /* natoms x 3 */, double *charges
  * outputs is fine).  stream: a cudaStream_t or null for the default stream.
  * Returns after the results are complete. */
 int gg_jtensor_batch(gg_ctx *ctx, const double *pts, int64_t n, double *jt, double *rho, double *divt, void *stream);
+/* The same with fp32 outputs (each value computed in fp64 and rounded once),
+ * for grids too large to keep in fp64 (no reference counterpart; the
+ * reference writes its fields through Fortran real(8) arrays). */
+int gg_jtensor_batch_f32(gg_ctx *ctx, const double *pts, int64_t n, float *jt, float *rho, float *divt,
+                         void *stream);
 
 /* jv = t . B with B the context's magnetic field (jtensor.F90:125-135). */
 int gg_jvector_batch(gg_ctx *ctx, const double *pts, int64_t n, double *jv, void *stream);

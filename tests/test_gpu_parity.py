@@ -246,3 +246,21 @@ def test_full_cube_properties(synth_dir):
     g64 = api.Gimic(mp, xp, screening=1e-8, precision="fp64")
     ref = g64.jtensor_batch(pts[idx].contiguous())
     assert rel_max_err(jt[idx].cpu().numpy(), ref.cpu().numpy()) <= TOL_SPLIT
+
+
+@pytest.mark.parametrize("precision", ["split16", "fp64"])
+def test_fp32_outputs_are_the_fp64_results_rounded(c6h6, precision):
+    """gg_jtensor_batch_f32 stores each fp64 result rounded once to fp32, on
+    host and device buffers alike."""
+    torch = pytest.importorskip("torch")
+    mp, xp, _ = c6h6
+    g = api.Gimic(mp, xp, screening=1e-8, precision=precision)
+    pts = sample_points(g.atoms()[0], 900, 300, 8.0, seed=11)
+    jt, rho, dv = g.jtensor_batch(pts, rho=True, divj=True)
+    jt32, rho32, dv32 = g.jtensor_batch(pts, rho=True, divj=True, dtype=np.float32)
+    assert jt32.dtype == np.float32
+    assert np.array_equal(jt32, jt.astype(np.float32))
+    assert np.array_equal(rho32, rho.astype(np.float32))
+    assert np.array_equal(dv32, dv.astype(np.float32))
+    djt = g.jtensor_batch(torch.as_tensor(pts, device="cuda"), dtype=np.float32)
+    assert djt.dtype == torch.float32 and np.array_equal(djt.cpu().numpy(), jt32)

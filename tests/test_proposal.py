@@ -48,23 +48,70 @@ def test_oracle_adam_first_step_is_signed_lr():
     assert np.allclose(p, -0.01 * np.sign(g), rtol=1e-6)
 
 
-def test_quadtree_panels_cover_the_plane():
+def _mapped_rule_sum(P, reg, mu, mv, panels, f):
+    tot = 0.0
+    for ta, tb, wa, wb, q in panels:
+        x, wx = mu.nodes(ta, tb, q)
+        y, wy = mv.nodes(wa, wb, q)
+        tot += np.sum(np.outer(wx, wy) * f(x[:, None], y[None, :]))
+    return tot
+
+
+def test_mapped_quadtree_integrates_a_peaked_function():
+    """The proposal machinery on an analytic integrand (no GPU): axis maps
+    and panels built from the function's own mass lattice integrate it far
+    more accurately than a uniform grid with the same number of points."""
+    pytest.importorskip("torch")
+    from gimic_gb300 import proposal as P
+    from gimic_gb300 import api
+
+    reg = P.Region(np.zeros(3), [1, 0, 0], [0, 1, 0], [0, 0, 1], 16.0, 13.0, [8.0, 6.0, 0.0])
+    c, d = 8.3, 5.1
+
+    def f(x, y):
+        return np.exp(-((x - c) / 0.6) ** 2) * (1.0 + 0.5 * np.cos(2.0 * (y - d))) * np.exp(-((y - d) / 1.2) ** 2)
+
+    # both factors are negligible (< 1e-8) at the plane's edges
+    exact = 0.6 * np.sqrt(np.pi) * (1.2 * np.sqrt(np.pi) * (1.0 + 0.5 * np.exp(-(2.0 * 1.2) ** 2 / 4.0)))
+    G = 96
+    cx = (np.arange(G) + 0.5) / G * reg.lx
+    cy = (np.arange(G) + 0.5) / G * reg.ly
+    mass = f(cx[:, None], cy[None, :]) * (reg.lx / G) * (reg.ly / G)
+    mu, mv, panels = P.propose_panels(mass, reg, dict(kappa_u=1.0, kappa_v=1.0, n0u=3, n0v=3, max_depth=0, tau=1.0,
+                                                      q_hi=6, q_lo=4, frac=0.0))
+    # the maps cover the plane and put their centres on the peak
+    assert abs(mu.x(mu.t0)) < 1e-12 and abs(mu.x(mu.t1) - reg.lx) < 1e-9
+    assert abs(mv.x(mv.t0)) < 1e-12 and abs(mv.x(mv.t1) - reg.ly) < 1e-9
+    assert abs(mu.c - c) < 0.2 and abs(mv.c - d) < 0.2
+    n = sum(p[4] ** 2 for p in panels)
+    assert n == 324
+    got = _mapped_rule_sum(P, reg, mu, mv, panels, f)
+    assert abs(got - exact) < 1e-4 * exact, (got, exact)
+    # the uniform composite Lobatto grid needs 1600 points to get near it
+    for k, worse in ((2, True), (3, True), (4, True)):
+        xu, wu = api.gauss_data(0.0, reg.lx, 10, 10 * k, "lobatto")
+        yu, wv = api.gauss_data(0.0, reg.ly, 10, 10 * k, "lobatto")
+        uni = np.sum(np.outer(wu, wv) * f(xu[:, None], yu[None, :]))
+        assert (abs(uni - exact) > abs(got - exact)) == worse, k
+
+
+def test_quadtree_refines_where_the_mass_is():
+    pytest.importorskip("torch")
     from gimic_gb300 import proposal as P
 
     reg = P.Region(np.zeros(3), [1, 0, 0], [0, 1, 0], [0, 0, 1], 16.0, 10.0, [8.0, 5.0, 0.0])
     m = np.full((64, 64), 1e-6)
     m[30:34, 20:28] = 1.0
-    pan = P.panels_from_mass(m, reg, dict(tau=2.0, max_depth=4, q_hi=10, q_lo=4, frac=0.02))
-    area = sum((x1 - x0) * (y1 - y0) for x0, x1, y0, y1, _ in pan)
+    rule = dict(kappa_u=None, kappa_v=None, n0u=1, n0v=1, max_depth=4, tau=2.0, q_hi=10, q_lo=4, frac=0.02)
+    mu, mv, pan = P.propose_panels(m, reg, rule)
+    assert mu.s is None and mv.s is None  # identity maps: panels in plane coordinates
+    area = sum((tb - ta) * (wb - wa) for ta, tb, wa, wb, _ in pan)
     assert abs(area - 160.0) < 1e-9
     assert {q for *_, q in pan} == {4, 10}
-    # panels over the massive cells (x 7.5-8.5, y 3.125-4.375 Bohr) are
-    # refined to depth 4 (1 x 0.625 Bohr) and get the high order
     hot = [p for p in pan if p[0] < 8.5 and p[1] > 7.5 and p[2] < 4.375 and p[3] > 3.125]
     assert hot and all(p[4] == 10 and abs(p[1] - p[0] - 1.0) < 1e-12 for p in hot)
-    # nothing to refine: one coarse panel
-    pan = P.panels_from_mass(np.full((64, 64), 1e-9), reg, dict(tau=2.0))
-    assert len(pan) == 1 and pan[0][4] == P.DEFAULT_RULE["q_lo"]
+    mu, mv, pan = P.propose_panels(np.full((64, 64), 1e-9), reg, rule)
+    assert len(pan) == 1 and pan[0][4] == 4
 
 
 # ---------------------------------------------------------------------------
