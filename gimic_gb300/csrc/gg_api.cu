@@ -295,6 +295,9 @@ struct gg_ctx {
     if (e == cudaSuccess) e = upload(axyz, &d.atom_xyz);
     if (e == cudaSuccess) e = upload(f_shell, &d.f_shell);
     if (e == cudaSuccess) e = upload(f_ijk, &d.f_ijk);
+    std::vector<int> f_pack(b.nbf);
+    for (int mu = 0; mu < b.nbf; ++mu) f_pack[mu] = (f_shell[mu] << 12) | f_ijk[mu];
+    if (e == cudaSuccess) e = upload(f_pack, &d.f_pack);
     if (e == cudaSuccess) e = upload(sh_atom, &d.sh_atom);
     if (e == cudaSuccess) e = upload(sh_prim, &d.sh_prim);
     if (e == cudaSuccess) e = upload(sh_npf, &d.sh_npf);

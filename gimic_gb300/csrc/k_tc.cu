@@ -33,7 +33,13 @@ constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kTmemCols = 512;
 constexpr int kAccStride = 256;
 constexpr int kMaxTileList = 512;  // ints: 2 + column chunks + K blocks of a tile (nbf <= 10,000)
-constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256 + kMaxTileList * 4;
+constexpr int kSmemFixed = kStages * kStageBytes + 1024 + 256 + kMaxTileList * 4;
+// The column scales and packed function records are copied to shared memory
+// when they fit next to the pipeline stages (nchunk * 224 + nbf <= 12,000
+// words, i.e. nbf up to about 1700); otherwise the epilogue reads them from
+// global memory.
+constexpr int kSmemTables = 227 * 1024 - kSmemFixed;
+constexpr int kSmemBytes = kSmemFixed + kSmemTables;
 static_assert(kBlockM * kNDots * 8 <= kStageBytes, "epilogue reduction buffer must fit in one stage");
 
 __device__ __forceinline__ void tmem_ld1(uint32_t taddr, float& v) {
@@ -87,6 +93,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* accempty = accfull + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accempty + 2);
   int* tlist = reinterpret_cast<int*>(tmem_slot + 4);  // {#chunks, #kblocks, chunk ids, kblock ids}
+  float* s_icol = reinterpret_cast<float*>(tlist + kMaxTileList);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t tile = tile_order ? static_cast<int64_t>(tile_order[blockIdx.x]) : static_cast<int64_t>(blockIdx.x);
@@ -106,6 +113,18 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   const int* clist = tlist + 2;
   const int* klist = tlist + 2 + nchunk_all;
+  // column scales and per-function records (shell << 12 | packed ijk)
+  const int ncol = nchunk_all * kBlockN;
+  const bool tables_in_smem = (ncol + Bs.nbf) * 4 <= kSmemTables;
+  const float* icol = inv_col;
+  const int* fpack = Bs.f_pack;
+  if (tables_in_smem) {
+    int* s_fpack = reinterpret_cast<int*>(s_icol + ncol);
+    for (int i = threadIdx.x; i < ncol; i += blockDim.x) s_icol[i] = inv_col[i];
+    for (int i = threadIdx.x; i < Bs.nbf; i += blockDim.x) s_fpack[i] = Bs.f_pack[i];
+    icol = s_icol;
+    fpack = s_fpack;
+  }
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -241,7 +260,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll 1
       for (int mu = mb; mu < me; ++mu) {
         const int u = mu - f0;
-        const int sh = __ldg(Bs.f_shell + mu);
+        const int fp = fpack[mu];
+        const int sh = fp >> 12;
         if (sh != cur_shell) {
           cur_shell = sh;
           const int a = __ldg(Bs.sh_atom + sh);
@@ -274,13 +294,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         tmem_wait7(v);
         if (on) {
           float ph, gx, gy, gz, lp;
-          cart_eval<float>(__ldg(Bs.f_ijk + mu), sx, sy, sz, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
-          const float* cs = inv_col + c * kBlockN + u;
-          const float w0 = v[0] * __ldg(cs);
-          const float wc[3] = {v[1] * __ldg(cs + 1 * kChunkF), v[2] * __ldg(cs + 2 * kChunkF),
-                               v[3] * __ldg(cs + 3 * kChunkF)};
-          const float qq[3] = {v[4] * __ldg(cs + 4 * kChunkF), v[5] * __ldg(cs + 5 * kChunkF),
-                               v[6] * __ldg(cs + 6 * kChunkF)};
+          cart_eval<float>(fp & 0xfff, sx, sy, sz, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
+          const float* cs = icol + c * kBlockN + u;
+          const float w0 = v[0] * cs[0];
+          const float wc[3] = {v[1] * cs[1 * kChunkF], v[2] * cs[2 * kChunkF], v[3] * cs[3 * kChunkF]};
+          const float qq[3] = {v[4] * cs[4 * kChunkF], v[5] * cs[5 * kChunkF], v[6] * cs[6 * kChunkF]};
           const float wp = w0 * ph;
           part[0] = fmaf(w0, ph, part[0]);
           part[1] = fmaf(wp, sx, part[1]);
