@@ -17,6 +17,7 @@
 #include "../../include/gimic_gb300.h"
 #include "gg_host.h"
 #include "gg_kernels.h"
+#include "gg_cart.cuh"
 
 namespace {
 
@@ -296,7 +297,11 @@ struct gg_ctx {
     if (e == cudaSuccess) e = upload(f_shell, &d.f_shell);
     if (e == cudaSuccess) e = upload(f_ijk, &d.f_ijk);
     std::vector<int> f_pack(b.nbf);
-    for (int mu = 0; mu < b.nbf; ++mu) f_pack[mu] = (f_shell[mu] << 12) | f_ijk[mu];
+    for (int mu = 0; mu < b.nbf; ++mu) {
+      const int id = gg::cart_case_id(f_ijk[mu]);
+      if (id < 0) return fail(GG_EUNSUPPORTED, "angular momentum above f is not supported");
+      f_pack[mu] = (f_shell[mu] << 12) | id;
+    }
     if (e == cudaSuccess) e = upload(f_pack, &d.f_pack);
     if (e == cudaSuccess) e = upload(sh_atom, &d.sh_atom);
     if (e == cudaSuccess) e = upload(sh_prim, &d.sh_prim);
@@ -469,6 +474,9 @@ struct gg_ctx {
       if (e != cudaSuccess) return cuda_fail(e, "FP64 path launch");
       return GG_OK;
     }
+    if (dB.kpad > 64 * gg::kBlockK)
+      return fail(GG_EUNSUPPORTED, "the split-FP16 path handles at most 4096 basis functions (nbf=" +
+                                       std::to_string(basis.nbf) + "); use the FP64 precision");
     const size_t abytes = static_cast<size_t>(n) * dB.kpad * sizeof(__half);
     e = a_hi.reserve(abytes);
     if (e == cudaSuccess) e = a_lo.reserve(abytes);

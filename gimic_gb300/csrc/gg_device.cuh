@@ -19,7 +19,7 @@ struct DevBasis {
   const double* atom_xyz;  // natoms x 3
   const int* f_shell;      // shell of each function
   const int* f_ijk;        // Cartesian exponents packed i | j << 4 | k << 8
-  const int* f_pack;       // shell << 12 | f_ijk
+  const int* f_pack;       // shell << 12 | Cartesian case id (gg_cart.cuh)
   const int* sh_atom;
   const int* sh_prim;      // first primitive
   const int* sh_npf;

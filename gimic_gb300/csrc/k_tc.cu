@@ -18,6 +18,7 @@
 //               gg_combine.cuh (src/libgimic/jtensor.F90:148-237).
 #include <cuda.h>
 
+#include "gg_cart.cuh"
 #include "gg_combine.cuh"
 #include "gg_kernels.h"
 
@@ -242,6 +243,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int i = 0; i < kNDots; ++i) thi[i] = tlo[i] = 0.f;
     int cur_shell = -1, cur_atom = -1;
     float sx = 0.f, sy = 0.f, sz = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
+    CartPow cp = cart_pow(0.f, 0.f, 0.f);
     DFloat d2a{0.f, 0.f};
     bool on = false;
     const uint32_t lane_base = tmem_base + (static_cast<uint32_t>(q * 32) << 16);
@@ -272,6 +274,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             sx = s3[0];
             sy = s3[1];
             sz = s3[2];
+            cp = cart_pow(sx, sy, sz);
           }
           on = df_le(d2a, __ldg(Bs.sh_rad2_df + sh));
           f1 = f2 = f3 = 0.f;
@@ -294,7 +297,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         tmem_wait7(v);
         if (on) {
           float ph, gx, gy, gz, lp;
-          cart_eval<float>(fp & 0xfff, sx, sy, sz, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
+          cart_case(fp & 0xfff, cp, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
           const float* cs = icol + c * kBlockN + u;
           const float w0 = v[0] * cs[0];
           const float wc[3] = {v[1] * cs[1 * kChunkF], v[2] * cs[2 * kChunkF], v[3] * cs[3 * kChunkF]};
