@@ -63,6 +63,8 @@ SIGNATURES = {
     "gg_profile_read": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "gg_jtensor_batch_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
+    "gg_properties": (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, _dp, C.c_int, C.POINTER(C.c_int64), C.c_int, _dp,
+                                _dp, C.c_void_p]),
     "gg_mlp_nparams": (C.c_int, []),
     "gg_mlp_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "gg_mlp_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -202,6 +202,27 @@ class Gimic:
         """One point, as Gimic.jvector in gimic.pyx:23-32 (a list of 3)."""
         return list(self.jvector_batch(np.asarray(r, dtype=np.float64).reshape(1, 3))[0])
 
+    def properties(self, points, weights, centres, block_npts=None):
+        """Shielding of every centre (ppm) and magnetizability (au) over a
+        molecular grid (gg_properties).  Returns (sigma, chi) with sigma of
+        shape (ncentres, nblocks, 5) and chi of shape (nblocks, 5): the
+        three diagonal sums, then the positive and negative parts."""
+        p = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+        w = np.ascontiguousarray(np.asarray(weights, dtype=np.float64).reshape(-1))
+        c = np.ascontiguousarray(np.asarray(centres, dtype=np.float64).reshape(-1, 3))
+        nb = 1
+        bp = None
+        if block_npts is not None and len(block_npts):
+            bp = np.ascontiguousarray(np.asarray(block_npts, dtype=np.int64))
+            nb = len(bp)
+        sig = np.zeros((len(c), nb, 5))
+        chi = np.zeros((nb, 5))
+        rc = self._L.gg_properties(self._h, _dptr(p), _dptr(w), len(p), _dptr(c), len(c),
+                                   bp.ctypes.data_as(C.POINTER(C.c_int64)) if bp is not None else None,
+                                   nb if bp is not None else 0, _dptr(sig), _dptr(chi), None)
+        check(rc, self._h)
+        return sig, chi
+
     def plane_integral(self, origin, basv, axes, radius=1e10, stream=None):
         """Quadrature over the product grid origin + x1 basv[:,0] + x2 basv[:,1]
         + x3 basv[:,2] with axes = ((x1, w1), (x2, w2), (x3, w3)).  Returns a

@@ -318,6 +318,10 @@ struct gg_ctx {
     if (e == cudaSuccess) e = upload(p_xp, &d.p_xp);
     if (e == cudaSuccess) e = upload(p_xplo, &d.p_xplo);
     if (e == cudaSuccess) e = upload(p_cc, &d.p_cc);
+    std::vector<float4> p_pack;
+    for (size_t i = 0; i < p_xp.size(); ++i) p_pack.push_back(make_float4(p_xp[i], p_xplo[i], p_cc[i], 0.f));
+    d.nprim = static_cast<int>(p_xp.size());
+    if (e == cudaSuccess) e = upload(p_pack, &d.p_pack);
     if (e == cudaSuccess) e = upload(p_xpd, &d.p_xpd);
     if (e == cudaSuccess) e = upload(p_ccd, &d.p_ccd);
     if (e != cudaSuccess) return cuda_fail(e, "uploading basis tables");
@@ -760,6 +764,62 @@ int gg_jtensor_batch(gg_ctx* ctx, const double* pts, int64_t n, double* jt, doub
   if (!ctx) return GG_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   return ctx->jtensor(pts, n, jt, rho, divt, static_cast<cudaStream_t>(stream));
+}
+
+int gg_properties(gg_ctx* ctx, const double* pts, const double* wgt, int64_t n, const double* centres, int ncentres,
+                  const int64_t* block_npts, int nblocks, double* sigma, double* chi, void* stream) {
+  if (!ctx || n <= 0 || !pts || !wgt || ncentres < 0 || (ncentres > 0 && (!centres || !sigma)) || !chi)
+    return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  std::vector<int64_t> off(1, 0);
+  if (block_npts && nblocks > 0) {
+    for (int l = 0; l < nblocks; ++l) {
+      if (block_npts[l] < 0) return ctx->fail(GG_EINVAL, "negative block size");
+      off.push_back(off.back() + block_npts[l]);
+    }
+    if (off.back() != n) return ctx->fail(GG_EINVAL, "block sizes do not add up to the number of points");
+  } else {
+    off.push_back(n);
+  }
+  const int nb = static_cast<int>(off.size()) - 1;
+  int rc = ctx->prepare();
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t aux = (static_cast<size_t>(n) + static_cast<size_t>(ncentres) * 3 + off.size() +
+                      static_cast<size_t>(ncentres + 1) * nb * 5) * sizeof(double) + 256;
+  cudaError_t e = ctx->pts.reserve(static_cast<size_t>(n) * 3 * sizeof(double));
+  if (e == cudaSuccess) e = ctx->jt.reserve(static_cast<size_t>(n) * 9 * sizeof(double));
+  if (e == cudaSuccess) e = ctx->plane_rows.reserve(aux);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "property scratch");
+  double* dw = ctx->plane_rows.as<double>();
+  double* dc = dw + n;
+  int64_t* doff = reinterpret_cast<int64_t*>(dc + 3 * static_cast<size_t>(ncentres));
+  double* dsig = reinterpret_cast<double*>(doff + off.size());
+  double* dchi = dsig + static_cast<size_t>(ncentres) * nb * 5;
+  e = cudaMemcpyAsync(ctx->pts.p, pts, static_cast<size_t>(n) * 3 * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dw, wgt, static_cast<size_t>(n) * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && ncentres > 0)
+    e = cudaMemcpyAsync(dc, centres, static_cast<size_t>(ncentres) * 3 * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(doff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "copying the property grid");
+  const int64_t batch = ctx->precision == GG_PREC_FP64 ? std::min<int64_t>(ctx->max_batch, 16384) : ctx->max_batch;
+  for (int64_t o = 0; o < n; o += batch) {
+    const int64_t m = std::min(batch, n - o);
+    rc = ctx->run_batch(ctx->pts.as<double>() + 3 * o, m, ctx->jt.as<double>() + 9 * o, nullptr, nullptr, st);
+    if (rc) return rc;
+  }
+  gg::launch_properties(ctx->jt.as<double>(), ctx->pts.as<double>(), dw, dc, ncentres, doff, nb, dsig, dchi, st);
+  ctx->launches += ncentres > 0 ? 2 : 1;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "property kernels");
+  if (ncentres > 0)
+    e = cudaMemcpyAsync(sigma, dsig, static_cast<size_t>(ncentres) * nb * 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                        st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(chi, dchi, static_cast<size_t>(nb) * 5 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "copying property sums");
+  return ctx->check_device_error(st);
 }
 
 int gg_jtensor_batch_f32(gg_ctx* ctx, const double* pts, int64_t n, float* jt, float* rho, float* divt,

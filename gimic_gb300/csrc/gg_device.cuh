@@ -32,6 +32,8 @@ struct DevBasis {
   const float* p_xp;       // primitive exponents (fp32, rounded)
   const float* p_xplo;     // exponent residuals: p_xpd - p_xp (fp32)
   const float* p_cc;       // normalised contraction coefficients (fp32)
+  const float4* p_pack;    // {p_xp, p_xplo, p_cc, 0} per primitive
+  int nprim;
   const int4* sh_pack;     // {atom, first function, ncomp | npf << 8 | l << 16, first primitive}
   const float2* sh_bound;  // {squared radius (fp32, rounded up), l}
   const float2* p_bound;   // {a log2(e) (rounded down), log2 |c| + log2(npf of the shell) (rounded up)}
@@ -135,6 +137,19 @@ __device__ __forceinline__ DFloat df_sqr(DFloat a) {
 
 // a <= b for normalised double-floats
 __device__ __forceinline__ bool df_le(DFloat a, float2 b) { return a.h < b.x || (a.h == b.x && a.l <= b.y); }
+
+// The same with the atom table read through a generic pointer (shared or
+// global memory).
+__device__ __forceinline__ DFloat atom_offset_t(const DFloat r[3], const float2* atom_df, int a, float s[3]) {
+  DFloat d2{0.f, 0.f};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const DFloat dc = df_sub(r[c], atom_df[3 * a + c]);
+    s[c] = dc.h;
+    d2 = df_add(d2, df_sqr(dc));
+  }
+  return d2;
+}
 
 // Position of a point relative to atom a and its squared distance, from the
 // point as double-floats and the atom table.

@@ -87,6 +87,13 @@ void launch_plane_batch(const double* jt, const double* pts, const double* w, co
                         const int* row_plane, int64_t nrows, const double bb[3], double* row_out, double* out,
                         cudaStream_t st);
 
+// Shielding of every centre and magnetizability over a molecular grid whose
+// points come in nblocks consecutive blocks [block_off[l], block_off[l+1]):
+// sigma_out[(k * nblocks + l) * 5 + q], chi_out[l * 5 + q] with q = the three
+// diagonal sums, then the positive and negative parts (k_reduce.cu).
+void launch_properties(const double* jt, const double* pts, const double* w, const double* centres, int ncentres,
+                       const int64_t* block_off, int nblocks, double* sigma_out, double* chi_out, cudaStream_t st);
+
 // Integration proposal network (k_mlp.cu): 5 -> 64 -> 64 -> 1, SiLU.
 constexpr int kMlpIn = 5;
 constexpr int kMlpHidden = 64;

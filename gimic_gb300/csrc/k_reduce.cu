@@ -97,4 +97,99 @@ void launch_plane_batch(const double* jt, const double* pts, const double* w, co
   plane_batch_sum_kernel<<<(nplanes * kQ + 127) / 128, 128, 0, st>>>(w, planes, nplanes, row_out, out);
 }
 
+// ---------------------------------------------------------------------------
+// Property quadratures over a molecular grid (src/fgimic/jfield.f90:584-929,
+// get_property): nuclear shielding of every centre and the magnetizability,
+// both from the current tensor with the field along -x, -y, -z.  Points come
+// in consecutive blocks (one per atom of the grid generator); one CTA sums one
+// (centre, block) pair, or one block for the magnetizability, with a fixed
+// tree in fp64, so the sums are deterministic.
+//   sigma_a(K) = sum_i w_i 1e6 f_i ((r_i - R_K) x j_i^(a))_a,
+//   f_i = -1 / |r_i - R_K|^3 / c^2,  c = 137.0359998,  j^(a) = t . (-e_a);
+//   chi_a = sum_i w_i 0.5 (r_i x j_i^(a))_a.
+// Each output record holds the three diagonal sums and the positive and
+// negative parts of sum_a (per-point value) w_i.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kPropThreads = 128;
+constexpr int kPropQ = 5;
+
+__device__ __forceinline__ void prop_block_reduce(double acc[kPropQ], double* dst) {
+  __shared__ double red[kPropQ][kPropThreads];
+  for (int q = 0; q < kPropQ; ++q) red[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int s = kPropThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int q = 0; q < kPropQ; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < kPropQ) dst[threadIdx.x] = red[threadIdx.x][0];
+}
+
+// (d x j^(a))_a for the field along -e_a, j^(a)_m = -t(m, a) = -t[m + 3a]
+__device__ __forceinline__ void cross_diag(const double* t, const double d[3], double out[3]) {
+  out[0] = -(d[1] * t[2 + 0] - d[2] * t[1 + 0]);
+  out[1] = -(d[2] * t[0 + 3] - d[0] * t[2 + 3]);
+  out[2] = -(d[0] * t[1 + 6] - d[1] * t[0 + 6]);
+}
+}  // namespace
+
+__global__ void __launch_bounds__(kPropThreads) prop_sigma_kernel(const double* __restrict__ jt,
+                                                                  const double* __restrict__ pts,
+                                                                  const double* __restrict__ w,
+                                                                  const double* __restrict__ centres,
+                                                                  const int64_t* __restrict__ block_off, int nblocks,
+                                                                  double* __restrict__ out) {
+  const int k = blockIdx.y, l = blockIdx.x;
+  const double R[3] = {centres[3 * k], centres[3 * k + 1], centres[3 * k + 2]};
+  const double c2 = 137.0359998 * 137.0359998;
+  double acc[kPropQ] = {0, 0, 0, 0, 0};
+  for (int64_t i = block_off[l] + threadIdx.x; i < block_off[l + 1]; i += kPropThreads) {
+    const double d[3] = {pts[3 * i] - R[0], pts[3 * i + 1] - R[1], pts[3 * i + 2] - R[2]};
+    const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const double f = -1.0 / (r2 * sqrt(r2)) / c2;
+    double c[3];
+    cross_diag(jt + 9 * i, d, c);
+    double sum = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      const double v = 1.0e6 * f * c[a];
+      acc[a] += w[i] * v;
+      sum += v;
+    }
+    if (sum >= 0.0) acc[3] += sum * w[i]; else acc[4] += sum * w[i];
+  }
+  prop_block_reduce(acc, out + (static_cast<int64_t>(k) * nblocks + l) * kPropQ);
+}
+
+__global__ void __launch_bounds__(kPropThreads) prop_chi_kernel(const double* __restrict__ jt,
+                                                                const double* __restrict__ pts,
+                                                                const double* __restrict__ w,
+                                                                const int64_t* __restrict__ block_off,
+                                                                double* __restrict__ out) {
+  const int l = blockIdx.x;
+  double acc[kPropQ] = {0, 0, 0, 0, 0};
+  for (int64_t i = block_off[l] + threadIdx.x; i < block_off[l + 1]; i += kPropThreads) {
+    const double r[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+    double c[3];
+    cross_diag(jt + 9 * i, r, c);
+    double sum = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      const double v = 0.5 * c[a];
+      acc[a] += w[i] * v;
+      sum += v;
+    }
+    if (sum >= 0.0) acc[3] += sum * w[i]; else acc[4] += sum * w[i];
+  }
+  prop_block_reduce(acc, out + static_cast<int64_t>(l) * kPropQ);
+}
+
+void launch_properties(const double* jt, const double* pts, const double* w, const double* centres, int ncentres,
+                       const int64_t* block_off, int nblocks, double* sigma_out, double* chi_out, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  if (ncentres > 0)
+    prop_sigma_kernel<<<dim3(static_cast<unsigned>(nblocks), static_cast<unsigned>(ncentres)), kPropThreads, 0, st>>>(
+        jt, pts, w, centres, block_off, nblocks, sigma_out);
+  prop_chi_kernel<<<static_cast<unsigned>(nblocks), kPropThreads, 0, st>>>(jt, pts, w, block_off, chi_out);
+}
+
 }  // namespace gg

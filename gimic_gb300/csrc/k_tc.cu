@@ -119,14 +119,38 @@ __global__ void __launch_bounds__(kThreads, 1)
   const bool tables_in_smem = (ncol + Bs.nbf) * 4 <= kSmemTables;
   const float* icol = inv_col;
   const int* fpack = Bs.f_pack;
+  // shell records, screening radii, primitives and atoms too when they fit
+  const int shell_bytes = Bs.nshells * (16 + 8) + Bs.nprim * 16 + Bs.natoms * 24;
+  const bool shells_in_smem = tables_in_smem && (ncol + Bs.nbf) * 4 + shell_bytes + 16 <= kSmemTables;
+  const int4* shp = Bs.sh_pack;
+  const float2* shr = Bs.sh_rad2_df;
+  const float4* prm = Bs.p_pack;
+  const float2* atm = Bs.atom_df;
   if (tables_in_smem) {
     int* s_fpack = reinterpret_cast<int*>(s_icol + ncol);
     for (int i = threadIdx.x; i < ncol; i += blockDim.x) s_icol[i] = inv_col[i];
     for (int i = threadIdx.x; i < Bs.nbf; i += blockDim.x) s_fpack[i] = Bs.f_pack[i];
     icol = s_icol;
     fpack = s_fpack;
+    if (shells_in_smem) {
+      unsigned char* q = reinterpret_cast<unsigned char*>(
+          (reinterpret_cast<uintptr_t>(s_fpack + Bs.nbf) + 15) & ~static_cast<uintptr_t>(15));
+      int4* s_shp = reinterpret_cast<int4*>(q);
+      float4* s_prm = reinterpret_cast<float4*>(s_shp + Bs.nshells);
+      float2* s_shr = reinterpret_cast<float2*>(s_prm + Bs.nprim);
+      float2* s_atm = s_shr + Bs.nshells;
+      for (int i = threadIdx.x; i < Bs.nshells; i += blockDim.x) {
+        s_shp[i] = Bs.sh_pack[i];
+        s_shr[i] = Bs.sh_rad2_df[i];
+      }
+      for (int i = threadIdx.x; i < Bs.nprim; i += blockDim.x) s_prm[i] = Bs.p_pack[i];
+      for (int i = threadIdx.x; i < 3 * Bs.natoms; i += blockDim.x) s_atm[i] = Bs.atom_df[i];
+      shp = s_shp;
+      shr = s_shr;
+      prm = s_prm;
+      atm = s_atm;
+    }
   }
-
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
@@ -266,23 +290,25 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int sh = fp >> 12;
         if (sh != cur_shell) {
           cur_shell = sh;
-          const int a = __ldg(Bs.sh_atom + sh);
+          const int4 pk = shp[sh];  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
+          const int a = pk.x;
           if (a != cur_atom) {
             cur_atom = a;
             float s3[3];
-            d2a = atom_offset(rdf, Bs.atom_df, a, s3);
+            d2a = atom_offset_t(rdf, atm, a, s3);
             sx = s3[0];
             sy = s3[1];
             sz = s3[2];
             cp = cart_pow(sx, sy, sz);
           }
-          on = df_le(d2a, __ldg(Bs.sh_rad2_df + sh));
+          on = df_le(d2a, shr[sh]);
           f1 = f2 = f3 = 0.f;
           if (on) {
-            const int p0 = __ldg(Bs.sh_prim + sh), np = __ldg(Bs.sh_npf + sh);
+            const int np = (pk.z >> 8) & 0xff;
             for (int k = 0; k < np; ++k) {
-              const float al = __ldg(Bs.p_xp + p0 + k);
-              const float e = __ldg(Bs.p_cc + p0 + k) * gauss_df(al, __ldg(Bs.p_xplo + p0 + k), d2a.h, d2a.l);
+              const float4 pr = prm[pk.w + k];  // exponent hi, exponent lo, coefficient
+              const float al = pr.x;
+              const float e = pr.z * gauss_df(al, pr.y, d2a.h, d2a.l);
               f1 += e;
               f2 += al * e;
               f3 += al * al * e;

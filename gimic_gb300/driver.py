@@ -12,7 +12,7 @@ import sys
 
 import numpy as np
 
-from . import api, inp, vtk
+from . import api, inp, properties, vtk
 from . import grid as ggrid
 
 AU2A = 0.52917726
@@ -134,6 +134,10 @@ class Driver:
             jv = t @ self.magnet
             out[spin] = {"jt": jt, "jvec": jv}
             self._write_fields(tag, pts, jt, jv)
+            if self.kw.get("Essential.prop"):
+                # get_property (jfield.f90:404-405): shielding and magnetizability
+                # over the molecular grid of gridfile.grd / grid_w.grd
+                out[spin]["properties"] = properties.run(self.g, self.stream, self.workdir)
         return out
 
     def _write_fields(self, tag, pts, jt, jv):

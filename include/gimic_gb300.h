@@ -94,6 +94,25 @@ int gg_atoms(const gg_ctx *ctx, double *coords /* natoms x 3 */, double *charges
  * outputs is fine).  stream: a cudaStream_t or null for the default stream.
  * Returns after the results are complete. */
 int gg_jtensor_batch(gg_ctx *ctx, const double *pts, int64_t n, double *jt, double *rho, double *divt, void *stream);
+/* Property quadratures over a molecular grid (replaces get_property,
+ * src/fgimic/jfield.f90:584-929): the current tensor is evaluated at the n
+ * points pts (n x 3, Bohr) with weights wgt (n), and for the field along -x,
+ * -y and -z the code sums
+ *   nuclear shielding of every centre K (ncentres x 3 coordinates, Bohr):
+ *     sigma_a(K) = sum_i w_i 1e6 f_i ((r_i - R_K) x j_i)_a,
+ *     f_i = -1 / |r_i - R_K|^3 / 137.0359998^2   (ppm),
+ *   magnetizability: chi_a = sum_i w_i 0.5 (r_i x j_i)_a   (au),
+ * separately over nblocks consecutive blocks of points of block_npts[l]
+ * points each (the per-atom blocks of the grid generator, nelpts.info; null
+ * or nblocks <= 0: one block).  Outputs, host memory:
+ *   sigma[(K * nb + l) * 5 + q], chi[l * 5 + q], nb = number of blocks,
+ *   q = 0..2 the diagonal sums, 3 and 4 the positive and negative parts of
+ *   sum_a (value at the point) * w_i.
+ * Summing over l gives the reference's totals; the per-block sums divided by
+ * 3 are its printed atom contributions. */
+int gg_properties(gg_ctx *ctx, const double *pts, const double *wgt, int64_t n, const double *centres, int ncentres,
+                  const int64_t *block_npts, int nblocks, double *sigma, double *chi, void *stream);
+
 /* The same with fp32 outputs (each value computed in fp64 and rounded once),
  * for grids too large to keep in fp64 (no reference counterpart; the
  * reference writes its fields through Fortran real(8) arrays). */

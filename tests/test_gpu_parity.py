@@ -264,3 +264,36 @@ def test_fp32_outputs_are_the_fp64_results_rounded(c6h6, precision):
     assert np.array_equal(dv32, dv.astype(np.float32))
     djt = g.jtensor_batch(torch.as_tensor(pts, device="cuda"), dtype=np.float32)
     assert djt.dtype == torch.float32 and np.array_equal(djt.cpu().numpy(), jt32)
+
+
+@pytest.mark.parametrize("precision,tol", [("split16", 1e-6), ("fp64", 1e-11)])
+def test_properties_against_oracle(c6h6, precision, tol):
+    """gg_properties (shielding of every nucleus, magnetizability, per-block
+    decomposition) against the FP64 restatement of get_property on the C
+    oracle's tensors; errors relative to the sums of |terms|."""
+    import prop_oracle
+
+    mp, xp, _ = c6h6
+    g, o = _pair(mp, xp, precision=precision)
+    xyz = o.atoms()[0]
+    rng = np.random.default_rng(21)
+    blocks = rng.integers(150, 400, len(xyz))
+    pts = np.vstack([xyz[a] + rng.normal(0.0, 1.2, (blocks[a], 3)) for a in range(len(xyz))])
+    w = rng.uniform(0.01, 0.2, len(pts))
+    sig, chi = g.properties(pts, w, xyz, blocks)
+    jt = o.jtensor(pts)
+    ref_sig, ref_chi = prop_oracle.properties(jt, pts, w, xyz, blocks)
+    assert sig.shape == ref_sig.shape == (len(xyz), len(xyz), 5) and chi.shape == ref_chi.shape
+    # error bound: tol * max|j| times the sum of |weight * kernel|
+    jmax = np.max(np.abs(jt))
+    for k, R in enumerate(xyz):
+        d = np.linalg.norm(pts - R, axis=1)
+        scale = jmax * np.sum(w * 1.0e6 * d / d ** 3 / 137.0359998 ** 2)
+        assert np.max(np.abs(sig[k] - ref_sig[k])) <= tol * scale, k
+    scale = jmax * np.sum(w * 0.5 * np.linalg.norm(pts, axis=1))
+    assert np.max(np.abs(chi - ref_chi)) <= tol * scale
+    # one block when no decomposition is given: the totals
+    s1, c1 = g.properties(pts, w, xyz)
+    assert s1.shape == (len(xyz), 1, 5)
+    assert np.allclose(s1[:, 0, :], sig.sum(axis=1), rtol=1e-9, atol=1e-12)
+    assert np.allclose(c1[0], chi.sum(axis=0), rtol=1e-9, atol=1e-15)

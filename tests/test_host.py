@@ -186,3 +186,41 @@ def test_bond_grid_geometry(c6h6):
     pts = g.points()
     assert pts.shape == (3600, 3)
     assert np.array_equal(pts[61], g.gridpoint(1, 1, 0))
+
+
+def test_property_files_and_report(tmp_path):
+    """get_property's inputs (coord.au, gridfile.grd, grid_w.grd, nelpts.info)
+    are read as the reference reads them, and the printed blocks sum the
+    per-block records (jfield.f90:700-928)."""
+    import io
+
+    from gimic_gb300 import properties
+
+    (tmp_path / "coord.au").write_text("0.0 0.0 0.0\n1.5D0 0.0 0.0\n")
+    pts = np.array([[0.1, 0.2, 0.3], [1.0, -0.5, 0.2], [2.0, 0.1, 0.1], [1.4, 0.3, -0.2], [0.5, 0.5, 0.5]])
+    (tmp_path / "gridfile.grd").write_text("".join("%.17g %.17g %.17g\n" % tuple(p) for p in pts))
+    (tmp_path / "grid_w.grd").write_text("".join("%r\n" % w for w in (0.1, 0.2, 0.3, 0.4, 0.5)))
+    assert properties.read_inputs(str(tmp_path)) is not None
+    coord, p, w, blocks = properties.read_inputs(str(tmp_path))
+    assert blocks is None and np.allclose(coord[1], [1.5, 0, 0]) and np.allclose(p, pts) and len(w) == 5
+    (tmp_path / "nelpts.info").write_text("1 2\n2 3\n")
+    assert list(properties.read_inputs(str(tmp_path))[3]) == [2, 3]
+
+    class Fake:
+        def properties(self, pts, w, centres, blocks):
+            sig = np.arange(2 * 2 * 5, dtype=float).reshape(2, 2, 5)
+            chi = np.arange(10, dtype=float).reshape(2, 5) * -0.01
+            return sig, chi
+
+    out = io.StringIO()
+    sig, chi = properties.run(Fake(), out, str(tmp_path))
+    text = out.getvalue()
+    # totals of centre 1: sigma_xx = 0 + 5, shielding = (5 + 7 + 9) / 3
+    # Fortran (X, A10, 2X, F14.6)
+    assert " sigma_xx    " + "%14.6f" % 5.0 in text
+    assert "%14.6f" % 7.0 in text
+    assert "chi_xx " in text and "isotropic magnetizability chi" in text
+    missing = io.StringIO()
+    (tmp_path / "grid_w.grd").unlink()
+    assert properties.run(Fake(), missing, str(tmp_path)) is None
+    assert "property calculation is skipped" in missing.getvalue()
