@@ -36,9 +36,10 @@ constexpr int kAccStride = 256;
 constexpr int kMaxTileList = 512;  // ints: 2 + column chunks + K blocks of a tile (nbf <= 10,000)
 constexpr int kSmemFixed = kStages * kStageBytes + 1024 + 256 + kMaxTileList * 4;
 // The column scales and packed function records are copied to shared memory
-// when they fit next to the pipeline stages (nchunk * 224 + nbf <= 12,000
-// words, i.e. nbf up to about 1700); otherwise the epilogue reads them from
-// global memory.
+// when they fit next to the pipeline stages (nchunk * 224 + nbf <= 12,224
+// words, i.e. nbf up to about 1500), the shell, primitive and atom tables as
+// well when those fit too; otherwise the epilogue reads them from global
+// memory.
 constexpr int kSmemTables = 227 * 1024 - kSmemFixed;
 constexpr int kSmemBytes = kSmemFixed + kSmemTables;
 static_assert(kBlockM * kNDots * 8 <= kStageBytes, "epilogue reduction buffer must fit in one stage");
