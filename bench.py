@@ -186,15 +186,33 @@ def run_scan(args):
     10), all strips of a molecule in one device pass."""
     import torch
 
-    from gimic_gb300 import api, build, scan, synth
+    from gimic_gb300 import api, build, scan, shard, synth
 
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", rank=rank, world_size=world)
     build.build()
     rng = np.random.default_rng(5)
-    jobs = []
+    all_jobs = []
     for i in range(args.molecules):
-        mp, xp, mol = synth.make_batch_molecule(os.path.join(args.data, "batch"), i)
         nstrips = int(rng.integers(20, 201))
         p = int(rng.choice(np.arange(40, 121, 10)))
+        all_jobs.append((i, nstrips, p))
+    # molecules are independent: each rank takes a cost-balanced share
+    # (no collective on the data path; weak scaling in molecules per GPU)
+    nbf_est = [synth.make_batch_molecule(os.path.join(args.data, "batch"), i)[2].nbf for i, _, _ in all_jobs]
+    costs = [n * n * s_ * p * p for n, (_, s_, p) in zip(nbf_est, all_jobs)]
+    jobs = []
+    for k in shard.shard_indices(costs, rank, world):
+        i, nstrips, p = all_jobs[k]
+        mp, xp, mol = synth.make_batch_molecule(os.path.join(args.data, "batch"), i)
         jobs.append((mp, xp, mol, nstrips, p))
     ctxs = [api.Gimic(mp, xp, screening=1e-8) for mp, xp, _, _, _ in jobs]
     specs = []
@@ -218,18 +236,24 @@ def run_scan(args):
             npl += nstrips
             npt += nstrips * p * p
     torch.cuda.synchronize()
-    wall = time.perf_counter() - t_all
-    nbfs = [m.nbf for _, _, m, _, _ in jobs]
+    wall = shard.reduce_scalar(time.perf_counter() - t_all, "max", dist, "cuda")
+    npl = int(shard.reduce_scalar(npl, "sum", dist, "cuda"))
+    npt = int(shard.reduce_scalar(npt, "sum", dist, "cuda"))
+    if rank != 0:
+        return
+    nbfs = nbf_est
     line = {"metric": "plane-integrals/s (batched bond-current profile scans)", "value": npl / wall,
-            "unit": "planes/s", "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": wall / args.steps * 1e3,
+            "unit": "planes/s", "n_gpus": world, "steps": args.steps, "warmup": 1, "ms_per_step": wall / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16x3/f32/f64",
             "data": "synthetic (seeded MOL/XDENS in the reference's formats)",
             "config": {"workload": "%d random rings/sheets (C 4-40), profile scans of 20-200 Lobatto strips of "
-                                   "40^2-120^2 points" % len(jobs), "nbf_min": min(nbfs), "nbf_max": max(nbfs),
+                                   "40^2-120^2 points" % len(all_jobs), "nbf_min": min(nbfs), "nbf_max": max(nbfs),
+                       "parallelism": "molecules sharded over %d GPUs" % world if world > 1 else "1 GPU",
                        "planes_per_step": npl // args.steps, "points_per_step": npt // args.steps},
             "points_per_s": npt / wall,
             "per_molecule_ms": {"p50": float(np.percentile(times, 50) * 1e3),
-                                "p99": float(np.percentile(times, 99) * 1e3)}}
+                                "p99": float(np.percentile(times, 99) * 1e3),
+                                "ranks": "rank 0's molecules" if world > 1 else "all"}}
     print(json.dumps(line), flush=True)
 
 

@@ -129,6 +129,10 @@ struct gg_ctx {
 
   // scratch
   DevBuf a_hi, a_lo, inv_row, pts, jt, rho, divt, jv;
+  // second staging slot and copy stream of the overlapped host-buffer path
+  DevBuf pts2, jt2, rho2, divt2;
+  cudaStream_t copy_stream = nullptr, out_stream = nullptr;
+  cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
   DevBuf sort_keys, sort_keys2, sort_idx, sort_perm, sort_temp, pts_sorted, tile_lists, tile_ord;
   DevBuf phi, gx, gy, gz, lap, w64;
   DevBuf plane_rows, plane_out;
@@ -181,6 +185,11 @@ struct gg_ctx {
   }
 
   ~gg_ctx() {
+    for (int i = 0; i < 2; ++i)
+      for (cudaEvent_t ev : {ev_in[i], ev_done[i], ev_out[i]})
+        if (ev) cudaEventDestroy(ev);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+    if (out_stream) cudaStreamDestroy(out_stream);
     if (prof.d_blocks) cudaFree(prof.d_blocks);
     for (auto& e : prof.pool) {
       cudaEventDestroy(e.first);
@@ -195,7 +204,7 @@ struct gg_ctx {
     tables_ready = false;
     for (DevBuf* b : {&b_fp64, &b_hi, &b_lo, &inv_col, &a_hi, &a_lo, &inv_row, &pts, &jt, &rho, &divt, &jv, &phi, &gx,
                       &gy, &gz, &lap, &w64, &plane_rows, &plane_out, &sort_keys, &sort_keys2, &sort_idx, &sort_perm,
-                      &sort_temp, &pts_sorted, &tile_lists, &tile_ord})
+                      &sort_temp, &pts_sorted, &tile_lists, &tile_ord, &pts2, &jt2, &rho2, &divt2})
       b->release();
     if (d_err) cudaFree(d_err);
     d_err = nullptr;
@@ -584,6 +593,7 @@ struct gg_ctx {
     const bool dev_out = (!jto || is_device_ptr(jto)) && (!rhoo || is_device_ptr(rhoo)) &&
                          (!divo || is_device_ptr(divo));
     const int64_t batch = precision == GG_PREC_FP64 ? std::min<int64_t>(max_batch, 16384) : max_batch;
+    if (!dev_in && !dev_out && n > batch) return jtensor_overlapped(p, n, batch, jto, rhoo, divo, st);
     cudaError_t e;
     for (int64_t off = 0; off < n; off += batch) {
       const int64_t m = std::min(batch, n - off);
@@ -629,6 +639,69 @@ struct gg_ctx {
         if ((rc = check_device_error(st))) return rc;
       }
     }
+    return check_device_error(st);
+  }
+
+  // Host inputs and outputs over several batches: the input and output
+  // copies run on two more streams and overlap the evaluation of the
+  // neighbouring batches (two staging slots; batch b uses slot b % 2).  Per slot, the input copy waits
+  // until the evaluation of batch b - 2 has read the points, the evaluation
+  // waits for its input copy and for the output copy of batch b - 2, and the
+  // output copy waits for the evaluation.
+  template <typename T>
+  int jtensor_overlapped(const double* p, int64_t n, int64_t batch, T* jto, T* rhoo, T* divo, cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
+    if (!copy_stream) e = cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !out_stream) e = cudaStreamCreateWithFlags(&out_stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+      for (cudaEvent_t* ev : {&ev_in[i], &ev_done[i], &ev_out[i]})
+        if (!*ev && e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    DevBuf* sp[2] = {&pts, &pts2};
+    DevBuf* sj[2] = {&jt, &jt2};
+    DevBuf* sr[2] = {&rho, &rho2};
+    DevBuf* sd[2] = {&divt, &divt2};
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+      e = sp[i]->reserve(static_cast<size_t>(batch) * 3 * sizeof(double));
+      if (e == cudaSuccess && jto) e = sj[i]->reserve(static_cast<size_t>(batch) * 9 * sizeof(T));
+      if (e == cudaSuccess && rhoo) e = sr[i]->reserve(static_cast<size_t>(batch) * sizeof(T));
+      if (e == cudaSuccess && divo) e = sd[i]->reserve(static_cast<size_t>(batch) * 3 * sizeof(T));
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "overlapped staging");
+    int b = 0;
+    for (int64_t off = 0; off < n; off += batch, ++b) {
+      const int64_t m = std::min(batch, n - off);
+      const int s = b & 1;
+      if (b >= 2) e = cudaStreamWaitEvent(copy_stream, ev_done[s], 0);  // batch b-2 has read its points
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(sp[s]->p, p + 3 * off, static_cast<size_t>(m) * 3 * sizeof(double),
+                            cudaMemcpyHostToDevice, copy_stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev_in[s], copy_stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_in[s], 0);
+      if (e == cudaSuccess && b >= 2) e = cudaStreamWaitEvent(st, ev_out[s], 0);  // slot's outputs copied out
+      if (e != cudaSuccess) return cuda_fail(e, "overlapped input copy");
+      gg::Outputs out{nullptr, nullptr, nullptr};
+      set_outputs(&out, jto ? sj[s]->as<T>() : nullptr, rhoo ? sr[s]->as<T>() : nullptr,
+                  divo ? sd[s]->as<T>() : nullptr);
+      int rc = run_batch(sp[s]->as<double>(), m, out, st);
+      if (rc) {
+        cudaStreamSynchronize(copy_stream);
+        cudaStreamSynchronize(out_stream);
+        return rc;
+      }
+      e = cudaEventRecord(ev_done[s], st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(out_stream, ev_done[s], 0);
+      if (e == cudaSuccess && jto)
+        e = cudaMemcpyAsync(jto + 9 * off, sj[s]->p, m * 9 * sizeof(T), cudaMemcpyDeviceToHost, out_stream);
+      if (e == cudaSuccess && rhoo)
+        e = cudaMemcpyAsync(rhoo + off, sr[s]->p, m * sizeof(T), cudaMemcpyDeviceToHost, out_stream);
+      if (e == cudaSuccess && divo)
+        e = cudaMemcpyAsync(divo + 3 * off, sd[s]->p, m * 3 * sizeof(T), cudaMemcpyDeviceToHost, out_stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev_out[s], out_stream);
+      if (e != cudaSuccess) return cuda_fail(e, "overlapped output copy");
+    }
+    e = cudaStreamSynchronize(copy_stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(out_stream);
+    if (e != cudaSuccess) return cuda_fail(e, "overlapped copies");
     return check_device_error(st);
   }
 

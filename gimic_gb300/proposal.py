@@ -278,8 +278,8 @@ def sample_plane(gimic, region, n, rng, core_frac=0.5, floor=J_FLOOR):
 # proposal builds the same set): the cheapest rule of a grid search over
 # kappa, initial panels, tau, depth and orders with every training plane
 # within 0.01 nA/T of its 200 x 200 uniform judge (largest error 0.0075).
-DEFAULT_RULE = {"mode": "mass", "kappa_u": 2.0, "kappa_v": 2.0, "tau": 1.0, "q_hi": 7, "q_lo": 4, "frac": 0.02,
-                "max_depth": 1, "n0u": 3, "n0v": 3, "lattice": 96, "tau_s": 1e-3}
+DEFAULT_RULE = {"mode": "mass", "kappa_u": 2.0, "kappa_v": 2.0, "tau": 1.0, "q_hi": 7, "q_hi_v": None, "q_lo": 4,
+                "frac": 0.02, "max_depth": 1, "n0u": 3, "n0v": 3, "lattice": 96, "tau_s": 1e-3}
 
 
 class AxisMap:
@@ -361,8 +361,9 @@ def propose_panels(mass, region, rule=None):
     mapped coordinates.  The mapped domain starts as n0u x n0v panels; a
     panel is split in four while its predicted current mass exceeds ``tau``
     (nA/T) and it is shallower than ``max_depth``; a leaf gets ``q_hi``
-    Gauss-Lobatto points per axis when its mass exceeds frac * tau, else
-    ``q_lo``.  Returns (map_u, map_v, [(ta, tb, wa, wb, q)])."""
+    Gauss-Lobatto points along u and ``q_hi_v`` (default q_hi) along v when
+    its mass exceeds frac * tau, else ``q_lo`` along both.  Returns
+    (map_u, map_v, [(ta, tb, wa, wb, q_u, q_v)])."""
     r = dict(DEFAULT_RULE, **(rule or {}))
     mu, mv = estimate_maps(mass, region, r)
     table = _MassTable(mass, region)
@@ -377,8 +378,10 @@ def propose_panels(mass, region, rule=None):
             tm, wm = 0.5 * (ta + tb), 0.5 * (wa + wb)
             stack += [(ta, tm, wa, wm, d + 1), (tm, tb, wa, wm, d + 1), (ta, tm, wm, wb, d + 1),
                       (tm, tb, wm, wb, d + 1)]
+        elif m > r["frac"] * r["tau"]:
+            panels.append((ta, tb, wa, wb, r["q_hi"], r["q_hi_v"] or r["q_hi"]))
         else:
-            panels.append((ta, tb, wa, wb, r["q_hi"] if m > r["frac"] * r["tau"] else r["q_lo"]))
+            panels.append((ta, tb, wa, wb, r["q_lo"], r["q_lo"]))
     return mu, mv, panels
 
 
@@ -430,14 +433,14 @@ def propose_panels_surrogate(net, gimic, region, mass, rule=None):
             else:
                 leaves.append(pn)
         todo = nxt
-    return mu, mv, [(ta, tb, wa, wb, q) for ta, tb, wa, wb in leaves]
+    return mu, mv, [(ta, tb, wa, wb, q, q) for ta, tb, wa, wb in leaves]
 
 
 def panel_planes(region, mu, mv, panels):
     """Each mapped panel as a plane for Gimic.plane_integrals."""
     out = []
-    for ta, tb, wa, wb, q in panels:
-        ax = [mu.nodes(ta, tb, q), mv.nodes(wa, wb, q), (np.zeros(1), np.ones(1))]
+    for ta, tb, wa, wb, qu, qv in panels:
+        ax = [mu.nodes(ta, tb, qu), mv.nodes(wa, wb, qv), (np.zeros(1), np.ones(1))]
         out.append((region.origin, region.basis(), ax, region.radius))
     return out
 
@@ -481,7 +484,7 @@ def integrate_adaptive(gimic, net, region, rule=None, min_inside=0.99, fallback_
             else:
                 mu, mv, panels = propose_panels(mass, region, r)
             cur = integrate_panels(gimic, region, mu, mv, panels)
-            return {"current": cur, "points": int(sum(p[4] ** 2 for p in panels)), "panels": panels,
+            return {"current": cur, "points": int(sum(p[4] * p[5] for p in panels)), "panels": panels,
                     "maps": (mu, mv), "method": "adaptive", "inside": inside}
     cur = integrate_uniform(gimic, region, fallback_npts)
     return {"current": cur, "points": fallback_npts * fallback_npts, "panels": None, "method": "uniform-fallback",

@@ -50,9 +50,9 @@ def test_oracle_adam_first_step_is_signed_lr():
 
 def _mapped_rule_sum(P, reg, mu, mv, panels, f):
     tot = 0.0
-    for ta, tb, wa, wb, q in panels:
-        x, wx = mu.nodes(ta, tb, q)
-        y, wy = mv.nodes(wa, wb, q)
+    for ta, tb, wa, wb, qu, qv in panels:
+        x, wx = mu.nodes(ta, tb, qu)
+        y, wy = mv.nodes(wa, wb, qv)
         tot += np.sum(np.outer(wx, wy) * f(x[:, None], y[None, :]))
     return tot
 
@@ -83,7 +83,7 @@ def test_mapped_quadtree_integrates_a_peaked_function():
     assert abs(mu.x(mu.t0)) < 1e-12 and abs(mu.x(mu.t1) - reg.lx) < 1e-9
     assert abs(mv.x(mv.t0)) < 1e-12 and abs(mv.x(mv.t1) - reg.ly) < 1e-9
     assert abs(mu.c - c) < 0.2 and abs(mv.c - d) < 0.2
-    n = sum(p[4] ** 2 for p in panels)
+    n = sum(p[4] * p[5] for p in panels)
     assert n == 324
     got = _mapped_rule_sum(P, reg, mu, mv, panels, f)
     assert abs(got - exact) < 1e-4 * exact, (got, exact)
@@ -105,13 +105,16 @@ def test_quadtree_refines_where_the_mass_is():
     rule = dict(kappa_u=None, kappa_v=None, n0u=1, n0v=1, max_depth=4, tau=2.0, q_hi=10, q_lo=4, frac=0.02)
     mu, mv, pan = P.propose_panels(m, reg, rule)
     assert mu.s is None and mv.s is None  # identity maps: panels in plane coordinates
-    area = sum((tb - ta) * (wb - wa) for ta, tb, wa, wb, _ in pan)
+    area = sum((tb - ta) * (wb - wa) for ta, tb, wa, wb, _, _ in pan)
     assert abs(area - 160.0) < 1e-9
-    assert {q for *_, q in pan} == {4, 10}
+    assert {p[4] for p in pan} == {4, 10} and all(p[4] == p[5] for p in pan)
     hot = [p for p in pan if p[0] < 8.5 and p[1] > 7.5 and p[2] < 4.375 and p[3] > 3.125]
     assert hot and all(p[4] == 10 and abs(p[1] - p[0] - 1.0) < 1e-12 for p in hot)
     mu, mv, pan = P.propose_panels(np.full((64, 64), 1e-9), reg, rule)
-    assert len(pan) == 1 and pan[0][4] == 4
+    assert len(pan) == 1 and pan[0][4:] == (4, 4)
+    # different orders along the two axes
+    _, _, pan = P.propose_panels(m, reg, dict(rule, q_hi_v=6))
+    assert {(p[4], p[5]) for p in pan} == {(4, 4), (10, 6)}
 
 
 # ---------------------------------------------------------------------------
