@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--cpu-sample", type=int, default=8192)
+    ap.add_argument("--batch", type=int, default=0, help="points per device pass (0: the library default)")
     ap.add_argument("--config", default="cube", choices=("cube", "scan", "large", "proposal"),
                     help="cube: the C24H24 128^3 cube (default); scan: batched bond-current profile scans")
     ap.add_argument("--molecules", type=int, default=16, help="molecules of the scan batch")
@@ -269,6 +270,8 @@ def run_large(args):
     build.build()
     mp, xp, mol = synth.make_workload("c96h24", args.data, seed=2024)
     g = api.Gimic(mp, xp, screening=1e-8, precision="split16")
+    if args.batch:
+        g.set_max_batch(args.batch)
     dev = torch.device("cuda", 0)
     ax = torch.arange(256, dtype=torch.float64, device=dev) * 0.1 - 12.75
     Z, Y, X = torch.meshgrid(ax, ax, ax, indexing="ij")
@@ -427,6 +430,8 @@ def run_profile_case(args):
     build.build()
     mp, xp, mol = synth.make_workload("c24h24", args.data, seed=2024)
     g = api.Gimic(mp, xp, screening=1e-8, precision="split16")
+    if args.batch:
+        g.set_max_batch(args.batch)
     P = torch.as_tensor(cube_points_np()[::32].copy(), device="cuda")
     for _ in range(2):
         g.jtensor_batch(P, rho=True, divj=True)
@@ -471,6 +476,8 @@ def main():
     mp, xp, mol = synth.make_workload("c24h24", args.data, seed=2024)
     n = mol.nbf
     g = api.Gimic(mp, xp, screening=1e-8, precision="split16")
+    if args.batch:
+        g.set_max_batch(args.batch)
     g.set_magnet([0.0, 0.0, 1.0])
     dev = torch.device("cuda", local)
     pts_np = cube_points_np()

@@ -128,12 +128,28 @@ struct gg_ctx {
   CUtensorMap tm_b_hi, tm_b_lo;
 
   // scratch
-  DevBuf a_hi, a_lo, inv_row, pts, jt, rho, divt, jv;
+  DevBuf pts, jt, rho, divt, jv;
+  // Per-batch scratch of the split path.  Two slots let the ordering,
+  // screening and basis evaluation of batch b+1 (on the auxiliary stream) run
+  // while the contraction of batch b runs on the caller's stream.
+  struct SplitSlot {
+    DevBuf a_hi, a_lo, inv_row, sort_keys, sort_keys2, sort_idx, sort_perm, sort_temp, pts_sorted, tile_lists,
+        tile_ord;
+    CUtensorMap tma_hi, tma_lo;
+    const double* tp = nullptr;
+    const int* tiles = nullptr;
+    const int* perm = nullptr;
+    const int* tord = nullptr;
+    int stride = 0;
+    int64_t n = 0;
+    bool used = false;  // a contraction has been enqueued on this slot
+    cudaEvent_t prepared = nullptr, consumed = nullptr;
+  } slot[2];
+  cudaStream_t aux_stream = nullptr;
   // second staging slot and copy stream of the overlapped host-buffer path
   DevBuf pts2, jt2, rho2, divt2;
   cudaStream_t copy_stream = nullptr, out_stream = nullptr;
   cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
-  DevBuf sort_keys, sort_keys2, sort_idx, sort_perm, sort_temp, pts_sorted, tile_lists, tile_ord;
   DevBuf phi, gx, gy, gz, lap, w64;
   DevBuf plane_rows, plane_out;
   int* d_err = nullptr;
@@ -188,6 +204,10 @@ struct gg_ctx {
     for (int i = 0; i < 2; ++i)
       for (cudaEvent_t ev : {ev_in[i], ev_done[i], ev_out[i]})
         if (ev) cudaEventDestroy(ev);
+    for (SplitSlot& sl : slot)
+      for (cudaEvent_t ev : {sl.prepared, sl.consumed})
+        if (ev) cudaEventDestroy(ev);
+    if (aux_stream) cudaStreamDestroy(aux_stream);
     if (copy_stream) cudaStreamDestroy(copy_stream);
     if (out_stream) cudaStreamDestroy(out_stream);
     if (prof.d_blocks) cudaFree(prof.d_blocks);
@@ -202,10 +222,15 @@ struct gg_ctx {
     for (void* p : table_allocs) cudaFree(p);
     table_allocs.clear();
     tables_ready = false;
-    for (DevBuf* b : {&b_fp64, &b_hi, &b_lo, &inv_col, &a_hi, &a_lo, &inv_row, &pts, &jt, &rho, &divt, &jv, &phi, &gx,
-                      &gy, &gz, &lap, &w64, &plane_rows, &plane_out, &sort_keys, &sort_keys2, &sort_idx, &sort_perm,
-                      &sort_temp, &pts_sorted, &tile_lists, &tile_ord, &pts2, &jt2, &rho2, &divt2})
+    for (DevBuf* b : {&b_fp64, &b_hi, &b_lo, &inv_col, &pts, &jt, &rho, &divt, &jv, &phi, &gx, &gy, &gz, &lap, &w64,
+                      &plane_rows, &plane_out, &pts2, &jt2, &rho2, &divt2})
       b->release();
+    for (SplitSlot& sl : slot) {
+      for (DevBuf* b : {&sl.a_hi, &sl.a_lo, &sl.inv_row, &sl.sort_keys, &sl.sort_keys2, &sl.sort_idx, &sl.sort_perm,
+                        &sl.sort_temp, &sl.pts_sorted, &sl.tile_lists, &sl.tile_ord})
+        b->release();
+      sl.used = false;
+    }
     if (d_err) cudaFree(d_err);
     d_err = nullptr;
     mats_spin = -1;
@@ -490,79 +515,143 @@ struct gg_ctx {
     if (dB.kpad > 64 * gg::kBlockK)
       return fail(GG_EUNSUPPORTED, "the split-FP16 path handles at most 4096 basis functions (nbf=" +
                                        std::to_string(basis.nbf) + "); use the FP64 precision");
+    int rc = prep_split(slot[0], d_pts, n, st);
+    if (rc) return rc;
+    rc = tc_split(slot[0], out, st, gg::tc_table_budget());
+    if (rc == GG_OK) slot[0].used = false;  // ordered on `st` itself
+    return rc;
+  }
+
+  // Ordering, tile screening and basis evaluation of one batch into a slot.
+  int prep_split(SplitSlot& sl, const double* d_pts, int64_t n, cudaStream_t st) {
+    cudaError_t e;
     const size_t abytes = static_cast<size_t>(n) * dB.kpad * sizeof(__half);
-    e = a_hi.reserve(abytes);
-    if (e == cudaSuccess) e = a_lo.reserve(abytes);
-    if (e == cudaSuccess) e = inv_row.reserve(static_cast<size_t>(n) * sizeof(float));
+    e = sl.a_hi.reserve(abytes);
+    if (e == cudaSuccess) e = sl.a_lo.reserve(abytes);
+    if (e == cudaSuccess) e = sl.inv_row.reserve(static_cast<size_t>(n) * sizeof(float));
     if (e != cudaSuccess) return cuda_fail(e, "split-path scratch");
-    size_t slot = 0;
+    size_t ps = 0;
     // Tile screening: order the points along a Z curve so that tiles are
     // compact, then list the shells each tile can see (k_tiles.cu).
     const int stride = gg::tile_stride(dB);
     const bool screen = tile_screening && stride <= 512;
-    const double* tp = d_pts;
-    const int* tiles = nullptr;
-    const int* perm = nullptr;
+    sl.n = n;
+    sl.stride = stride;
+    sl.tp = d_pts;
+    sl.tiles = nullptr;
+    sl.perm = nullptr;
+    sl.tord = nullptr;
     if (screen) {
       const int64_t ntiles = (n + gg::kBlockM - 1) / gg::kBlockM;
       const size_t tb = std::max(gg::sort_temp_bytes(n), gg::tile_order_temp_bytes(ntiles));
-      e = sort_keys.reserve(n * sizeof(uint32_t));
-      if (e == cudaSuccess) e = sort_keys2.reserve(n * sizeof(uint32_t));
-      if (e == cudaSuccess) e = sort_idx.reserve(n * sizeof(int));
-      if (e == cudaSuccess) e = sort_perm.reserve(n * sizeof(int));
-      if (e == cudaSuccess) e = sort_temp.reserve(std::max<size_t>(tb, 16));
-      if (e == cudaSuccess) e = pts_sorted.reserve(static_cast<size_t>(n) * 3 * sizeof(double));
-      if (e == cudaSuccess) e = tile_lists.reserve(static_cast<size_t>(ntiles) * stride * sizeof(int));
-      if (e == cudaSuccess) e = tile_ord.reserve(static_cast<size_t>(ntiles) * sizeof(int));
+      e = sl.sort_keys.reserve(n * sizeof(uint32_t));
+      if (e == cudaSuccess) e = sl.sort_keys2.reserve(n * sizeof(uint32_t));
+      if (e == cudaSuccess) e = sl.sort_idx.reserve(n * sizeof(int));
+      if (e == cudaSuccess) e = sl.sort_perm.reserve(n * sizeof(int));
+      if (e == cudaSuccess) e = sl.sort_temp.reserve(std::max<size_t>(tb, 16));
+      if (e == cudaSuccess) e = sl.pts_sorted.reserve(static_cast<size_t>(n) * 3 * sizeof(double));
+      if (e == cudaSuccess) e = sl.tile_lists.reserve(static_cast<size_t>(ntiles) * stride * sizeof(int));
+      if (e == cudaSuccess) e = sl.tile_ord.reserve(static_cast<size_t>(ntiles) * sizeof(int));
       if (e != cudaSuccess) return cuda_fail(e, "tile-screening scratch");
       double lo[3] = {0, 0, 0};
       for (const gg::Atom& a : basis.atoms)
         for (int d = 0; d < 3; ++d) lo[d] += a.coord[d] / static_cast<double>(basis.atoms.size());
       for (int d = 0; d < 3; ++d) lo[d] -= 64.0;  // 1024 cells of 0.125 Bohr around the molecule
-      prof_begin(GG_PROF_ORDER, st, &slot);
-      e = gg::launch_spatial_order(d_pts, n, lo, 0.125, sort_keys.as<uint32_t>(), sort_keys2.as<uint32_t>(),
-                                   sort_idx.as<int>(), sort_perm.as<int>(), sort_temp.p, tb,
-                                   pts_sorted.as<double>(), st);
+      prof_begin(GG_PROF_ORDER, st, &ps);
+      e = gg::launch_spatial_order(d_pts, n, lo, 0.125, sl.sort_keys.as<uint32_t>(), sl.sort_keys2.as<uint32_t>(),
+                                   sl.sort_idx.as<int>(), sl.sort_perm.as<int>(), sl.sort_temp.p, tb,
+                                   sl.pts_sorted.as<double>(), st);
       if (e != cudaSuccess) return cuda_fail(e, "spatial ordering");
-      gg::launch_tile_screen(dB, pts_sorted.as<double>(), n, tile_lists.as<int>(), st);
+      gg::launch_tile_screen(dB, sl.pts_sorted.as<double>(), n, sl.tile_lists.as<int>(), st);
       // heaviest tiles first; the key/index scratch of the point sort is reused
-      e = gg::launch_tile_order(tile_lists.as<int>(), ntiles, stride, sort_keys.as<uint32_t>(),
-                                sort_keys2.as<uint32_t>(), sort_idx.as<int>(), tile_ord.as<int>(), sort_temp.p, tb,
-                                st);
+      e = gg::launch_tile_order(sl.tile_lists.as<int>(), ntiles, stride, sl.sort_keys.as<uint32_t>(),
+                                sl.sort_keys2.as<uint32_t>(), sl.sort_idx.as<int>(), sl.tile_ord.as<int>(),
+                                sl.sort_temp.p, tb, st);
       if (e != cudaSuccess) return cuda_fail(e, "tile ordering");
-      prof_end(st, slot);
-      if (prof.on && prof.d_blocks) gg::launch_tile_work(tile_lists.as<int>(), ntiles, stride, prof.d_blocks, st);
+      prof_end(st, ps);
+      if (prof.on && prof.d_blocks) gg::launch_tile_work(sl.tile_lists.as<int>(), ntiles, stride, prof.d_blocks, st);
       launches += 6;
-      tp = pts_sorted.as<double>();
-      tiles = tile_lists.as<int>();
-      perm = sort_perm.as<int>();
+      sl.tp = sl.pts_sorted.as<double>();
+      sl.tiles = sl.tile_lists.as<int>();
+      sl.perm = sl.sort_perm.as<int>();
+      sl.tord = sl.tile_ord.as<int>();
     }
-    CUtensorMap tma_hi, tma_lo;
-    if (!encode_fp16_2d(&tma_hi, a_hi.p, n, dB.kpad, gg::kBlockM) ||
-        !encode_fp16_2d(&tma_lo, a_lo.p, n, dB.kpad, gg::kBlockM))
+    if (!encode_fp16_2d(&sl.tma_hi, sl.a_hi.p, n, dB.kpad, gg::kBlockM) ||
+        !encode_fp16_2d(&sl.tma_lo, sl.a_lo.p, n, dB.kpad, gg::kBlockM))
       return fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
-    prof_begin(GG_PROF_BASIS, st, &slot);
-    e = gg::launch_basis_tile(dB, &tma_hi, &tma_lo, tp, n, tiles, stride, inv_row.as<float>(), st);
-    prof_end(st, slot);
+    prof_begin(GG_PROF_BASIS, st, &ps);
+    e = gg::launch_basis_tile(dB, &sl.tma_hi, &sl.tma_lo, sl.tp, n, sl.tiles, stride, sl.inv_row.as<float>(), st);
+    prof_end(st, ps);
     if (e != cudaSuccess) return cuda_fail(e, "basis kernel launch");
-    gg::TcArgs ta{&tma_hi, &tma_lo, &tm_b_hi, &tm_b_lo, inv_row.as<float>(), inv_col.as<float>(),
-                  tp,      n,       flags,    out,      d_err};
-    ta.tiles = tiles;
-    ta.tile_stride = stride;
-    ta.perm = perm;
-    ta.tile_order = screen ? tile_ord.as<int>() : nullptr;
+    launches += 1;
+    return GG_OK;
+  }
+
+  // The contraction of a prepared slot; table_bytes of shared memory for the
+  // epilogue's tables (0: they stay in global memory).
+  int tc_split(SplitSlot& sl, gg::Outputs out, cudaStream_t st, int table_bytes) {
+    gg::TcArgs ta{&sl.tma_hi, &sl.tma_lo, &tm_b_hi, &tm_b_lo, sl.inv_row.as<float>(), inv_col.as<float>(),
+                  sl.tp,       sl.n,       flags,    out,      d_err};
+    ta.tiles = sl.tiles;
+    ta.tile_stride = sl.stride;
+    ta.perm = sl.perm;
+    ta.tile_order = sl.tord;
+    ta.table_bytes = table_bytes;
     if (prof.on) {
-      const unsigned long long blocks = static_cast<unsigned long long>((n + gg::kBlockM - 1) / gg::kBlockM) *
+      const unsigned long long blocks = static_cast<unsigned long long>((sl.n + gg::kBlockM - 1) / gg::kBlockM) *
                                         dB.nchunk * (dB.kpad / gg::kBlockK);
       prof.dense_blocks += blocks;
-      if (!screen && prof.d_blocks) prof_add_blocks(blocks, st);
+      if (!sl.tiles && prof.d_blocks) prof_add_blocks(blocks, st);
     }
-    prof_begin(GG_PROF_TC, st, &slot);
-    e = gg::launch_tc_fused(dB, ta, st);
-    prof_end(st, slot);
+    size_t ps = 0;
+    prof_begin(GG_PROF_TC, st, &ps);
+    cudaError_t e = gg::launch_tc_fused(dB, ta, st);
+    prof_end(st, ps);
     if (e != cudaSuccess) return cuda_fail(e, "tensor-core kernel launch");
-    launches += 2;
+    launches += 1;
     return GG_OK;
+  }
+
+  // Batch b of a multi-batch call.  On the split path the preparation of the
+  // batch runs on the auxiliary stream (after `input_ready`, when given, and
+  // after the previous contraction of the same slot) and the contraction on
+  // `st`, so batch b+1 is prepared while batch b is contracted.  Those
+  // contractions leave the epilogue's tables in global memory: the smaller
+  // shared-memory request lets a basis CTA share each SM with them.
+  int pipe_batch(int b, const double* d_pts, int64_t n, gg::Outputs out, cudaStream_t st,
+                 cudaEvent_t input_ready = nullptr) {
+    cudaError_t e = cudaSuccess;
+    if (precision == GG_PREC_FP64) {
+      if (input_ready) e = cudaStreamWaitEvent(st, input_ready, 0);
+      if (e != cudaSuccess) return cuda_fail(e, "batch input wait");
+      return run_batch(d_pts, n, out, st);
+    }
+    if ((out.divt || out.divt32) && !(flags.giao && flags.dia && flags.para))
+      return fail(GG_EUNSUPPORTED, "div j needs GIAO, diamagnetic and paramagnetic terms on");
+    if (dB.kpad > 64 * gg::kBlockK)
+      return fail(GG_EUNSUPPORTED, "the split-FP16 path handles at most 4096 basis functions (nbf=" +
+                                       std::to_string(basis.nbf) + "); use the FP64 precision");
+    if (!aux_stream) e = cudaStreamCreateWithFlags(&aux_stream, cudaStreamNonBlocking);
+    SplitSlot& sl = slot[b & 1];
+    for (cudaEvent_t* ev : {&sl.prepared, &sl.consumed})
+      if (!*ev && e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    if (e == cudaSuccess && sl.used) e = cudaStreamWaitEvent(aux_stream, sl.consumed, 0);
+    if (e == cudaSuccess && input_ready) e = cudaStreamWaitEvent(aux_stream, input_ready, 0);
+    // the preparation may start only once work already queued on `st` that
+    // produced d_pts is done
+    if (e == cudaSuccess) e = cudaEventRecord(sl.prepared, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux_stream, sl.prepared, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "batch pipeline");
+    int rc = prep_split(sl, d_pts, n, aux_stream);
+    if (rc) return rc;
+    e = cudaEventRecord(sl.prepared, aux_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, sl.prepared, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "batch pipeline");
+    rc = tc_split(sl, out, st, 0);
+    if (rc) return rc;
+    sl.used = true;
+    e = cudaEventRecord(sl.consumed, st);
+    return e == cudaSuccess ? GG_OK : cuda_fail(e, "batch pipeline");
   }
 
   int64_t launches = 0;  // kernels launched by this context
@@ -595,7 +684,8 @@ struct gg_ctx {
     const int64_t batch = precision == GG_PREC_FP64 ? std::min<int64_t>(max_batch, 16384) : max_batch;
     if (!dev_in && !dev_out && n > batch) return jtensor_overlapped(p, n, batch, jto, rhoo, divo, st);
     cudaError_t e;
-    for (int64_t off = 0; off < n; off += batch) {
+    int b = 0;
+    for (int64_t off = 0; off < n; off += batch, ++b) {
       const int64_t m = std::min(batch, n - off);
       const double* dp = p + 3 * off;
       if (!dev_in) {
@@ -626,7 +716,7 @@ struct gg_ctx {
       }
       gg::Outputs out{nullptr, nullptr, nullptr};
       set_outputs(&out, dj, dr, dd);
-      rc = run_batch(dp, m, out, st);
+      rc = n > batch ? pipe_batch(b, dp, m, out, st) : run_batch(dp, m, out, st);
       if (rc) return rc;
       if (!dev_out) {
         e = cudaSuccess;
@@ -682,7 +772,7 @@ struct gg_ctx {
       gg::Outputs out{nullptr, nullptr, nullptr};
       set_outputs(&out, jto ? sj[s]->as<T>() : nullptr, rhoo ? sr[s]->as<T>() : nullptr,
                   divo ? sd[s]->as<T>() : nullptr);
-      int rc = run_batch(sp[s]->as<double>(), m, out, st);
+      int rc = pipe_batch(b, sp[s]->as<double>(), m, out, st, ev_in[s]);
       if (rc) {
         cudaStreamSynchronize(copy_stream);
         cudaStreamSynchronize(out_stream);
@@ -877,9 +967,11 @@ int gg_properties(gg_ctx* ctx, const double* pts, const double* wgt, int64_t n, 
     e = cudaMemcpyAsync(doff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "copying the property grid");
   const int64_t batch = ctx->precision == GG_PREC_FP64 ? std::min<int64_t>(ctx->max_batch, 16384) : ctx->max_batch;
-  for (int64_t o = 0; o < n; o += batch) {
+  for (int64_t o = 0, b = 0; o < n; o += batch, ++b) {
     const int64_t m = std::min(batch, n - o);
-    rc = ctx->run_batch(ctx->pts.as<double>() + 3 * o, m, ctx->jt.as<double>() + 9 * o, nullptr, nullptr, st);
+    const gg::Outputs out{ctx->jt.as<double>() + 9 * o, nullptr, nullptr};
+    rc = n > batch ? ctx->pipe_batch(static_cast<int>(b), ctx->pts.as<double>() + 3 * o, m, out, st)
+                   : ctx->run_batch(ctx->pts.as<double>() + 3 * o, m, out, st);
     if (rc) return rc;
   }
   gg::launch_properties(ctx->jt.as<double>(), ctx->pts.as<double>(), dw, dc, ncentres, doff, nb, dsig, dchi, st);
@@ -992,9 +1084,11 @@ int gg_plane_integrals(gg_ctx* ctx, const gg_grid* grids, int nplanes, double* o
     e = cudaMemcpyAsync(drp, row_plane.data(), row_plane.size() * sizeof(int), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane points");
   const int64_t batch = ctx->precision == GG_PREC_FP64 ? std::min<int64_t>(ctx->max_batch, 16384) : ctx->max_batch;
-  for (int64_t off = 0; off < npts; off += batch) {
+  for (int64_t off = 0, b = 0; off < npts; off += batch, ++b) {
     const int64_t m = std::min(batch, npts - off);
-    rc = ctx->run_batch(ctx->pts.as<double>() + 3 * off, m, ctx->jt.as<double>() + 9 * off, nullptr, nullptr, st);
+    const gg::Outputs out{ctx->jt.as<double>() + 9 * off, nullptr, nullptr};
+    rc = npts > batch ? ctx->pipe_batch(static_cast<int>(b), ctx->pts.as<double>() + 3 * off, m, out, st)
+                      : ctx->run_batch(ctx->pts.as<double>() + 3 * off, m, out, st);
     if (rc) return rc;
   }
   size_t slot = 0;
@@ -1293,6 +1387,7 @@ extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t 
   if (e != cudaSuccess) return ctx->cuda_fail(e, "basis kernel launch");
   gg::TcArgs ta{&tma_hi, &tma_lo, &ctx->tm_b_hi, &ctx->tm_b_lo, inv_row, ctx->inv_col.as<float>(),
                 pts,     n,       ctx->flags,     gg::Outputs{jt, rho, divt}, ctx->d_err};
+  ta.table_bytes = gg::tc_table_budget();
   e = gg::launch_tc_fused(ctx->dB, ta, st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "tensor-core kernel launch");
   ctx->launches += 2;

@@ -20,7 +20,6 @@ constexpr int kNDots = 37;
 // bound, K blocks staged in shared memory and written with TMA tensor stores
 // through the point operand's own tensor maps; with tile lists, inactive K
 // blocks are skipped.
-int basis_tile_smem_bytes();
 cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* tm_lo, const double* pts,
                               int64_t npts, const int* tiles, int stride, float* inv_scale, cudaStream_t st);
 // phi, grad phi and the Laplacian in fp64 for the plain FP64 path.
@@ -54,8 +53,11 @@ struct TcArgs {
   int tile_stride = 0;
   const int* perm = nullptr;   // output index of each (sorted) point (null: identity)
   const int* tile_order = nullptr;  // tile processed by each CTA (null: CTA i -> tile i)
+  int table_bytes = 0;              // shared memory for the epilogue's tables (0: global memory)
 };
 int tc_smem_bytes();
+// Shared memory left for the epilogue's tables next to the pipeline stages.
+int tc_table_budget();
 
 // Spatial ordering and tile screening (k_tiles.cu)
 int tile_stride(const DevBasis& B);

@@ -210,8 +210,6 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
   if (threadIdx.x == 0) bulk_wait_all();
 }
 
-int basis_tile_smem_bytes() { return kTileSmem; }
-
 cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* tm_lo, const double* pts,
                               int64_t npts, const int* tiles, int stride, float* inv_scale, cudaStream_t st) {
   if (npts <= 0) return cudaSuccess;

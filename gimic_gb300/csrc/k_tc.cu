@@ -18,6 +18,8 @@
 //               gg_combine.cuh (src/libgimic/jtensor.F90:148-237).
 #include <cuda.h>
 
+#include <algorithm>
+
 #include "gg_cart.cuh"
 #include "gg_combine.cuh"
 #include "gg_kernels.h"
@@ -41,7 +43,7 @@ constexpr int kSmemFixed = kStages * kStageBytes + 1024 + 256 + kMaxTileList * 4
 // well when those fit too; otherwise the epilogue reads them from global
 // memory.
 constexpr int kSmemTables = 227 * 1024 - kSmemFixed;
-constexpr int kSmemBytes = kSmemFixed + kSmemTables;
+constexpr int kSmemBytes = kSmemFixed + kSmemTables;  // upper bound of the dynamic request
 static_assert(kBlockM * kNDots * 8 <= kStageBytes, "epilogue reduction buffer must fit in one stage");
 
 __device__ __forceinline__ void tmem_ld1(uint32_t taddr, float& v) {
@@ -72,6 +74,7 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 }  // namespace
 
 int tc_smem_bytes() { return kSmemBytes; }
+int tc_table_budget() { return kSmemTables; }
 
 // Per chunk the MMAs run in two passes over K into the same accumulator:
 // first the two small cross products (hi*lo, lo*hi), then the main product
@@ -85,7 +88,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     DevBasis Bs, const float* __restrict__ inv_row, const float* __restrict__ inv_col,
                     const double* __restrict__ pts, int64_t npts, Flags fl, Outputs out, int* err,
                     const int* __restrict__ tiles, int tstride, const int* __restrict__ perm,
-                    const int* __restrict__ tile_order) {
+                    const int* __restrict__ tile_order, int table_bytes) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                          ~static_cast<uintptr_t>(1023));
@@ -117,12 +120,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int* klist = tlist + 2 + nchunk_all;
   // column scales and per-function records (shell << 12 | packed ijk)
   const int ncol = nchunk_all * kBlockN;
-  const bool tables_in_smem = (ncol + Bs.nbf) * 4 <= kSmemTables;
+  const bool tables_in_smem = (ncol + Bs.nbf) * 4 <= table_bytes;
   const float* icol = inv_col;
   const int* fpack = Bs.f_pack;
   // shell records, screening radii, primitives and atoms too when they fit
   const int shell_bytes = Bs.nshells * (16 + 8) + Bs.nprim * 16 + Bs.natoms * 24;
-  const bool shells_in_smem = tables_in_smem && (ncol + Bs.nbf) * 4 + shell_bytes + 16 <= kSmemTables;
+  const bool shells_in_smem = tables_in_smem && (ncol + Bs.nbf) * 4 + shell_bytes + 16 <= table_bytes;
   const int4* shp = Bs.sh_pack;
   const float2* shr = Bs.sh_rad2_df;
   const float4* prm = Bs.p_pack;
@@ -399,11 +402,12 @@ cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st)
     attr_set = true;
   }
   const unsigned grid = static_cast<unsigned>((a.npts + kBlockM - 1) / kBlockM);
-  tc_fused_kernel<<<grid, kThreads, kSmemBytes, st>>>(
+  const int tables = std::max(0, std::min(a.table_bytes, kSmemTables));
+  tc_fused_kernel<<<grid, kThreads, kSmemFixed + tables, st>>>(
       *static_cast<const CUtensorMap*>(a.tmap_a_hi), *static_cast<const CUtensorMap*>(a.tmap_a_lo),
       *static_cast<const CUtensorMap*>(a.tmap_b_hi), *static_cast<const CUtensorMap*>(a.tmap_b_lo), B,
       a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err, a.tiles, a.tile_stride, a.perm,
-      a.tile_order);
+      a.tile_order, tables);
   return cudaGetLastError();
 }
 

@@ -278,8 +278,8 @@ def sample_plane(gimic, region, n, rng, core_frac=0.5, floor=J_FLOOR):
 # proposal builds the same set): the cheapest rule of a grid search over
 # kappa, initial panels, tau, depth and orders with every training plane
 # within 0.01 nA/T of its 200 x 200 uniform judge (largest error 0.0075).
-DEFAULT_RULE = {"mode": "mass", "kappa_u": 2.0, "kappa_v": 2.0, "tau": 1.0, "q_hi": 7, "q_hi_v": None, "q_lo": 4,
-                "frac": 0.02, "max_depth": 1, "n0u": 3, "n0v": 3, "lattice": 96, "tau_s": 1e-3}
+DEFAULT_RULE = {"kappa_u": 2.0, "kappa_v": 2.0, "tau": 1.0, "q_hi": 7, "q_hi_v": None, "q_lo": 4, "frac": 0.02,
+                "max_depth": 1, "n0u": 3, "n0v": 3, "lattice": 96}
 
 
 class AxisMap:
@@ -385,57 +385,6 @@ def propose_panels(mass, region, rule=None):
     return mu, mv, panels
 
 
-def predict_at(net, gimic, region, xy):
-    """Predicted |j| (au) at in-plane points xy (N, 2)."""
-    dev = torch.device("cuda", torch.cuda.current_device())
-    f = features(gimic, torch.as_tensor(region.points(xy), device=dev), torch.as_tensor(region.uv(xy), device=dev))
-    return np.exp(net.predict(f).double().cpu().numpy())
-
-
-def _panel_rule(mu, mv, ta, tb, wa, wb, q):
-    x, wx = mu.nodes(ta, tb, q)
-    y, wy = mv.nodes(wa, wb, q)
-    X, Y = np.meshgrid(x, y, indexing="ij")
-    return np.stack([X.reshape(-1), Y.reshape(-1)], axis=1), np.outer(wx, wy).reshape(-1)
-
-
-def propose_panels_surrogate(net, gimic, region, mass, rule=None):
-    """Quadtree driven by the network as a surrogate integrand: a mapped
-    panel is split in four while its order-q rule and an order-2q rule
-    applied to the predicted |j| differ by more than ``tau_s`` (nA/T), up to
-    ``max_depth``.  Returns (map_u, map_v, panels) as propose_panels."""
-    r = dict(DEFAULT_RULE, **(rule or {}))
-    mu, mv = estimate_maps(mass, region, r)
-    q = int(r["q_hi"])
-    tu = np.linspace(mu.t0, mu.t1, int(r["n0u"]) + 1)
-    tv = np.linspace(mv.t0, mv.t1, int(r["n0v"]) + 1)
-    todo = [(tu[i], tu[i + 1], tv[j], tv[j + 1]) for i in range(len(tu) - 1) for j in range(len(tv) - 1)]
-    leaves = []
-    conv = api.au2si(1.0)
-    for depth in range(int(r["max_depth"]) + 1):
-        if not todo:
-            break
-        if depth == int(r["max_depth"]):
-            leaves += todo
-            break
-        rules = [(_panel_rule(mu, mv, *pn, q), _panel_rule(mu, mv, *pn, 2 * q)) for pn in todo]
-        xy = np.concatenate([a[0] for pair in rules for a in pair])
-        g = predict_at(net, gimic, region, xy) * conv
-        nxt, off = [], 0
-        for pn, (lo, hi) in zip(todo, rules):
-            n1, n2 = len(lo[1]), len(hi[1])
-            e = abs(np.dot(g[off:off + n1], lo[1]) - np.dot(g[off + n1:off + n1 + n2], hi[1]))
-            off += n1 + n2
-            if e > r["tau_s"]:
-                ta, tb, wa, wb = pn
-                tm, wm = 0.5 * (ta + tb), 0.5 * (wa + wb)
-                nxt += [(ta, tm, wa, wm), (tm, tb, wa, wm), (ta, tm, wm, wb), (tm, tb, wm, wb)]
-            else:
-                leaves.append(pn)
-        todo = nxt
-    return mu, mv, [(ta, tb, wa, wb, q, q) for ta, tb, wa, wb in leaves]
-
-
 def panel_planes(region, mu, mv, panels):
     """Each mapped panel as a plane for Gimic.plane_integrals."""
     out = []
@@ -479,10 +428,7 @@ def integrate_adaptive(gimic, net, region, rule=None, min_inside=0.99, fallback_
         r = dict(DEFAULT_RULE, **(rule or {}))
         mass, inside = predict_mass(net, gimic, region, r["lattice"])
         if inside >= min_inside:
-            if r["mode"] == "surrogate":
-                mu, mv, panels = propose_panels_surrogate(net, gimic, region, mass, r)
-            else:
-                mu, mv, panels = propose_panels(mass, region, r)
+            mu, mv, panels = propose_panels(mass, region, r)
             cur = integrate_panels(gimic, region, mu, mv, panels)
             return {"current": cur, "points": int(sum(p[4] * p[5] for p in panels)), "panels": panels,
                     "maps": (mu, mv), "method": "adaptive", "inside": inside}
