@@ -517,7 +517,7 @@ struct gg_ctx {
                                        std::to_string(basis.nbf) + "); use the FP64 precision");
     int rc = prep_split(slot[0], d_pts, n, st);
     if (rc) return rc;
-    rc = tc_split(slot[0], out, st, gg::tc_table_budget());
+    rc = tc_split(slot[0], out, st);
     if (rc == GG_OK) slot[0].used = false;  // ordered on `st` itself
     return rc;
   }
@@ -587,16 +587,14 @@ struct gg_ctx {
     return GG_OK;
   }
 
-  // The contraction of a prepared slot; table_bytes of shared memory for the
-  // epilogue's tables (0: they stay in global memory).
-  int tc_split(SplitSlot& sl, gg::Outputs out, cudaStream_t st, int table_bytes) {
+  // The contraction of a prepared slot.
+  int tc_split(SplitSlot& sl, gg::Outputs out, cudaStream_t st) {
     gg::TcArgs ta{&sl.tma_hi, &sl.tma_lo, &tm_b_hi, &tm_b_lo, sl.inv_row.as<float>(), inv_col.as<float>(),
                   sl.tp,       sl.n,       flags,    out,      d_err};
     ta.tiles = sl.tiles;
     ta.tile_stride = sl.stride;
     ta.perm = sl.perm;
     ta.tile_order = sl.tord;
-    ta.table_bytes = table_bytes;
     if (prof.on) {
       const unsigned long long blocks = static_cast<unsigned long long>((sl.n + gg::kBlockM - 1) / gg::kBlockM) *
                                         dB.nchunk * (dB.kpad / gg::kBlockK);
@@ -615,9 +613,7 @@ struct gg_ctx {
   // Batch b of a multi-batch call.  On the split path the preparation of the
   // batch runs on the auxiliary stream (after `input_ready`, when given, and
   // after the previous contraction of the same slot) and the contraction on
-  // `st`, so batch b+1 is prepared while batch b is contracted.  Those
-  // contractions leave the epilogue's tables in global memory: the smaller
-  // shared-memory request lets a basis CTA share each SM with them.
+  // `st`, so batch b+1 is prepared while batch b is contracted.
   int pipe_batch(int b, const double* d_pts, int64_t n, gg::Outputs out, cudaStream_t st,
                  cudaEvent_t input_ready = nullptr) {
     cudaError_t e = cudaSuccess;
@@ -647,7 +643,7 @@ struct gg_ctx {
     e = cudaEventRecord(sl.prepared, aux_stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st, sl.prepared, 0);
     if (e != cudaSuccess) return cuda_fail(e, "batch pipeline");
-    rc = tc_split(sl, out, st, 0);
+    rc = tc_split(sl, out, st);
     if (rc) return rc;
     sl.used = true;
     e = cudaEventRecord(sl.consumed, st);
@@ -1021,26 +1017,25 @@ int gg_plane_integrals(gg_ctx* ctx, const gg_grid* grids, int nplanes, double* o
     nw += gr.npts[0] + gr.npts[1] + gr.npts[2];
   }
   // points r(i,j,k) = origin + x1_i basv1 + x2_j basv2 + x3_k basv3, i fastest
-  // (gridpoint, src/fgimic/grid.f90:498-511); centre as grid_center (:529-541)
-  std::vector<double> hp(static_cast<size_t>(npts) * 3), hw(static_cast<size_t>(nw));
+  // (gridpoint, src/fgimic/grid.f90:498-511), generated on the device from
+  // the axis coordinates; centre as grid_center (:529-541)
+  std::vector<double> hw(static_cast<size_t>(nw)), hx(static_cast<size_t>(nw));
   std::vector<gg::PlaneDesc> desc(nplanes);
   std::vector<int> row_plane(static_cast<size_t>(nrows));
   int64_t po = 0, ro = 0, wo = 0;
   for (int q = 0; q < nplanes; ++q) {
     const gg_grid& gr = grids[q];
     const int p1 = gr.npts[0], p2 = gr.npts[1], p3 = gr.npts[2];
-    for (int k = 0; k < p3; ++k)
-      for (int j = 0; j < p2; ++j)
-        for (int i = 0; i < p1; ++i) {
-          const int64_t idx = po + i + static_cast<int64_t>(p1) * (j + static_cast<int64_t>(p2) * k);
-          for (int c = 0; c < 3; ++c)
-            hp[3 * idx + c] = gr.origin[c] + gr.pts[0][i] * gr.basv[c] + gr.pts[1][j] * gr.basv[3 + c] +
-                              gr.pts[2][k] * gr.basv[6 + c];
-        }
     std::copy(gr.wgt[0], gr.wgt[0] + p1, hw.begin() + wo);
     std::copy(gr.wgt[1], gr.wgt[1] + p2, hw.begin() + wo + p1);
     std::copy(gr.wgt[2], gr.wgt[2] + p3, hw.begin() + wo + p1 + p2);
+    std::copy(gr.pts[0], gr.pts[0] + p1, hx.begin() + wo);
+    std::copy(gr.pts[1], gr.pts[1] + p2, hx.begin() + wo + p1);
+    std::copy(gr.pts[2], gr.pts[2] + p3, hx.begin() + wo + p1 + p2);
     gg::PlaneDesc& d = desc[q];
+    d.x_off = static_cast<int>(wo);
+    for (int c = 0; c < 3; ++c) d.origin[c] = gr.origin[c];
+    for (int c = 0; c < 9; ++c) d.basv[c] = gr.basv[c];
     d.pt_off = po;
     d.row_off = ro;
     d.p1 = p1;
@@ -1064,25 +1059,29 @@ int gg_plane_integrals(gg_ctx* ctx, const gg_grid* grids, int nplanes, double* o
   int rc = ctx->prepare();
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const size_t aux = hw.size() * sizeof(double) + desc.size() * sizeof(gg::PlaneDesc) + row_plane.size() * sizeof(int) +
-                     static_cast<size_t>(nrows) * 7 * sizeof(double) + static_cast<size_t>(nplanes) * 7 * sizeof(double) + 64;
-  cudaError_t e = ctx->pts.reserve(hp.size() * sizeof(double));
+  const size_t aux = 2 * hw.size() * sizeof(double) + desc.size() * sizeof(gg::PlaneDesc) +
+                     row_plane.size() * sizeof(int) + static_cast<size_t>(nrows) * 7 * sizeof(double) +
+                     static_cast<size_t>(nplanes) * 7 * sizeof(double) + 64;
+  cudaError_t e = ctx->pts.reserve(static_cast<size_t>(npts) * 3 * sizeof(double));
   if (e == cudaSuccess) e = ctx->jt.reserve(static_cast<size_t>(npts) * 9 * sizeof(double));
   if (e == cudaSuccess) e = ctx->plane_rows.reserve(aux);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "plane scratch");
   char* ab = ctx->plane_rows.as<char>();
   double* dw = reinterpret_cast<double*>(ab);
-  double* drow = dw + hw.size();
+  double* dx = dw + hw.size();
+  double* drow = dx + hx.size();
   double* dout = drow + static_cast<size_t>(nrows) * 7;
   gg::PlaneDesc* ddesc = reinterpret_cast<gg::PlaneDesc*>(dout + static_cast<size_t>(nplanes) * 7);
   int* drp = reinterpret_cast<int*>(ddesc + nplanes);
-  e = cudaMemcpyAsync(ctx->pts.p, hp.data(), hp.size() * sizeof(double), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dw, hw.data(), hw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+  e = cudaMemcpyAsync(dw, hw.data(), hw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, hx.data(), hx.size() * sizeof(double), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(ddesc, desc.data(), desc.size() * sizeof(gg::PlaneDesc), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(drp, row_plane.data(), row_plane.size() * sizeof(int), cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane points");
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane axes");
+  gg::launch_plane_points(dx, ddesc, drp, nrows, ctx->pts.as<double>(), st);
+  ctx->launches += 1;
   const int64_t batch = ctx->precision == GG_PREC_FP64 ? std::min<int64_t>(ctx->max_batch, 16384) : ctx->max_batch;
   for (int64_t off = 0, b = 0; off < npts; off += batch, ++b) {
     const int64_t m = std::min(batch, npts - off);
@@ -1387,7 +1386,6 @@ extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t 
   if (e != cudaSuccess) return ctx->cuda_fail(e, "basis kernel launch");
   gg::TcArgs ta{&tma_hi, &tma_lo, &ctx->tm_b_hi, &ctx->tm_b_lo, inv_row, ctx->inv_col.as<float>(),
                 pts,     n,       ctx->flags,     gg::Outputs{jt, rho, divt}, ctx->d_err};
-  ta.table_bytes = gg::tc_table_budget();
   e = gg::launch_tc_fused(ctx->dB, ta, st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "tensor-core kernel launch");
   ctx->launches += 2;

@@ -53,11 +53,8 @@ struct TcArgs {
   int tile_stride = 0;
   const int* perm = nullptr;   // output index of each (sorted) point (null: identity)
   const int* tile_order = nullptr;  // tile processed by each CTA (null: CTA i -> tile i)
-  int table_bytes = 0;              // shared memory for the epilogue's tables (0: global memory)
 };
 int tc_smem_bytes();
-// Shared memory left for the epilogue's tables next to the pipeline stages.
-int tc_table_budget();
 
 // Spatial ordering and tile screening (k_tiles.cu)
 int tile_stride(const DevBasis& B);
@@ -84,7 +81,15 @@ struct PlaneDesc {
   double center[3];
   double normal[3];
   double radius;
+  double origin[3];
+  double basv[9];  // basv[3 d + c]: component c of axis d
+  int x_off;       // axis coordinates xs[x_off ..] (p1 values, then p2, then p3)
 };
+// Points of every plane, r(i,j,k) = origin + x1_i basv1 + x2_j basv2 +
+// x3_k basv3 in the host's operation order (no fused multiply-adds), one
+// block per plane row.
+void launch_plane_points(const double* xs, const PlaneDesc* planes, const int* row_plane, int64_t nrows, double* pts,
+                         cudaStream_t st);
 void launch_plane_batch(const double* jt, const double* pts, const double* w, const PlaneDesc* planes, int nplanes,
                         const int* row_plane, int64_t nrows, const double bb[3], double* row_out, double* out,
                         cudaStream_t st);

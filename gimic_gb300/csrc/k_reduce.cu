@@ -88,6 +88,31 @@ __global__ void plane_batch_sum_kernel(const double* __restrict__ w, const Plane
   out[t] = s3;
 }
 
+__global__ void __launch_bounds__(kRowThreads) plane_points_kernel(const double* __restrict__ xs,
+                                                                   const PlaneDesc* __restrict__ planes,
+                                                                   const int* __restrict__ row_plane,
+                                                                   double* __restrict__ pts) {
+  const int64_t row = blockIdx.x;
+  const PlaneDesc& pl = planes[row_plane[row]];
+  const int64_t r = row - pl.row_off;
+  const int j = static_cast<int>(r % pl.p2), k = static_cast<int>(r / pl.p2);
+  const double x2 = xs[pl.x_off + pl.p1 + j], x3 = xs[pl.x_off + pl.p1 + pl.p2 + k];
+  for (int i = threadIdx.x; i < pl.p1; i += kRowThreads) {
+    const double x1 = xs[pl.x_off + i];
+    const int64_t idx = pl.pt_off + i + static_cast<int64_t>(pl.p1) * (j + static_cast<int64_t>(pl.p2) * k);
+    for (int c = 0; c < 3; ++c)
+      pts[3 * idx + c] = __dadd_rn(__dadd_rn(__dadd_rn(pl.origin[c], __dmul_rn(x1, pl.basv[c])),
+                                             __dmul_rn(x2, pl.basv[3 + c])),
+                                   __dmul_rn(x3, pl.basv[6 + c]));
+  }
+}
+
+void launch_plane_points(const double* xs, const PlaneDesc* planes, const int* row_plane, int64_t nrows, double* pts,
+                         cudaStream_t st) {
+  if (nrows <= 0) return;
+  plane_points_kernel<<<static_cast<unsigned>(nrows), kRowThreads, 0, st>>>(xs, planes, row_plane, pts);
+}
+
 void launch_plane_batch(const double* jt, const double* pts, const double* w, const PlaneDesc* planes, int nplanes,
                         const int* row_plane, int64_t nrows, const double bb[3], double* row_out, double* out,
                         cudaStream_t st) {

@@ -36,14 +36,7 @@ constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kTmemCols = 512;
 constexpr int kAccStride = 256;
 constexpr int kMaxTileList = 512;  // ints: 2 + column chunks + K blocks of a tile (nbf <= 10,000)
-constexpr int kSmemFixed = kStages * kStageBytes + 1024 + 256 + kMaxTileList * 4;
-// The column scales and packed function records are copied to shared memory
-// when they fit next to the pipeline stages (nchunk * 224 + nbf <= 12,224
-// words, i.e. nbf up to about 1500), the shell, primitive and atom tables as
-// well when those fit too; otherwise the epilogue reads them from global
-// memory.
-constexpr int kSmemTables = 227 * 1024 - kSmemFixed;
-constexpr int kSmemBytes = kSmemFixed + kSmemTables;  // upper bound of the dynamic request
+constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256 + kMaxTileList * 4;
 static_assert(kBlockM * kNDots * 8 <= kStageBytes, "epilogue reduction buffer must fit in one stage");
 
 __device__ __forceinline__ void tmem_ld1(uint32_t taddr, float& v) {
@@ -74,7 +67,6 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 }  // namespace
 
 int tc_smem_bytes() { return kSmemBytes; }
-int tc_table_budget() { return kSmemTables; }
 
 // Per chunk the MMAs run in two passes over K into the same accumulator:
 // first the two small cross products (hi*lo, lo*hi), then the main product
@@ -88,7 +80,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     DevBasis Bs, const float* __restrict__ inv_row, const float* __restrict__ inv_col,
                     const double* __restrict__ pts, int64_t npts, Flags fl, Outputs out, int* err,
                     const int* __restrict__ tiles, int tstride, const int* __restrict__ perm,
-                    const int* __restrict__ tile_order, int table_bytes) {
+                    const int* __restrict__ tile_order) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                          ~static_cast<uintptr_t>(1023));
@@ -98,7 +90,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* accempty = accfull + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accempty + 2);
   int* tlist = reinterpret_cast<int*>(tmem_slot + 4);  // {#chunks, #kblocks, chunk ids, kblock ids}
-  float* s_icol = reinterpret_cast<float*>(tlist + kMaxTileList);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t tile = tile_order ? static_cast<int64_t>(tile_order[blockIdx.x]) : static_cast<int64_t>(blockIdx.x);
@@ -118,43 +109,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   const int* clist = tlist + 2;
   const int* klist = tlist + 2 + nchunk_all;
-  // column scales and per-function records (shell << 12 | packed ijk)
-  const int ncol = nchunk_all * kBlockN;
-  const bool tables_in_smem = (ncol + Bs.nbf) * 4 <= table_bytes;
+  // epilogue tables: column scales, per-function records (shell << 12 |
+  // Cartesian case), shell records, primitives, atoms
   const float* icol = inv_col;
   const int* fpack = Bs.f_pack;
-  // shell records, screening radii, primitives and atoms too when they fit
-  const int shell_bytes = Bs.nshells * (16 + 8) + Bs.nprim * 16 + Bs.natoms * 24;
-  const bool shells_in_smem = tables_in_smem && (ncol + Bs.nbf) * 4 + shell_bytes + 16 <= table_bytes;
   const int4* shp = Bs.sh_pack;
   const float2* shr = Bs.sh_rad2_df;
   const float4* prm = Bs.p_pack;
   const float2* atm = Bs.atom_df;
-  if (tables_in_smem) {
-    int* s_fpack = reinterpret_cast<int*>(s_icol + ncol);
-    for (int i = threadIdx.x; i < ncol; i += blockDim.x) s_icol[i] = inv_col[i];
-    for (int i = threadIdx.x; i < Bs.nbf; i += blockDim.x) s_fpack[i] = Bs.f_pack[i];
-    icol = s_icol;
-    fpack = s_fpack;
-    if (shells_in_smem) {
-      unsigned char* q = reinterpret_cast<unsigned char*>(
-          (reinterpret_cast<uintptr_t>(s_fpack + Bs.nbf) + 15) & ~static_cast<uintptr_t>(15));
-      int4* s_shp = reinterpret_cast<int4*>(q);
-      float4* s_prm = reinterpret_cast<float4*>(s_shp + Bs.nshells);
-      float2* s_shr = reinterpret_cast<float2*>(s_prm + Bs.nprim);
-      float2* s_atm = s_shr + Bs.nshells;
-      for (int i = threadIdx.x; i < Bs.nshells; i += blockDim.x) {
-        s_shp[i] = Bs.sh_pack[i];
-        s_shr[i] = Bs.sh_rad2_df[i];
-      }
-      for (int i = threadIdx.x; i < Bs.nprim; i += blockDim.x) s_prm[i] = Bs.p_pack[i];
-      for (int i = threadIdx.x; i < 3 * Bs.natoms; i += blockDim.x) s_atm[i] = Bs.atom_df[i];
-      shp = s_shp;
-      shr = s_shr;
-      prm = s_prm;
-      atm = s_atm;
-    }
-  }
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
@@ -402,12 +364,11 @@ cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st)
     attr_set = true;
   }
   const unsigned grid = static_cast<unsigned>((a.npts + kBlockM - 1) / kBlockM);
-  const int tables = std::max(0, std::min(a.table_bytes, kSmemTables));
-  tc_fused_kernel<<<grid, kThreads, kSmemFixed + tables, st>>>(
+  tc_fused_kernel<<<grid, kThreads, kSmemBytes, st>>>(
       *static_cast<const CUtensorMap*>(a.tmap_a_hi), *static_cast<const CUtensorMap*>(a.tmap_a_lo),
       *static_cast<const CUtensorMap*>(a.tmap_b_hi), *static_cast<const CUtensorMap*>(a.tmap_b_lo), B,
       a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err, a.tiles, a.tile_stride, a.perm,
-      a.tile_order, tables);
+      a.tile_order);
   return cudaGetLastError();
 }
 
