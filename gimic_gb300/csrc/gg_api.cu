@@ -129,6 +129,7 @@ struct gg_ctx {
 
   // scratch
   DevBuf pts, jt, rho, divt, jv;
+  DevBuf tile_ctr;  // tile queue counter of the contraction kernel
   // Per-batch scratch of the split path.  Two slots let the ordering,
   // screening and basis evaluation of batch b+1 (on the auxiliary stream) run
   // while the contraction of batch b runs on the caller's stream.
@@ -223,7 +224,7 @@ struct gg_ctx {
     table_allocs.clear();
     tables_ready = false;
     for (DevBuf* b : {&b_fp64, &b_hi, &b_lo, &inv_col, &pts, &jt, &rho, &divt, &jv, &phi, &gx, &gy, &gz, &lap, &w64,
-                      &plane_rows, &plane_out, &pts2, &jt2, &rho2, &divt2})
+                      &plane_rows, &plane_out, &pts2, &jt2, &rho2, &divt2, &tile_ctr})
       b->release();
     for (SplitSlot& sl : slot) {
       for (DevBuf* b : {&sl.a_hi, &sl.a_lo, &sl.inv_row, &sl.sort_keys, &sl.sort_keys2, &sl.sort_idx, &sl.sort_perm,
@@ -601,9 +602,13 @@ struct gg_ctx {
       prof.dense_blocks += blocks;
       if (!sl.tiles && prof.d_blocks) prof_add_blocks(blocks, st);
     }
+    cudaError_t e = tile_ctr.reserve(sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(tile_ctr.p, 0, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(e, "tile queue");
+    ta.tile_counter = tile_ctr.as<int>();
     size_t ps = 0;
     prof_begin(GG_PROF_TC, st, &ps);
-    cudaError_t e = gg::launch_tc_fused(dB, ta, st);
+    e = gg::launch_tc_fused(dB, ta, st);
     prof_end(st, ps);
     if (e != cudaSuccess) return cuda_fail(e, "tensor-core kernel launch");
     launches += 1;
@@ -1311,13 +1316,15 @@ int gg_mlp_infer(const float* params, const float* x, int64_t n, float* y, void*
 // scratch (the fp16 hi/lo point operand and the per-point scale factors)
 // placed in the fixed array below instead of in buffers that grow on demand.
 // The array occupies kNoAllocScratchBytes on every GPU where the library's
-// device code is loaded, until the process exits.
+// device code is loaded, until the process exits; a 4-byte static counter
+// next to it holds the contraction kernel's tile queue.
 // ---------------------------------------------------------------------------
 namespace {
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;  // 32 MiB
 constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+static __device__ int g_noalloc_tile_counter;  // the contraction kernel's tile queue
 
 std::mutex g_noalloc_mu;
 void* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
@@ -1334,6 +1341,21 @@ cudaError_t noalloc_scratch(int device, void** out) {
     g_noalloc_addr[device] = p;
   }
   *out = g_noalloc_addr[device];
+  return cudaSuccess;
+}
+
+void* g_noalloc_ctr_addr[kNoAllocMaxDevices] = {nullptr};
+
+cudaError_t noalloc_counter(int device, int** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (!g_noalloc_ctr_addr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_tile_counter);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ctr_addr[device] = p;
+  }
+  *out = static_cast<int*>(g_noalloc_ctr_addr[device]);
   return cudaSuccess;
 }
 
@@ -1377,6 +1399,9 @@ extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t 
   __half* a_lo = reinterpret_cast<__half*>(c);
   c += align256(static_cast<size_t>(n) * kpad * sizeof(__half));
   float* inv_row = reinterpret_cast<float*>(c);
+  int* tile_counter = nullptr;
+  e = noalloc_counter(ctx->device, &tile_counter);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaGetSymbolAddress(no-allocation tile counter)");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   CUtensorMap tma_hi, tma_lo;
   if (!encode_fp16_2d(&tma_hi, a_hi, n, ctx->dB.kpad, gg::kBlockM) ||
@@ -1386,7 +1411,9 @@ extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t 
   if (e != cudaSuccess) return ctx->cuda_fail(e, "basis kernel launch");
   gg::TcArgs ta{&tma_hi, &tma_lo, &ctx->tm_b_hi, &ctx->tm_b_lo, inv_row, ctx->inv_col.as<float>(),
                 pts,     n,       ctx->flags,     gg::Outputs{jt, rho, divt}, ctx->d_err};
-  e = gg::launch_tc_fused(ctx->dB, ta, st);
+  ta.tile_counter = tile_counter;
+  e = cudaMemsetAsync(tile_counter, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = gg::launch_tc_fused(ctx->dB, ta, st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "tensor-core kernel launch");
   ctx->launches += 2;
   return ctx->check_device_error(st);

@@ -52,7 +52,8 @@ struct TcArgs {
   const int* tiles = nullptr;  // per-tile active chunk / K-block lists (null: all)
   int tile_stride = 0;
   const int* perm = nullptr;   // output index of each (sorted) point (null: identity)
-  const int* tile_order = nullptr;  // tile processed by each CTA (null: CTA i -> tile i)
+  const int* tile_order = nullptr;  // tile of each queue step (null: step i -> tile i)
+  int* tile_counter = nullptr;      // device int, zero at launch: the tile queue
 };
 int tc_smem_bytes();
 

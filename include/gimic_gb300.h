@@ -201,8 +201,9 @@ int gg_mlp_infer(const float *params, const float *x, int64_t n, float *y, void 
  * applications that budget all device memory themselves, and time-critical
  * loops where an allocation would stall the device.  Same results as
  * gg_jtensor_batch on the split-FP16 path, but the per-point scratch lives in
- * a fixed 32 MiB static device array (held on every GPU where the library's
- * device code is loaded, until the process exits), so n is limited to
+ * a fixed 32 MiB static device array (plus a 4-byte static counter, held on
+ * every GPU where the library's device code is loaded, until the process
+ * exits), so n is limited to
  * floor((32 MiB - 768) / (4 * kpad + 4)) points, kpad = nbf rounded up to 64
  * (10,908 points for nbf 720); larger n is rejected with GG_EINVAL and a
  * message.  All buffers must be device memory, and the context must already
