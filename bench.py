@@ -38,6 +38,9 @@ CUBE_N = 128
 CUBE_HALF = 16.0
 
 
+METRIC = "jtensor points/s (+ plane-integrals/s) at <=1e-6 rel err vs FP64"
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -168,7 +171,7 @@ def run_reference(args, rank, world):
     dt = time.perf_counter() - t
     v = sample * args.steps / dt
     n = mol.nbf
-    line = {"impl": "reference", "metric": "jtensor points/s (+ plane-integrals/s)", "value": v,
+    line = {"impl": "reference", "metric": METRIC, "value": v,
             "unit": "points/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded MOL/XDENS in the reference's formats)",
@@ -600,7 +603,7 @@ def main():
         return
     cpu = cpu_baseline(mp, xp, args.cpu_sample)
     line = {
-        "metric": "jtensor points/s (+ plane-integrals/s) at <=1e-6 rel err vs FP64",
+        "metric": METRIC,
         "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16x3/f32/f64",
         "data": "synthetic (seeded MOL/XDENS in the reference's formats)",
