@@ -106,6 +106,8 @@ struct gg_ctx {
   std::string molfile, xdensfile;
   gg::Basis basis;
   gg::Density dens;
+  std::vector<int> shell_src;  // position in the current shell order -> shell index in the file
+  int shell_order = 1;         // 0: file order, 1: locality order
   bool uhf = false;
   double screening = 1e-8;
   int spin = 0;
@@ -469,6 +471,31 @@ struct gg_ctx {
     mats_spin = spin;
     mats_prec = precision;
     return GG_OK;
+  }
+
+  // Puts the shells (functions, density blocks) into the file order or the
+  // locality order of gg::locality_shell_order; device tables and matrices
+  // are rebuilt on the next evaluation.
+  void set_shell_order(int mode) {
+    const int ns = static_cast<int>(basis.shells.size());
+    if (static_cast<int>(shell_src.size()) != ns) {
+      shell_src.resize(ns);
+      for (int k = 0; k < ns; ++k) shell_src[k] = k;
+    }
+    std::vector<int> back(ns);  // back to the file order
+    for (int k = 0; k < ns; ++k) back[shell_src[k]] = k;
+    bool ident = true;
+    for (int k = 0; k < ns; ++k) ident = ident && shell_src[k] == k;
+    if (!ident) gg::permute_shells(&basis, &dens, back);
+    for (int k = 0; k < ns; ++k) shell_src[k] = k;
+    if (mode == 1) {
+      const std::vector<int> ord = gg::locality_shell_order(basis);
+      gg::permute_shells(&basis, &dens, ord);
+      shell_src = ord;
+    }
+    shell_order = mode;
+    tables_ready = false;
+    mats_spin = -1;
   }
 
   int prepare() {
@@ -837,6 +864,7 @@ int gg_ctx_create(const char* molfile, const char* xdens, int uhf, double screen
     delete c;
     return GG_EIO;
   }
+  c->set_shell_order(1);
   cudaGetDevice(&c->device);
   cudaGetLastError();
   *out = c;
@@ -880,6 +908,22 @@ int gg_set_screening(gg_ctx* ctx, double thrs) {
   ctx->screening = thrs;
   gg::set_screening(&ctx->basis, thrs);
   ctx->tables_ready = false;
+  return GG_OK;
+}
+
+int gg_set_shell_order(gg_ctx* ctx, int mode) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (mode != 0 && mode != 1) return ctx->fail(GG_EINVAL, "shell order mode must be 0 (file) or 1 (locality)");
+  if (mode != ctx->shell_order) ctx->set_shell_order(mode);
+  return GG_OK;
+}
+
+int gg_get_shell_order(const gg_ctx* ctx, int* mode, int* order) {
+  if (!ctx || !mode) return GG_EINVAL;
+  *mode = ctx->shell_order;
+  if (order)
+    for (size_t k = 0; k < ctx->shell_src.size(); ++k) order[k] = ctx->shell_src[k];
   return GG_OK;
 }
 

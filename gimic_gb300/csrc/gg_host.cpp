@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <fstream>
 #include <sstream>
@@ -376,6 +377,178 @@ int gauss_data(double a, double b, int order, int npts, int quadrature, double* 
       wgt[blk * order + i] = w[i] * half;
     }
   return 0;
+}
+
+namespace {
+
+// Visiting order of the atoms: start at the atom farthest from the centroid,
+// then always step to the nearest atom not yet visited.
+std::vector<int> atom_tour(const Basis& b) {
+  const int na = static_cast<int>(b.atoms.size());
+  double c[3] = {0, 0, 0};
+  for (const Atom& a : b.atoms)
+    for (int d = 0; d < 3; ++d) c[d] += a.coord[d] / na;
+  auto dist2 = [&](const double* x, const double* y) {
+    double s = 0;
+    for (int d = 0; d < 3; ++d) s += (x[d] - y[d]) * (x[d] - y[d]);
+    return s;
+  };
+  int cur = 0;
+  for (int a = 1; a < na; ++a)
+    if (dist2(b.atoms[a].coord, c) > dist2(b.atoms[cur].coord, c)) cur = a;
+  std::vector<char> seen(na, 0);
+  std::vector<int> tour;
+  for (int step = 0; step < na; ++step) {
+    tour.push_back(cur);
+    seen[cur] = 1;
+    int next = -1;
+    double best = 0;
+    for (int a = 0; a < na; ++a) {
+      if (seen[a]) continue;
+      const double d2 = dist2(b.atoms[a].coord, b.atoms[cur].coord);
+      if (next < 0 || d2 < best) {
+        next = a;
+        best = d2;
+      }
+    }
+    cur = next;
+  }
+  return tour;
+}
+
+// Active (K block, chunk) pairs of a shell order summed over the bricks;
+// dist[i * natoms + a] = distance from brick i's centre to atom a.
+double order_cost(const Basis& b, const std::vector<int>& order, const std::vector<double>& dist, int nbricks,
+                  double brick_radius) {
+  const int na = static_cast<int>(b.atoms.size());
+  const int nkb = (b.nbf + 63) / 64, nch = (b.nbf + 31) / 32;
+  std::vector<int> f0(order.size());
+  int f = 0;
+  for (size_t k = 0; k < order.size(); ++k) {
+    f0[k] = f;
+    f += b.shells[order[k]].ncomp;
+  }
+  std::vector<char> kb(nkb), ch(nch);
+  double cost = 0;
+  for (int i = 0; i < nbricks; ++i) {
+    std::fill(kb.begin(), kb.end(), 0);
+    std::fill(ch.begin(), ch.end(), 0);
+    for (size_t k = 0; k < order.size(); ++k) {
+      const Shell& s = b.shells[order[k]];
+      if (dist[static_cast<size_t>(i) * na + s.atom] - brick_radius > s.radius) continue;
+      const int a = f0[k], e = f0[k] + s.ncomp - 1;
+      for (int q = a / 64; q <= e / 64; ++q) kb[q] = 1;
+      for (int q = a / 32; q <= e / 32; ++q) ch[q] = 1;
+    }
+    double nk = 0, nc = 0;
+    for (char v : kb) nk += v;
+    for (char v : ch) nc += v;
+    cost += nk * nc;
+  }
+  return cost;
+}
+
+}  // namespace
+
+std::vector<int> locality_shell_order(const Basis& b) {
+  const int ns = static_cast<int>(b.shells.size()), na = static_cast<int>(b.atoms.size());
+  std::vector<int> ident(ns);
+  for (int k = 0; k < ns; ++k) ident[k] = k;
+  if (ns < 2 || na < 1) return ident;
+  // bricks of 2 x 1 x 1 Bohr over the atoms' bounding box + 4 Bohr, thinned
+  // to at most 8192 by a stride
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = hi[d] = b.atoms[0].coord[d];
+    for (const Atom& a : b.atoms) {
+      lo[d] = std::min(lo[d], a.coord[d]);
+      hi[d] = std::max(hi[d], a.coord[d]);
+    }
+    lo[d] -= 4.0;
+    hi[d] += 4.0;
+  }
+  const double edge[3] = {2.0, 1.0, 1.0};
+  int nb[3];
+  for (int d = 0; d < 3; ++d) nb[d] = std::max(1, static_cast<int>(std::ceil((hi[d] - lo[d]) / edge[d])));
+  const int64_t total = static_cast<int64_t>(nb[0]) * nb[1] * nb[2];
+  const int64_t stride = std::max<int64_t>(1, (total + 8191) / 8192);
+  std::vector<double> dist;
+  int nbricks = 0;
+  for (int64_t i = 0; i < total; i += stride, ++nbricks) {
+    const int64_t ix = i / (static_cast<int64_t>(nb[1]) * nb[2]), iy = (i / nb[2]) % nb[1], iz = i % nb[2];
+    const double c[3] = {lo[0] + (ix + 0.5) * edge[0], lo[1] + (iy + 0.5) * edge[1], lo[2] + (iz + 0.5) * edge[2]};
+    for (const Atom& a : b.atoms) {
+      double s = 0;
+      for (int d = 0; d < 3; ++d) s += (c[d] - a.coord[d]) * (c[d] - a.coord[d]);
+      dist.push_back(std::sqrt(s));
+    }
+  }
+  const double brick_radius = 0.5 * std::sqrt(edge[0] * edge[0] + edge[1] * edge[1] + edge[2] * edge[2]);
+  const std::vector<int> tour = atom_tour(b);
+  std::vector<int> tpos(na);
+  for (int k = 0; k < na; ++k) tpos[tour[k]] = k;
+  std::vector<double> radii;
+  for (const Shell& s : b.shells) radii.push_back(s.radius);
+  std::sort(radii.begin(), radii.end());
+  std::vector<int> best = ident;
+  double best_cost = order_cost(b, ident, dist, nbricks, brick_radius);
+  for (int nclass = 1; nclass <= 4; ++nclass) {
+    // class boundaries at the radius quantiles; class 0 holds the widest shells
+    std::vector<double> edges;
+    for (int q = 1; q < nclass; ++q) edges.push_back(radii[static_cast<size_t>(q) * ns / nclass]);
+    std::vector<int> cls(ns);
+    for (int k = 0; k < ns; ++k) {
+      const double r = b.shells[k].radius;
+      cls[k] = nclass - 1 - static_cast<int>(std::upper_bound(edges.begin(), edges.end(), r) - edges.begin());
+    }
+    std::vector<int> ord = ident;
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+      if (cls[x] != cls[y]) return cls[x] < cls[y];
+      return tpos[b.shells[x].atom] < tpos[b.shells[y].atom];
+    });
+    const double c = order_cost(b, ord, dist, nbricks, brick_radius);
+    if (c < best_cost) {
+      best_cost = c;
+      best = ord;
+    }
+  }
+  return best;
+}
+
+void permute_shells(Basis* b, Density* d, const std::vector<int>& order) {
+  const int n = b->nbf;
+  std::vector<int> src(n);  // new function -> current function
+  std::vector<Shell> shells;
+  shells.reserve(order.size());
+  int f = 0;
+  for (int k : order) {
+    Shell s = b->shells[k];
+    for (int c = 0; c < s.ncomp; ++c) src[f + c] = s.first + c;
+    s.first = f;
+    f += s.ncomp;
+    shells.push_back(std::move(s));
+  }
+  b->shells = std::move(shells);
+  b->func_atom.clear();
+  b->func_shell.clear();
+  b->func_comp.clear();
+  for (size_t i = 0; i < b->shells.size(); ++i)
+    for (int c = 0; c < b->shells[i].ncomp; ++c) {
+      b->func_atom.push_back(b->shells[i].atom);
+      b->func_shell.push_back(static_cast<int>(i));
+      b->func_comp.push_back(c);
+    }
+  const size_t nn = static_cast<size_t>(n) * n;
+  for (std::vector<double>* m : {&d->a, &d->b}) {
+    if (m->empty()) continue;
+    std::vector<double> out(m->size());
+    const size_t nblk = m->size() / nn;
+    for (size_t blk = 0; blk < nblk; ++blk)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i)
+          out[blk * nn + i + static_cast<size_t>(j) * n] = (*m)[blk * nn + src[i] + static_cast<size_t>(src[j]) * n];
+    m->swap(out);
+  }
 }
 
 double au2si(double au) {

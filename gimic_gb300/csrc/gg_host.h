@@ -66,6 +66,24 @@ struct Density {
 // (reorder.f90:54-96, dens.f90:210-234).
 std::string read_xdens(const std::string& path, const Basis& basis, bool uhf, Density* out);
 
+// Shell order for the screened split path.  Tile screening skips the
+// 64-function K blocks and 32-function column chunks in which no shell
+// reaches a tile, so the work falls when the shells that are in range of the
+// same region of space sit next to each other.  Candidates: the file order,
+// and shells grouped into 1..4 screening-radius classes (widest first) with
+// the atoms of each class along a nearest-neighbour tour.  Each candidate is
+// scored by the number of (K block, chunk) pairs active over 2 x 1 x 1 Bohr
+// bricks covering the atoms' bounding box plus 4 Bohr; the file order wins
+// ties.  Returns order[k] = index of the shell placed at position k.
+std::vector<int> locality_shell_order(const Basis& b);
+
+// Moves the shells to the given order (order[k] = current index of the shell
+// placed at k): renumbers the basis functions and permutes the rows and
+// columns of every density block to match.  The current and magnetically
+// induced densities are sums over function pairs, so nothing computed from
+// them changes beyond rounding.
+void permute_shells(Basis* b, Density* d, const std::vector<int>& order);
+
 // Composite Gauss / Gauss-Lobatto nodes (src/libgimic/gaussint.f90:267-319):
 // npts points made of npts/order panels on [0, b - a].  quadrature: 0 gauss,
 // 1 lobatto.  Returns 0, or -1 (npts not divisible / Newton failed).

@@ -101,7 +101,11 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
     int cur_atom = -1;
     float d2 = 0.f, hl2d = 0.f;
     for (int sh = 0; sh < B.nshells; ++sh) {
-      const int a = __ldg(&B.sh_pack[sh].x);
+      const int4 pk = __ldg(B.sh_pack + sh);  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
+      // shells of inactive K blocks are never stored, so they do not enter the bound
+      const int k_first = pk.y >> 6, k_last = (pk.y + (pk.z & 0xff) - 1) >> 6;
+      if (!((kb_on >> k_first) & 1ull) && !((kb_on >> k_last) & 1ull)) continue;
+      const int a = pk.x;
       if (a != cur_atom) {
         cur_atom = a;
         const float dx = r[0].h - __ldg(&B.atom_df[3 * a].x), dy = r[1].h - __ldg(&B.atom_df[3 * a + 1].x),
@@ -111,7 +115,6 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
       }
       const float2 bd = __ldg(B.sh_bound + sh);  // radius^2 (rounded up), l
       if (d2 > bd.x) continue;                   // screened
-      const int4 pk = __ldg(B.sh_pack + sh);
       const int np = (pk.z >> 8) & 0xff;
       float m = -INFINITY;
       for (int k = 0; k < np; ++k) {

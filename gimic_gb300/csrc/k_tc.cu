@@ -290,10 +290,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int mb = f0 + half * (kChunkF / 2);
         const int me = min(mb + kChunkF / 2, Bs.nbf);
         const uint32_t tcol = lane_base + b * kAccStride;
+        int fp_next = mb < me ? fpack[mb] : 0;
 #pragma unroll 1
         for (int mu = mb; mu < me; ++mu) {
           const int u = mu - f0;
-          const int fp = fpack[mu];
+          const int fp = fp_next;
+          if (mu + 1 < me) fp_next = fpack[mu + 1];
           const int sh = fp >> 12;
           if (sh != cur_shell) {
             cur_shell = sh;
@@ -327,14 +329,20 @@ __global__ void __launch_bounds__(kThreads, 1)
           float v[kMats];
 #pragma unroll
           for (int m = 0; m < kMats; ++m) tmem_ld1(tcol + m * kChunkF + u, v[m]);
+          // while the loads are in flight: the column scales and the
+          // function's value, gradient and Laplacian (all zero on lanes
+          // whose shell is screened, as f1 = f2 = f3 = 0 there)
+          const float* cs = icol + c * kBlockN + u;
+          float sc[kMats];
+#pragma unroll
+          for (int m = 0; m < kMats; ++m) sc[m] = cs[m * kChunkF];
+          float ph, gx, gy, gz, lp;
+          cart_case(fp & 0xfff, cp, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
           tmem_wait7(v);
-          if (on) {
-            float ph, gx, gy, gz, lp;
-            cart_case(fp & 0xfff, cp, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
-            const float* cs = icol + c * kBlockN + u;
-            const float w0 = v[0] * cs[0];
-            const float wc[3] = {v[1] * cs[1 * kChunkF], v[2] * cs[2 * kChunkF], v[3] * cs[3 * kChunkF]};
-            const float qq[3] = {v[4] * cs[4 * kChunkF], v[5] * cs[5 * kChunkF], v[6] * cs[6 * kChunkF]};
+          {
+            const float w0 = v[0] * sc[0];
+            const float wc[3] = {v[1] * sc[1], v[2] * sc[2], v[3] * sc[3]};
+            const float qq[3] = {v[4] * sc[4], v[5] * sc[5], v[6] * sc[6]};
             const float wp = w0 * ph;
             part[0] = fmaf(w0, ph, part[0]);
             part[1] = fmaf(wp, sx, part[1]);

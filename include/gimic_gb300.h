@@ -81,6 +81,15 @@ int gg_set_max_batch(gg_ctx *ctx, int64_t npts);           /* points per device 
  * shells that are screened for all of its points (on by default; results do
  * not change, only the work skipped). */
 int gg_set_tile_screening(gg_ctx *ctx, int enable);
+/* Internal order of the shells (and so of the basis functions and density
+ * rows/columns).  mode 1 (the default, set at creation): shells grouped by
+ * screening radius, atoms along a nearest-neighbour tour, when that activates
+ * fewer tiles' K blocks and column chunks than the file order; mode 0: the
+ * file order.  Results are the same up to rounding.  gg_get_shell_order
+ * returns the mode and, when order is not NULL, order[k] = file index of the
+ * shell at position k (nshells entries, see gg_basis_info). */
+int gg_set_shell_order(gg_ctx *ctx, int mode);
+int gg_get_shell_order(const gg_ctx *ctx, int *mode, int *order);
 
 /* nbf: contracted Cartesian functions; turbomole: 1 if the MOL file has the
  * TURBOMOLE header (component order gtodefs.f90:108-123). */

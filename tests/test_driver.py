@@ -10,7 +10,7 @@ import shutil
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, rel_max_err
+from conftest import GOLDEN
 from gimic_gb300 import driver
 
 pytestmark = pytest.mark.gpu
@@ -60,6 +60,21 @@ def _vtk_vectors(path, name):
     return np.array(m.group(1).split(), dtype=np.float64)
 
 
+def _print_ulp(x):
+    """One unit in the last place of Fortran e14.6 output (0.dddddd E+ee)."""
+    ax = np.abs(x)
+    e = np.floor(np.log10(np.where(ax > 0, ax, 1.0))) + 1.0
+    return np.where(ax > 0, 10.0 ** (e - 6), 0.0)
+
+
+def _agree_printed(got, ref, tol=1e-6):
+    """Both sides are e14.6 prints: each element may differ by the path's
+    error (tol x the largest value) plus one unit of the print, since the two
+    roundings can fall on either side of a digit."""
+    bound = tol * np.abs(ref).max() + np.maximum(_print_ulp(got), _print_ulp(ref))
+    return bool(np.all(np.abs(got - ref) <= bound))
+
+
 def test_openshell_3d_cdens_files(tmp_path, golden_dir):
     d = _workdir(tmp_path, golden_dir, "open-shell", "3d.inp")
     drv = driver.Driver(str(d / "gimic.inp"), precision="split16", stream=io.StringIO())
@@ -69,9 +84,9 @@ def test_openshell_3d_cdens_files(tmp_path, golden_dir):
     for tag, spin in (("", "total"), ("alpha", "alpha"), ("beta", "beta"), ("spindens", "spindens")):
         jv = _vtk_vectors(d / ("jvec%s.vti" % tag), "vectors").reshape(-1, 3)
         assert jv.shape == (33 ** 3, 3)
-        assert rel_max_err(jv[idx], ref["jvec_" + spin]) <= 2e-6  # 1e-6 path + 6-digit print
+        assert _agree_printed(jv[idx], ref["jvec_" + spin])
         jm = _vtk_vectors(d / ("jmod%s.vti" % tag), "scalars")
-        assert rel_max_err(jm[idx], ref["jmod_" + spin]) <= 2e-6
+        assert _agree_printed(jm[idx], ref["jmod_" + spin])
 
 
 def test_readgrid_vtu(tmp_path, golden_dir):

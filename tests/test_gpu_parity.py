@@ -179,6 +179,40 @@ def test_tile_screening_is_exact(c6h6):
     assert rel_max_err(a[0][sel], o.jtensor(pts[sel])) <= TOL_SPLIT
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL_FP64), ("split16", TOL_SPLIT)])
+def test_shell_order_does_not_change_results(c6h6_uhf, precision, tol):
+    """The locality order permutes the functions and density rows/columns:
+    every output agrees with the file order (and with the oracle) for all
+    spin cases of an open-shell density, and tile screening issues fewer
+    GEMM blocks on a cube."""
+    mp, xp, _ = c6h6_uhf
+    g = api.Gimic(mp, xp, uhf=True, screening=1e-8, precision=precision)
+    o = oracle.Oracle(mp, xp, uhf=True, screening=1e-8)
+    assert g.shell_order()[0] == "locality"
+    pts = sample_points(g.atoms()[0], 1200, 300, 8.0, seed=21)
+    for spin in ("alpha", "beta", "total", "spindens"):
+        g.set_spin(spin)
+        g.set_shell_order("locality")
+        a = g.jtensor_batch(pts, rho=True, divj=True)
+        g.set_shell_order("file")
+        b = g.jtensor_batch(pts, rho=True, divj=True)
+        for x, y in zip(a, b):
+            assert rel_max_err(x, y) <= tol
+        assert rel_max_err(a[0], o.jtensor(pts, spin=spin)) <= tol
+    ax = np.linspace(-16.0, 16.0, 48)
+    cube = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+    g.set_spin("total")
+    blocks = {}
+    for mode in ("file", "locality"):
+        g.set_shell_order(mode)
+        g.profile(True)
+        g.jtensor_batch(cube)
+        blocks[mode] = g.profile_read()["gemm_blocks"][0]
+        g.profile(False)
+    if precision == "split16":
+        assert blocks["locality"] < blocks["file"]
+
+
 def test_profile_counts_screened_work(c6h6):
     mp, xp, _ = c6h6
     g = api.Gimic(mp, xp, screening=1e-8)

@@ -224,3 +224,22 @@ def test_property_files_and_report(tmp_path):
     (tmp_path / "grid_w.grd").unlink()
     assert properties.run(Fake(), missing, str(tmp_path)) is None
     assert "property calculation is skipped" in missing.getvalue()
+
+
+def test_shell_order_permutation(synth_dir):
+    """The locality order is a permutation of the file's shells; switching to
+    the file order and back restores both, and without screening radii the
+    file order is kept."""
+    mp, xp, mol = synth.make_workload("c24h24", str(synth_dir), seed=2024)
+    g = api.Gimic(mp, xp, screening=1e-8)
+    mode, order = g.shell_order()
+    assert mode == "locality"
+    assert sorted(order) == list(range(g.nshells)) and order != list(range(g.nshells))
+    g.set_shell_order("file")
+    assert g.shell_order() == ("file", list(range(g.nshells)))
+    g.set_shell_order("locality")
+    assert g.shell_order() == ("locality", order)
+    with pytest.raises(_lib.GimicError):
+        g.set_shell_order(2)
+    g0 = api.Gimic(mp, xp, screening=0.0)
+    assert g0.shell_order()[1] == list(range(g0.nshells))
