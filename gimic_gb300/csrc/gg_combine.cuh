@@ -56,4 +56,31 @@ __device__ __forceinline__ void combine_point(const double* d, const double r[3]
   }
 }
 
+// The same with GIAO, diamagnetic and paramagnetic terms all on, in
+// double-float arithmetic (about 44 bits; the r_c rho terms cancel
+// algebraically above, so no catastrophic cancellation is left): the FP64
+// pipe, 1/64 of the fp32 rate, is then needed only for the outputs.  d(i)
+// returns bilinear form i (slots as in combine_point) and put(k, v) takes
+// output k (ct(m, b) at m + 3 b, then div_b at 9 + b), so that neither the
+// inputs nor the outputs are held all at once.
+template <typename F, typename G>
+__device__ __forceinline__ void combine_point_df(F d, const DFloat r[3], G put) {
+  constexpr int X = 1, E = 4, Y = 13, YL = 22, Z = 25, ZL = 34;
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    const int e1 = (b + 1) % 3, e2 = (b + 2) % 3;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      DFloat t = df_add(d(Z + 3 * b + m), df_sub(df_mul(r[e1], d(Y + 3 * e2 + m)), df_mul(r[e2], d(Y + 3 * e1 + m))));
+      if (m == e1) t = df_sub(t, d(X + e2));
+      if (m == e2) t = df_add(t, d(X + e1));
+      put(m + 3 * b, DFloat{0.5f * t.h, 0.5f * t.l});
+    }
+    DFloat v = df_add(d(ZL + b), df_sub(df_mul(r[e1], d(YL + e2)), df_mul(r[e2], d(YL + e1))));
+    const DFloat w = df_sub(d(E + 3 * e1 + e2), d(E + 3 * e2 + e1));
+    v = df_sub(v, DFloat{2.f * w.h, 2.f * w.l});
+    put(9 + b, DFloat{0.5f * v.h, 0.5f * v.l});
+  }
+}
+
 }  // namespace gg

@@ -71,6 +71,22 @@ __device__ __forceinline__ void store_outputs(const Outputs& out, int64_t o, con
     for (int i = 0; i < 3; ++i) out.divt32[3 * o + i] = static_cast<float>(dv[i]);
 }
 
+// Output k of a point (ct(m, b) at m + 3 b for k < 9, div_b at 9 + b) and
+// its density, for whichever of the output arrays are set.
+__device__ __forceinline__ void store_output(const Outputs& out, int64_t o, int k, double v) {
+  if (k < 9) {
+    if (out.jt) out.jt[9 * o + k] = v;
+    if (out.jt32) out.jt32[9 * o + k] = static_cast<float>(v);
+  } else {
+    if (out.divt) out.divt[3 * o + (k - 9)] = v;
+    if (out.divt32) out.divt32[3 * o + (k - 9)] = static_cast<float>(v);
+  }
+}
+__device__ __forceinline__ void store_density(const Outputs& out, int64_t o, double rho) {
+  if (out.rho) out.rho[o] = rho;
+  if (out.rho32) out.rho32[o] = static_cast<float>(rho);
+}
+
 // Split-FP16 GEMM geometry
 constexpr int kChunkF = 32;              // functions per column chunk
 constexpr int kMats = 7;                 // D, C_x, C_y, C_z, P_x, P_y, P_z
@@ -133,6 +149,21 @@ __device__ __forceinline__ DFloat df_sqr(DFloat a) {
   const float p = __fmul_rn(a.h, a.h);
   const float e = fmaf(a.h, a.h, -p);
   return fast_two_sum(p, fmaf(2.0f * a.h, a.l, e));
+}
+
+// (a.h + a.l) * (b.h + b.l), the product error recovered by fmas
+__device__ __forceinline__ DFloat df_mul(DFloat a, DFloat b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ DFloat df_sub(DFloat a, DFloat b) { return df_add(a, DFloat{-b.h, -b.l}); }
+
+__device__ __forceinline__ double df_to_double(DFloat a) {
+  return static_cast<double>(a.h) + static_cast<double>(a.l);
 }
 
 // a <= b for normalised double-floats

@@ -10,7 +10,8 @@
 //     W[p, (m, nu)] = sum_mu phi_p,mu * M_m[mu, nu],   M = D, C_x, C_y, C_z, P_x, P_y, P_z
 // for 32 functions nu at a time (224 columns), as three fp16 tcgen05 MMAs
 // per K step (hi*hi + hi*lo + lo*hi of power-of-two scaled operands) with
-// fp32 accumulation in TMEM.  The two TMEM accumulators alternate between
+// fp32 accumulation in TMEM (a four-stage TMA/mbarrier pipeline, one
+// operand pair per stage).  The two TMEM accumulators alternate between
 // chunks so that the epilogue of chunk c overlaps the MMAs of chunk c+1.
 //
 // Roles (320 threads):
@@ -34,10 +35,13 @@
 namespace gg {
 
 namespace {
-constexpr int kStages = 2;
+// A stage holds one A piece and one B piece of one K block: (hi, lo) or
+// (lo, hi) in the cross pass, (hi, hi) in the main pass.  Four 44 KiB stages
+// keep up to 132 KiB of loads in flight while the MMAs read the fourth.
+constexpr int kStages = 4;
 constexpr int kTileA = kBlockM * kBlockK * 2;          // 16 KiB
 constexpr int kTileB = kBlockN * kBlockK * 2;          // 28 KiB
-constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;   // 88 KiB
+constexpr int kStageBytes = kTileA + kTileB;           // 44 KiB
 constexpr int kEpiWarps = 8;                           // 2 per TMEM lane quarter
 constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kTmemCols = 512;
@@ -74,8 +78,8 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 int tc_smem_bytes() { return kSmemBytes; }
 
 // Per chunk the MMAs run in two passes over K into the same accumulator:
-// first the two small cross products (hi*lo, lo*hi), then the main product
-// (hi*hi).  Tensor-core accumulation truncates each partial sum to fp32; the
+// first the two small cross products (hi*lo, lo*hi of each K block), then
+// the main product (hi*hi).  Tensor-core accumulation truncates each partial sum to fp32; the
 // small terms are added while the accumulator is still small, which keeps
 // their truncation error negligible (measured: max error of j 1.2e-6 with the
 // products interleaved, 4.6e-7 cross-first, for nbf = 720).
@@ -156,33 +160,20 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (t >= ntiles) break;
         const int64_t tile = tile_of(t);
         const int m0 = static_cast<int>(tile * kBlockM);
-        const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb), nkb2 = (nkb + 1) / 2;
+        const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
         for (int ci = 0; ci < nchunk; ++ci) {
           const int c = chunk_at(tile, ci);
-          // pass 1: A_hi, A_lo, B_hi, B_lo of one K block per stage
-          for (int ki = 0; ki < nkb; ++ki, ++it) {
-            const int kb = kb_at(tile, ki);
+          // cross pass: (A_hi, B_lo) then (A_lo, B_hi) of every K block;
+          // main pass: (A_hi, B_hi) of every K block; one pair per stage
+          for (int q = 0; q < 3 * nkb; ++q, ++it) {
+            const int kb = kb_at(tile, q < 2 * nkb ? q >> 1 : q - 2 * nkb);
+            const bool a_lo = q < 2 * nkb && (q & 1), b_lo = q < 2 * nkb && !(q & 1);
             const int s = it % kStages, round = it / kStages;
             if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto done;
             unsigned char* st = base + s * kStageBytes;
             mbar_expect_tx(&full[s], kStageBytes);
-            tma_load_2d(st, &tm_a_hi, &full[s], kb * kBlockK, m0);
-            tma_load_2d(st + kTileA, &tm_a_lo, &full[s], kb * kBlockK, m0);
-            tma_load_2d(st + 2 * kTileA, &tm_b_hi, &full[s], kb * kBlockK, c * kBlockN);
-            tma_load_2d(st + 2 * kTileA + kTileB, &tm_b_lo, &full[s], kb * kBlockK, c * kBlockN);
-          }
-          // pass 2: A_hi, B_hi of two K blocks per stage (same slots)
-          for (int k2 = 0; k2 < nkb2; ++k2, ++it) {
-            const int s = it % kStages, round = it / kStages;
-            if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto done;
-            unsigned char* st = base + s * kStageBytes;
-            const int ki0 = 2 * k2, nk = (ki0 + 1 < nkb) ? 2 : 1;
-            mbar_expect_tx(&full[s], nk * (kTileA + kTileB));
-            for (int j = 0; j < nk; ++j) {
-              const int kb = kb_at(tile, ki0 + j);
-              tma_load_2d(st + j * kTileA, &tm_a_hi, &full[s], kb * kBlockK, m0);
-              tma_load_2d(st + 2 * kTileA + j * kTileB, &tm_b_hi, &full[s], kb * kBlockK, c * kBlockN);
-            }
+            tma_load_2d(st, a_lo ? &tm_a_lo : &tm_a_hi, &full[s], kb * kBlockK, m0);
+            tma_load_2d(st + kTileA, b_lo ? &tm_b_lo : &tm_b_hi, &full[s], kb * kBlockK, c * kBlockN);
           }
         }
       }
@@ -198,40 +189,23 @@ __global__ void __launch_bounds__(kThreads, 1)
         mbar_arrive(&ring_empty[slot]);
         if (t < 0) break;
         const int64_t tile = tile_of(t);
-        const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb), nkb2 = (nkb + 1) / 2;
+        const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
         for (int ci = 0; ci < nchunk; ++ci, ++acc) {
           const int b = acc & 1, rb = acc >> 1;
           if (!mbar_wait(&accempty[b], (rb & 1) ^ 1, err, 2)) goto done;
           tc_fence_after();
           const uint32_t d_tmem = tmem_base + b * kAccStride;
-          for (int kb = 0; kb < nkb; ++kb, ++it) {
+          // the stage sequence of the producer: 2 nkb cross pieces, then nkb main
+          for (int q = 0; q < 3 * nkb; ++q, ++it) {
             const int s = it % kStages, round = it / kStages;
             if (!mbar_wait(&full[s], round & 1, err, 3)) goto done;
             tc_fence_after();
             unsigned char* st = base + s * kStageBytes;
-            const uint64_t ah = smem_desc_sw128(st), al = smem_desc_sw128(st + kTileA);
-            const uint64_t bh = smem_desc_sw128(st + 2 * kTileA), bl = smem_desc_sw128(st + 2 * kTileA + kTileB);
+            const uint64_t a = smem_desc_sw128(st), b = smem_desc_sw128(st + kTileA);
 #pragma unroll
             for (int k = 0; k < kBlockK / 16; ++k) {
               const uint64_t o = static_cast<uint64_t>(k * 32) >> 4;  // 16 fp16 = 32 bytes along K
-              mma_f16(d_tmem, ah + o, bl + o, idesc, (kb > 0 || k > 0) ? 1u : 0u);
-              mma_f16(d_tmem, al + o, bh + o, idesc, 1u);
-            }
-            mma_commit(&empty[s]);
-          }
-          for (int k2 = 0; k2 < nkb2; ++k2, ++it) {
-            const int s = it % kStages, round = it / kStages;
-            if (!mbar_wait(&full[s], round & 1, err, 3)) goto done;
-            tc_fence_after();
-            unsigned char* st = base + s * kStageBytes;
-            const int nk = (2 * k2 + 1 < nkb) ? 2 : 1;
-            for (int j = 0; j < nk; ++j) {
-              const uint64_t ah = smem_desc_sw128(st + j * kTileA), bh = smem_desc_sw128(st + 2 * kTileA + j * kTileB);
-#pragma unroll
-              for (int k = 0; k < kBlockK / 16; ++k) {
-                const uint64_t o = static_cast<uint64_t>(k * 32) >> 4;
-                mma_f16(d_tmem, ah + o, bh + o, idesc, 1u);
-              }
+              mma_f16(d_tmem, a + o, b + o, idesc, (q > 0 || k > 0) ? 1u : 0u);
             }
             mma_commit(&empty[s]);
           }
@@ -376,27 +350,41 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (i != 4 && i != 8 && i != 12) two_sum_acc(thi[i], tlo[i], part[i]);
       }
       if (!ok) break;
-      // combine the two halves of every point through `red`: half 1 writes
-      // once half 0 has read the previous tile's sums, half 0 reads them
+      // combine the two halves of every point through `red` (float pairs):
+      // half 1 writes once half 0 has read the previous tile's sums, half 0
+      // reads them
+      float2* redf = reinterpret_cast<float2*>(red);
       if (half == 1) {
         if (!mbar_wait(xempty, (tk & 1) ^ 1, err, 5)) break;
 #pragma unroll
-        for (int i = 0; i < kNDots; ++i)
-          red[row * kNDots + i] = static_cast<double>(thi[i]) + static_cast<double>(tlo[i]);
+        for (int i = 0; i < kNDots; ++i) redf[row * kNDots + i] = make_float2(thi[i], tlo[i]);
         __syncwarp();
         if (lane == 0) mbar_arrive(xfull);
       } else {
         if (!mbar_wait(xfull, tk & 1, err, 6)) break;
         if (valid) {
-          double tot[kNDots];
-          const double sc = static_cast<double>(inv_row[p]);
-#pragma unroll
-          for (int i = 0; i < kNDots; ++i)
-            tot[i] = ((static_cast<double>(thi[i]) + static_cast<double>(tlo[i])) + red[row * kNDots + i]) * sc;
-          double ct[9], dv[3];
-          combine_point(tot, r, fl, ct, dv);
+          // the row scale is a power of two: scaling a double-float is exact
+          const float sc = inv_row[p];
+          const float2* h1 = redf + row * kNDots;
+          auto tot = [&](int i) -> DFloat {
+            const float2 o = h1[i];
+            const DFloat t = df_add(DFloat{thi[i], tlo[i]}, DFloat{o.x, o.y});
+            return DFloat{t.h * sc, t.l * sc};
+          };
           const int64_t o = perm ? static_cast<int64_t>(perm[p]) : p;  // caller's point order
-          store_outputs(out, o, ct, tot[0], dv);
+          if (fl.giao && fl.dia && fl.para) {
+            combine_point_df(tot, rdf, [&](int k, DFloat v) { store_output(out, o, k, df_to_double(v)); });
+          } else {
+            double td[kNDots], ct[9], dv[3];
+#pragma unroll
+            for (int i = 0; i < kNDots; ++i) td[i] = df_to_double(tot(i));
+            combine_point(td, r, fl, ct, dv);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) store_output(out, o, k, ct[k]);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) store_output(out, o, 9 + k, dv[k]);
+          }
+          store_density(out, o, df_to_double(tot(0)));
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(xempty);
