@@ -14,16 +14,18 @@
 // operand pair per stage).  The two TMEM accumulators alternate between
 // chunks so that the epilogue of chunk c overlaps the MMAs of chunk c+1.
 //
-// Roles (320 threads):
+// Roles (384 threads, three warpgroups):
 //   warp 0      TMA producer (A: phi pieces of the tile, B: matrix pieces)
 //   warp 1      TMEM owner and MMA issuer
-//   warps 2..9  epilogue, two warps per TMEM lane quarter, each taking half
+//   warps 2, 3  none (they complete the first warpgroup, which hands its
+//               registers to the epilogue)
+//   warps 4..11 epilogue, two warps per TMEM lane quarter, each taking half
 //               of a chunk's functions: for its point (one TMEM lane) it
 //               re-evaluates phi, grad phi and the Laplacian of the chunk's 32
 //               functions in fp32 (src/libgimic/caos.f90:17-110 semantics)
 //               and accumulates the kNDots bilinear forms; fp32 within a
-//               chunk, fp64 across chunks; final fp64 combination as in
-//               gg_combine.cuh (src/libgimic/jtensor.F90:148-237).
+//               chunk, double-float across chunks and in the final
+//               combination (gg_combine.cuh, src/libgimic/jtensor.F90:148-237).
 #include <cuda.h>
 
 #include <algorithm>
@@ -43,12 +45,25 @@ constexpr int kTileA = kBlockM * kBlockK * 2;          // 16 KiB
 constexpr int kTileB = kBlockN * kBlockK * 2;          // 28 KiB
 constexpr int kStageBytes = kTileA + kTileB;           // 44 KiB
 constexpr int kEpiWarps = 8;                           // 2 per TMEM lane quarter
-constexpr int kThreads = 32 * (2 + kEpiWarps);
+constexpr int kCtlWarps = 4;                           // TMA producer, MMA issuer, two idle: one warpgroup
+constexpr int kThreads = 32 * (kCtlWarps + kEpiWarps);
+// Register split (setmaxnreg, per warpgroup): the control warpgroup gives
+// registers up so that the epilogue warpgroups can hold their accumulators,
+// the geometry and the TMEM values of two functions without spilling.  The
+// shares add up to the launch allocation of 168 per thread (65,536 / 384,
+// rounded down to a multiple of 8), which the launcher checks.
+constexpr int kRegsLaunch = 168;
+constexpr int kRegsCtl = 56;
+constexpr int kRegsEpi = 224;
+static_assert(kCtlWarps * kRegsCtl + kEpiWarps * kRegsEpi <= (kCtlWarps + kEpiWarps) * kRegsLaunch,
+              "register split exceeds the launch allocation");
 constexpr uint32_t kTmemCols = 512;
 constexpr int kAccStride = 256;
 constexpr int kRedBytes = kBlockM * kNDots * 8;        // half-sums exchanged between the two epilogue halves
 constexpr int kRing = 4;  // tile steps in flight between the producer and the other roles
 constexpr int kSmemBytes = kStages * kStageBytes + kRedBytes + 1024 + 256;
+
+__device__ __forceinline__ void reg_dealloc_ctl() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kRegsCtl)); }
 
 __device__ __forceinline__ void tmem_ld1(uint32_t taddr, float& v) {
   uint32_t r;
@@ -147,7 +162,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
+  // each role changes its register allocation at its start, so that the
+  // compiler allocates every role's code with that role's budget
   if (warp == 0) {
+    reg_dealloc_ctl();
     if (lane == 0) {
       int it = 0;
       for (int step = 0;; ++step) {
@@ -179,6 +197,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else if (warp == 1) {
+    reg_dealloc_ctl();
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_f16(kBlockM, kBlockN);
       int it = 0, acc = 0;
@@ -213,12 +232,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
     }
-  } else {
+  } else if (warp >= kCtlWarps) {
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kRegsEpi));
     // ---------------- epilogue: 8 warps ----------------
     // warp w reads TMEM lanes 32*(w%4) .. +31 (its 32 points) and handles
-    // half (w-2)/4 of the 32 functions of every chunk.
+    // half (w-4)/4 of the 32 functions of every chunk.
     const int q = warp & 3;
-    const int half = (warp - 2) >> 2;
+    const int half = (warp - kCtlWarps) >> 2;
     const int row = q * 32 + lane;
     const uint32_t lane_base = tmem_base + (static_cast<uint32_t>(q * 32) << 16);
     int acc = 0, tk = 0;
@@ -390,6 +410,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(xempty);
       }
     }
+  } else {
+    reg_dealloc_ctl();  // warps 2 and 3: no role
   }
 done:
   tc_fence_before();
@@ -406,6 +428,12 @@ cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st)
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(tc_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     if (e != cudaSuccess) return e;
+    // the register split assumes the launch allocation; with fewer registers
+    // per thread the epilogue's setmaxnreg.inc could never be granted
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, tc_fused_kernel);
+    if (e != cudaSuccess) return e;
+    if (fa.numRegs < kRegsLaunch) return cudaErrorInvalidConfiguration;
     attr_set = true;
   }
   static int nsm[64] = {0};
