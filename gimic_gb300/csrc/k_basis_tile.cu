@@ -154,12 +154,13 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
       active = kb < nkb && ((kb_on >> kb) & 1ull);
     }
   };
-  auto emit = [&](int mu, float v) {
+  auto emit = [&](int mu, float v, bool zero) {
     const int k = mu >> 6;
     if (k != kb) advance_to(k);
     if (!active) return;
-    const __half h = __float2half_rn(v);
-    const __half l = __float2half_rn(v - __half2float(h));
+    const __half z = __float2half_rn(0.f);
+    const __half h = zero ? z : __float2half_rn(v);
+    const __half l = zero ? z : __float2half_rn(v - __half2float(h));
     if ((mu & 1) == 0) {
       st.ph = h;
       st.pl = l;
@@ -192,10 +193,16 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
         pz[3] = pz[2] * pz[1];
       }
       float f1 = 0.f;
-      if (df_le(d2, __ldg(B.sh_rad2_df + sh))) {
+      const bool in_range = df_le(d2, __ldg(B.sh_rad2_df + sh));
+      if (in_range) {
         for (int k = 0; k < np; ++k)
           f1 += __ldg(B.p_cc + pk.w + k) * gauss_df(__ldg(B.p_xp + pk.w + k), __ldg(B.p_xplo + pk.w + k), d2.h, d2.l);
         f1 *= scale;
+      }
+      // a shell out of range for the whole warp only writes zeros
+      if (!__any_sync(0xffffffffu, in_range)) {
+        for (int c = 0; c < ncomp; ++c) emit(mu0 + c, 0.f, true);
+        continue;
       }
       for (int c = 0; c < ncomp; ++c) {
         const int ijk = __ldg(B.f_ijk + mu0 + c);
@@ -203,11 +210,11 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
         const float xi = i == 0 ? 1.f : (i == 1 ? px[1] : (i == 2 ? px[2] : px[3]));
         const float yj = j == 0 ? 1.f : (j == 1 ? py[1] : (j == 2 ? py[2] : py[3]));
         const float zk = k == 0 ? 1.f : (k == 1 ? pz[1] : (k == 2 ? pz[2] : pz[3]));
-        emit(mu0 + c, xi * yj * zk * f1);
+        emit(mu0 + c, xi * yj * zk * f1, false);
       }
     }
     // padding columns nbf .. kpad-1 of the last K block are zero
-    for (int mu = B.nbf; mu < B.kpad; ++mu) emit(mu, 0.f);
+    for (int mu = B.nbf; mu < B.kpad; ++mu) emit(mu, 0.f, true);
     advance_to(nkb);
   }
   if (threadIdx.x == 0) bulk_wait_all();
