@@ -39,7 +39,15 @@ struct DevBasis {
   const float2* p_bound;   // {a log2(e) (rounded down), log2 |c| + log2(npf of the shell) (rounded up)}
   const double* p_xpd;     // same in fp64
   const double* p_ccd;
+  // Row-scale envelope: atom_env[a * env_bins + b] bounds log2 |phi| over all
+  // in-range shells of atom a at squared distances d2 with
+  // floor((log2 d2 + kEnvOffset) * kEnvPerOctave) = b (bin 0 also takes
+  // every smaller d2; -inf where no shell of the atom reaches).
+  const float* atom_env;
+  int env_bins;
 };
+constexpr float kEnvPerOctave = 8.f;
+constexpr float kEnvOffset = 14.f;
 
 // Flags of the tensor assembly (src/libgimic/jtensor.F90:148-237 switches)
 struct Flags {

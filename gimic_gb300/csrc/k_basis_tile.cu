@@ -11,12 +11,16 @@
 // The row's power-of-two scale has to be known before the first value is
 // written, so a first pass computes an upper bound of max_mu |phi_mu| in the
 // log domain, without exponentials:
-//   |x^i y^j z^k sum_p c_p e^{-a_p d^2}| <= d^l npf max_p |c_p| e^{-a_p d^2}.
-// The scale puts that bound just under 2^14.  When the bound exceeds the
-// true row maximum by 2^k, the values whose fp16 lo part is subnormal are
-// stored with an absolute error of at most 2^(k-38) times the row maximum;
-// k stays below 4 for the seeded bases (checked against the oracle's basis
-// values), i.e. far below 1e-9 of the maximum.
+//   |x^i y^j z^k sum_p c_p e^{-a_p d^2}| <= d^l npf max_p |c_p| e^{-a_p d^2},
+// read per atom from a host-built envelope of its shells' bounds over bins
+// of log2 d^2 (one lookup per atom instead of a walk over the shells and
+// primitives).  The scale puts that bound just under 2^14.  When the bound
+// exceeds the true row maximum by 2^k, the values whose fp16 lo part is
+// subnormal are stored with an absolute error of at most 2^(k-38) times the
+// row maximum.  The per-shell bound exceeds the maximum by 2^0.05..2^3.8 on
+// the seeded bases (checked against the oracle's basis values) and the
+// envelope adds at most 2.4 bits (median 0.1), so k < 7: far below 1e-9 of
+// the maximum.
 //
 // Values go to a shared-memory tile laid out in the 128-byte swizzle that the
 // contraction's TMA loads expect, and every finished 128 x 64 K block is
@@ -96,32 +100,20 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
   for (int c = 0; c < 3; ++c) r[c] = df_split(pts[3 * p + c]);
 
   // ---- pass 1: log2 of an upper bound of |phi| over the row -------------
+  // one table lookup per atom: the envelope of its shells' bounds at the
+  // point's distance (shells of K blocks inactive for the tile are out of
+  // range of every point of it, so the envelope does not see them)
   float lb = -INFINITY;
   {
-    int cur_atom = -1;
-    float d2 = 0.f, hl2d = 0.f;
-    for (int sh = 0; sh < B.nshells; ++sh) {
-      const int4 pk = __ldg(B.sh_pack + sh);  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
-      // shells of inactive K blocks are never stored, so they do not enter the bound
-      const int k_first = pk.y >> 6, k_last = (pk.y + (pk.z & 0xff) - 1) >> 6;
-      if (!((kb_on >> k_first) & 1ull) && !((kb_on >> k_last) & 1ull)) continue;
-      const int a = pk.x;
-      if (a != cur_atom) {
-        cur_atom = a;
-        const float dx = r[0].h - __ldg(&B.atom_df[3 * a].x), dy = r[1].h - __ldg(&B.atom_df[3 * a + 1].x),
-                    dz = r[2].h - __ldg(&B.atom_df[3 * a + 2].x);
-        d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        hl2d = 0.5f * __log2f(fmaxf(d2, 1e-30f));
-      }
-      const float2 bd = __ldg(B.sh_bound + sh);  // radius^2 (rounded up), l
-      if (d2 > bd.x) continue;                   // screened
-      const int np = (pk.z >> 8) & 0xff;
-      float m = -INFINITY;
-      for (int k = 0; k < np; ++k) {
-        const float2 pb = __ldg(B.p_bound + pk.w + k);  // a log2 e, log2 |c| + log2 npf
-        m = fmaxf(m, fmaf(-pb.x, d2, pb.y));
-      }
-      lb = fmaxf(lb, bd.y > 0.f ? fmaf(bd.y, hl2d, m) : m);
+    const float* __restrict__ env = B.atom_env;
+    const int nb = B.env_bins;
+    for (int a = 0; a < B.natoms; ++a) {
+      const float dx = r[0].h - __ldg(&B.atom_df[3 * a].x), dy = r[1].h - __ldg(&B.atom_df[3 * a + 1].x),
+                  dz = r[2].h - __ldg(&B.atom_df[3 * a + 2].x);
+      const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const float t = (__log2f(fmaxf(d2, 1e-30f)) + kEnvOffset) * kEnvPerOctave;
+      const int bin = t <= 0.f ? 0 : static_cast<int>(t);
+      if (bin < nb) lb = fmaxf(lb, __ldg(env + static_cast<int64_t>(a) * nb + bin));
     }
   }
   float scale = 1.f;

@@ -59,7 +59,7 @@ void mkgausspoints(double *a, double *b, int *npts, int *order, double *pts, dou
 #define GG_EUNSUPPORTED (-6)
 
 #define GG_PREC_FP64 0     /* plain FP64 path: SIMT DGEMM + FP64 assembly */
-#define GG_PREC_SPLIT16 1  /* split-FP16 x3 tcgen05 GEMM, FP32 accumulate, FP64 combine (default) */
+#define GG_PREC_SPLIT16 1  /* split-FP16 x3 tcgen05 GEMM, FP32 accumulate, double-float combine (default) */
 
 typedef struct gg_ctx gg_ctx;
 
@@ -76,7 +76,11 @@ int gg_get_magnet(const gg_ctx *ctx, double b[3]);
 int gg_set_screening(gg_ctx *ctx, double thrs);            /* takes effect on the next evaluation */
 int gg_set_flags(gg_ctx *ctx, int giao, int diamag, int paramag);  /* Advanced.GIAO/diamag/paramag */
 int gg_set_precision(gg_ctx *ctx, int mode);               /* GG_PREC_* */
-int gg_set_max_batch(gg_ctx *ctx, int64_t npts);           /* points per device pass (scratch size) */
+/* Points per device pass (scratch size), at least 128.  By default the split
+ * path takes the largest power of two from 2^18 to 2^21 whose scratch (two
+ * pipeline slots of 4 nbf + 128 bytes per point) fits 16 GiB; the FP64 path
+ * at most 16,384. */
+int gg_set_max_batch(gg_ctx *ctx, int64_t npts);
 /* Split path: order the points into compact tiles and skip, per tile, the
  * shells that are screened for all of its points (on by default; results do
  * not change, only the work skipped). */
