@@ -65,18 +65,20 @@ EncodeTiled get_encoder() {
   return fn;
 }
 
-// 2-D fp16 tensor [rows][cols] (cols contiguous) loaded in boxes of
-// box_rows x 64 with a 128-byte swizzle.
-bool encode_fp16_2d(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+// 2-D fp16 tensor [rows][cols] (cols contiguous) moved in boxes of
+// box_rows x 64 with the 128-byte swizzle (the contraction's loads) or, with
+// half, box_rows x 32 with the 64-byte swizzle (the basis kernel's stores).
+bool encode_fp16_2d(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows,
+                    bool half = false) {
   EncodeTiled enc = get_encoder();
   if (!enc) return false;
   const cuuint64_t dims[2] = {cols, rows};
   const cuuint64_t strides[1] = {cols * 2};
-  const cuuint32_t box[2] = {64, box_rows};
+  const cuuint32_t box[2] = {half ? 32u : 64u, box_rows};
   const cuuint32_t estr[2] = {1, 1};
   return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+             CU_TENSOR_MAP_INTERLEAVE_NONE, half ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 bool is_device_ptr(const void* p) {
@@ -138,7 +140,8 @@ struct gg_ctx {
   struct SplitSlot {
     DevBuf a_hi, a_lo, inv_row, sort_keys, sort_keys2, sort_idx, sort_perm, sort_temp, pts_sorted, tile_lists,
         tile_ord;
-    CUtensorMap tma_hi, tma_lo;
+    CUtensorMap tma_hi, tma_lo;  // the contraction's loads
+    CUtensorMap tms_hi, tms_lo;  // the basis kernel's stores
     const double* tp = nullptr;
     const int* tiles = nullptr;
     const int* perm = nullptr;
@@ -398,6 +401,15 @@ struct gg_ctx {
     if (e == cudaSuccess) e = upload(p_xpd, &d.p_xpd);
     if (e == cudaSuccess) e = upload(p_ccd, &d.p_ccd);
     if (e == cudaSuccess) e = upload(env, &d.atom_env);
+    std::vector<float4> atom_f4;
+    for (const gg::Atom& a : b.atoms)
+      atom_f4.push_back(make_float4(static_cast<float>(a.coord[0]), static_cast<float>(a.coord[1]),
+                                    static_cast<float>(a.coord[2]), 0.f));
+    std::vector<float> sh_radf;
+    for (const gg::Shell& s : b.shells)
+      sh_radf.push_back(std::nextafter(static_cast<float>(std::min(s.radius, 1e30)), INFINITY));
+    if (e == cudaSuccess) e = upload(atom_f4, &d.atom_f4);
+    if (e == cudaSuccess) e = upload(sh_radf, &d.sh_rad);
     d.env_bins = env_bins;
     if (e != cudaSuccess) return cuda_fail(e, "uploading basis tables");
     if (!d_err) {
@@ -658,10 +670,12 @@ struct gg_ctx {
       sl.tord = sl.tile_ord.as<int>();
     }
     if (!encode_fp16_2d(&sl.tma_hi, sl.a_hi.p, n, dB.kpad, gg::kBlockM) ||
-        !encode_fp16_2d(&sl.tma_lo, sl.a_lo.p, n, dB.kpad, gg::kBlockM))
+        !encode_fp16_2d(&sl.tma_lo, sl.a_lo.p, n, dB.kpad, gg::kBlockM) ||
+        !encode_fp16_2d(&sl.tms_hi, sl.a_hi.p, n, dB.kpad, gg::kBlockM, true) ||
+        !encode_fp16_2d(&sl.tms_lo, sl.a_lo.p, n, dB.kpad, gg::kBlockM, true))
       return fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
     prof_begin(GG_PROF_BASIS, st, &ps);
-    e = gg::launch_basis_tile(dB, &sl.tma_hi, &sl.tma_lo, sl.tp, n, sl.tiles, stride, sl.inv_row.as<float>(), st);
+    e = gg::launch_basis_tile(dB, &sl.tms_hi, &sl.tms_lo, sl.tp, n, sl.tiles, stride, sl.inv_row.as<float>(), st);
     prof_end(st, ps);
     if (e != cudaSuccess) return cuda_fail(e, "basis kernel launch");
     launches += 1;
@@ -1508,11 +1522,13 @@ extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t 
   e = noalloc_counter(ctx->device, &tile_counter);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaGetSymbolAddress(no-allocation tile counter)");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  CUtensorMap tma_hi, tma_lo;
+  CUtensorMap tma_hi, tma_lo, tms_hi, tms_lo;
   if (!encode_fp16_2d(&tma_hi, a_hi, n, ctx->dB.kpad, gg::kBlockM) ||
-      !encode_fp16_2d(&tma_lo, a_lo, n, ctx->dB.kpad, gg::kBlockM))
+      !encode_fp16_2d(&tma_lo, a_lo, n, ctx->dB.kpad, gg::kBlockM) ||
+      !encode_fp16_2d(&tms_hi, a_hi, n, ctx->dB.kpad, gg::kBlockM, true) ||
+      !encode_fp16_2d(&tms_lo, a_lo, n, ctx->dB.kpad, gg::kBlockM, true))
     return ctx->fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
-  e = gg::launch_basis_tile(ctx->dB, &tma_hi, &tma_lo, pts, n, nullptr, 0, inv_row, st);
+  e = gg::launch_basis_tile(ctx->dB, &tms_hi, &tms_lo, pts, n, nullptr, 0, inv_row, st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "basis kernel launch");
   gg::TcArgs ta{&tma_hi, &tma_lo, &ctx->tm_b_hi, &ctx->tm_b_lo, inv_row, ctx->inv_col.as<float>(),
                 pts,     n,       ctx->flags,     gg::Outputs{jt, rho, divt}, ctx->d_err};

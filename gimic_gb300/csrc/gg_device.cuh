@@ -45,6 +45,8 @@ struct DevBasis {
   // every smaller d2; -inf where no shell of the atom reaches).
   const float* atom_env;
   int env_bins;
+  const float4* atom_f4;   // natoms: {x, y, z, 0} in fp32 (tile screening)
+  const float* sh_rad;     // screening radius in fp32, rounded up (tile screening)
 };
 constexpr float kEnvPerOctave = 8.f;
 constexpr float kEnvOffset = 14.f;

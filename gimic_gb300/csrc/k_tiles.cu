@@ -91,13 +91,18 @@ __global__ void __launch_bounds__(128) tile_screen_kernel(DevBasis B, const doub
     const double h = 0.5 * (bmax[d][0] - bmin[d][0]);
     rho2 += h * h;
   }
-  const double rho = sqrt(rho2);
+  // fp32 without square roots (the FP64 pipe runs at 1/64 of the fp32
+  // rate): out of range when |R_A - c|^2 > (radius + rho)^2, the right side
+  // widened by 1e-5 relative and 1e-4 Bohr^2, far above the fp32 rounding of
+  // either side, so the test stays conservative
+  const float rhof = static_cast<float>(sqrt(rho2)) * (1.f + 1e-6f);
+  const float cf[3] = {static_cast<float>(c[0]), static_cast<float>(c[1]), static_cast<float>(c[2])};
   for (int sh = threadIdx.x; sh < B.nshells; sh += 128) {
-    const int a = B.sh_atom[sh];
-    const double dx = B.atom_xyz[3 * a] - c[0], dy = B.atom_xyz[3 * a + 1] - c[1], dz = B.atom_xyz[3 * a + 2] - c[2];
-    const double dist = sqrt(dx * dx + dy * dy + dz * dz);
-    const double rad = sqrt(B.sh_rad2[sh]);
-    shell_on[sh] = !(dist - rho > rad * (1.0 + 1e-12) + 1e-9);
+    const float4 at = __ldg(B.atom_f4 + __ldg(B.sh_atom + sh));
+    const float dx = at.x - cf[0], dy = at.y - cf[1], dz = at.z - cf[2];
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float reach = __ldg(B.sh_rad + sh) + rhof;
+    shell_on[sh] = !(d2 > fmaf(reach * reach, 1.00001f, 1e-4f));
   }
   __syncthreads();
   for (int mu = threadIdx.x; mu < B.nbf; mu += 128)
