@@ -72,6 +72,8 @@ class Driver:
 
     def run(self):
         calc = self.kw.get("calc")
+        for w in getattr(self.grid, "warnings", []):
+            self.stream.write(" WARNING: %s\n" % w)
         if self.kw.get("dryrun"):
             _out(self.stream, "Dry run, not calculating ...")
             return {}

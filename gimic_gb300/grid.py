@@ -222,6 +222,13 @@ def _setup_gauss(g, inp, quadrature):
             adjusted = True
     g.adjusted = adjusted
     g.gauss = True
+    # the Newton iteration for the Lobatto nodes is unreliable above 13
+    # points per panel; like lobattomy (src/libgimic/gaussint.f90:68-75) the
+    # grid is kept and a warning is issued
+    g.warnings = []
+    if quadrature == "lobatto" and order > 13:
+        g.warnings = ["lobattomy(): Warning, too many Gauss points:%4d" % order,
+                      "lobattomy(): using this many points is not stable."]
     g.pts, g.wgt = [], []
     for i in range(3):
         if npts[i] > 0:

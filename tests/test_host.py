@@ -186,6 +186,13 @@ def test_bond_grid_geometry(c6h6):
     pts = g.points()
     assert pts.shape == (3600, 3)
     assert np.array_equal(pts[61], g.gridpoint(1, 1, 0))
+    assert g.warnings == []
+    # above 13 Lobatto points per panel the reference warns and goes on
+    # (gaussint.f90:68-75); the rule itself is then not reliable
+    i14 = ginp.read(text.replace("gauss_order=10", "gauss_order=14").replace("[60, 60, 0]", "[56, 56, 0]"),
+                    is_text=True)
+    g14 = ggrid.new_grid(i14, mol.coords)
+    assert g14.warnings[0] == "lobattomy(): Warning, too many Gauss points:  14"
 
 
 def test_property_files_and_report(tmp_path):
