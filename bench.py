@@ -414,6 +414,10 @@ def run_proposal(args):
                        "train_planes": len(train), "held_out_planes": len(held), "samples": int(x.shape[0]),
                        "rule": P.DEFAULT_RULE},
             "uniform_points_total": u, "adaptive_points_total": a,
+            # against the uniform 200 x 200 grid that is the judge and the
+            # fallback (the value above compares with the smallest uniform
+            # grid from which every finer one is converged, a stricter base)
+            "vs_uniform_judge_grid": 40000.0 * len(rows) / a,
             "adaptive_max_err_nAT": max(errs), "planes_within_0.01": int(sum(e <= 0.01 for e in errs)),
             "untrained_max_err_nAT": max(abs(r["untrained_err_nAT"]) for r in rows),
             "untrained_planes_within_0.01": int(sum(abs(r["untrained_err_nAT"]) <= 0.01 for r in rows)),
