@@ -80,13 +80,13 @@ __device__ __forceinline__ void tmem_wait7(float* v) {
                : "memory");
 }
 
-// error-free fp32 sum: s + e = a + b exactly (Knuth two-sum)
+// compensated fp32 sum (Kahan): hi + lo tracks the running total; lo holds
+// what the last additions lost and is fed into the next one
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
-  const float s = hi + x;
-  const float bp = s - hi;
-  const float e = (hi - (s - bp)) + (x - bp);
-  hi = s;
-  lo += e;
+  const float y = x + lo;
+  const float t = hi + y;
+  lo = y - (t - hi);
+  hi = t;
 }
 }  // namespace
 
