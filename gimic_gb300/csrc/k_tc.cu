@@ -81,9 +81,9 @@ __device__ __forceinline__ void tmem_wait7(float* v) {
 }
 
 // compensated fp32 sum (Kahan): hi + lo tracks the running total; lo holds
-// what the last additions lost and is fed into the next one
-__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
-  const float y = x + lo;
+// what the last addition lost.  The chunk's partial sum y starts from lo
+// (instead of zero), which feeds the loss into the next addition.
+__device__ __forceinline__ void kahan_add(float& hi, float& lo, float y) {
   const float t = hi + y;
   lo = y - (t - hi);
   hi = t;
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       float sx = 0.f, sy = 0.f, sz = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
       CartPow cp = cart_pow(0.f, 0.f, 0.f);
       DFloat d2a{0.f, 0.f};
-      bool on = false;
+      bool on = false, warp_on = false;
       const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
       for (int ci = 0; ci < nchunk; ++ci, ++acc) {
         const int c = chunk_at(tile, ci);
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc_fence_after();
         float part[kNDots];
 #pragma unroll
-        for (int i = 0; i < kNDots; ++i) part[i] = 0.f;
+        for (int i = 0; i < kNDots; ++i) part[i] = tlo[i];
         const int f0 = c * kChunkF;
         const int mb = f0 + half * (kChunkF / 2);
         const int me = min(mb + kChunkF / 2, Bs.nbf);
@@ -305,6 +305,17 @@ __global__ void __launch_bounds__(kThreads, 1)
               cp = cart_pow(sx, sy, sz);
             }
             on = df_le(d2a, shr[sh]);
+            // a shell screened for all 32 points of the warp contributes
+            // nothing: skip its remaining functions in this range
+            warp_on = __any_sync(0xffffffffu, on);
+            if (!warp_on) {
+              const int last = min(me, pk.y + (pk.z & 0xff)) - 1;
+              if (last > mu) {
+                mu = last;
+                fp_next = mu + 1 < me ? fpack[mu + 1] : 0;
+              }
+              continue;
+            }
             f1 = f2 = f3 = 0.f;
             if (on) {
               const int np = (pk.z >> 8) & 0xff;
@@ -318,8 +329,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               }
             }
           }
-          // functions screened for all 32 points of the warp contribute nothing
-          if (!__any_sync(0xffffffffu, on)) continue;
+          if (!warp_on) continue;
           float v[kMats];
 #pragma unroll
           for (int m = 0; m < kMats; ++m) tmem_ld1(tcol + m * kChunkF + u, v[m]);
@@ -367,7 +377,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(&accempty[b]);
 #pragma unroll
         for (int i = 0; i < kNDots; ++i)
-          if (i != 4 && i != 8 && i != 12) two_sum_acc(thi[i], tlo[i], part[i]);
+          if (i != 4 && i != 8 && i != 12) kahan_add(thi[i], tlo[i], part[i]);
       }
       if (!ok) break;
       // combine the two halves of every point through `red` (float pairs):
