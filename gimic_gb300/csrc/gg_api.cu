@@ -273,7 +273,6 @@ struct gg_ctx {
     for (const gg::Atom& a : b.atoms) axyz.insert(axyz.end(), a.coord, a.coord + 3);
     std::vector<int> f_shell = b.func_shell, f_ijk(b.nbf), sh_atom, sh_prim, sh_npf, sh_l, sh_f0, sh_ncomp;
     std::vector<int4> sh_pack;
-    std::vector<float2> sh_bound, p_bound;
     std::vector<double> sh_rad2, p_xpd, p_ccd;
     std::vector<float> p_xp, p_xplo, p_cc;
     std::vector<float2> sh_rad2_df, atom_df;
@@ -313,18 +312,11 @@ struct gg_ctx {
         p_cc.push_back(static_cast<float>(s.ncc[i]));
       }
     }
-    // per-shell and per-primitive records of the shell-blocked basis kernel;
-    // the row-scale bound is |phi| <= d^l npf max_p |c_p| exp(-a_p d^2)
+    // per-shell records of the shell-blocked kernels
     for (size_t si = 0; si < b.shells.size(); ++si) {
       const gg::Shell& sh = b.shells[si];
       sh_pack.push_back(make_int4(sh.atom, sh_f0[si],
                                   sh_ncomp[si] | (static_cast<int>(sh.xp.size()) << 8) | (sh.l << 16), sh_prim[si]));
-      sh_bound.push_back(make_float2(static_cast<float>(sh.radius * sh.radius * (1.0 + 1e-4)),
-                                     static_cast<float>(sh.l)));
-      for (size_t i = 0; i < sh.xp.size(); ++i)
-        p_bound.push_back(make_float2(static_cast<float>(sh.xp[i] * 1.4426950408889634 * (1.0 - 1e-6)),
-                                      static_cast<float>(std::log2(std::max(std::fabs(sh.ncc[i]), 1e-300)) +
-                                                         std::log2(static_cast<double>(sh.xp.size())) + 1e-4)));
     }
     // per-atom envelope of the row-scale bound over bins of log2 d^2 (the
     // shell bound l log2 d + max_p (log2 |c_p| + log2 npf - a_p log2(e) d^2)
@@ -386,8 +378,6 @@ struct gg_ctx {
     if (e == cudaSuccess) e = upload(sh_f0, &d.sh_f0);
     if (e == cudaSuccess) e = upload(sh_ncomp, &d.sh_ncomp);
     if (e == cudaSuccess) e = upload(sh_pack, &d.sh_pack);
-    if (e == cudaSuccess) e = upload(sh_bound, &d.sh_bound);
-    if (e == cudaSuccess) e = upload(p_bound, &d.p_bound);
     if (e == cudaSuccess) e = upload(sh_rad2, &d.sh_rad2);
     if (e == cudaSuccess) e = upload(sh_rad2_df, &d.sh_rad2_df);
     if (e == cudaSuccess) e = upload(atom_df, &d.atom_df);

@@ -35,8 +35,6 @@ struct DevBasis {
   const float4* p_pack;    // {p_xp, p_xplo, p_cc, 0} per primitive
   int nprim;
   const int4* sh_pack;     // {atom, first function, ncomp | npf << 8 | l << 16, first primitive}
-  const float2* sh_bound;  // {squared radius (fp32, rounded up), l}
-  const float2* p_bound;   // {a log2(e) (rounded down), log2 |c| + log2(npf of the shell) (rounded up)}
   const double* p_xpd;     // same in fp64
   const double* p_ccd;
   // Row-scale envelope: atom_env[a * env_bins + b] bounds log2 |phi| over all
@@ -337,19 +335,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
 }
-
-// 32 lanes x 32 bit, 8 consecutive columns per thread
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr)
-               : "memory");
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Shared-memory matrix descriptor (tcgen05 format): K-major operand whose
 // rows are 128 bytes, 128-byte swizzle, 8-row groups 1024 bytes apart.
