@@ -7,11 +7,20 @@ evaluation on numpy arrays or CUDA torch tensors and plane integrals.  All
 evaluation runs in libgimic_gb300.so on the GPU.
 """
 import ctypes as C
+import math
 
 import numpy as np
 
 from . import _lib
 from ._lib import GG_PREC_FP64, GG_PREC_SPLIT16, check
+
+# gg_grid as a numpy record (same offsets as _lib.GridSpec; checked below)
+_GRID_DTYPE = np.dtype({"names": ["origin", "basv", "npts", "pts", "wgt", "radius"],
+                        "formats": [(np.float64, 3), (np.float64, 9), (np.int32, 3), (np.uint64, 3), (np.uint64, 3),
+                                    np.float64],
+                        "offsets": [_lib.GridSpec.origin.offset, _lib.GridSpec.basv.offset, _lib.GridSpec.npts.offset,
+                                    _lib.GridSpec.pts.offset, _lib.GridSpec.wgt.offset, _lib.GridSpec.radius.offset],
+                        "itemsize": C.sizeof(_lib.GridSpec)})
 
 try:  # torch is optional: used only to accept device tensors
     import torch
@@ -250,26 +259,26 @@ class Gimic:
         """Many planes (origin, basv, axes, radius) in one device pass, e.g. a
         bond-current profile scan; returns one dict per plane."""
         n = len(planes)
-        specs = (_lib.GridSpec * n)()
-        keep = []
-        for q, (origin, basv, axes, radius) in enumerate(planes):
-            g = specs[q]
-            basv = np.asarray(basv, dtype=np.float64)
-            for c in range(3):
-                g.origin[c] = float(origin[c])
-            for d in range(3):
-                for c in range(3):
-                    g.basv[3 * d + c] = float(basv[c, d])
-            for d in range(3):
-                x = np.ascontiguousarray(axes[d][0], dtype=np.float64)
-                w = np.ascontiguousarray(axes[d][1], dtype=np.float64)
-                keep += [x, w]
-                g.npts[d] = len(x)
-                g.pts[d] = _dptr(x)
-                g.wgt[d] = _dptr(w)
-            g.radius = float(radius)
+        # the gg_grid records are filled as one numpy structured array (a
+        # per-field ctypes loop cost about 25 us per plane); the axis
+        # arrays are concatenated, and the records point into that buffer
+        lens = np.array([[len(ax[0]) for ax in pl[2]] for pl in planes], dtype=np.int64).reshape(n, 3)
+        flat = np.concatenate([np.asarray(v, dtype=np.float64).reshape(-1)
+                               for pl in planes for ax in pl[2] for v in ax])
+        specs = np.zeros(n, dtype=_GRID_DTYPE)
+        specs["origin"] = np.asarray([pl[0] for pl in planes], dtype=np.float64).reshape(n, 3)
+        # basv[3 d + c] = basv[c, d]
+        specs["basv"] = np.asarray([pl[1] for pl in planes], dtype=np.float64).reshape(n, 3, 3).transpose(0, 2, 1).reshape(n, 9)
+        specs["npts"] = lens
+        specs["radius"] = np.asarray([pl[3] for pl in planes], dtype=np.float64)
+        # layout of flat: per plane, per axis d, the points then the weights
+        sizes = np.repeat(lens.reshape(-1), 2)
+        starts = np.concatenate([[0], np.cumsum(sizes)[:-1]]).reshape(n, 3, 2)
+        base = flat.ctypes.data
+        specs["pts"] = base + 8 * starts[:, :, 0]
+        specs["wgt"] = base + 8 * starts[:, :, 1]  # flat stays referenced until the call returns
         out = np.zeros((n, 7))
-        check(self._L.gg_plane_integrals(self._h, specs, n, _dptr(out), C.c_void_p(stream) if stream else None),
-              self._h)
-        return [{"current": tuple(o[0:3]), "modulus": tuple(o[3:6]), "acid": float(np.sqrt(max(o[6], 0.0))),
-                 "acid_sum": float(o[6])} for o in out]
+        check(self._L.gg_plane_integrals(self._h, specs.ctypes.data_as(C.POINTER(_lib.GridSpec)), n, _dptr(out),
+                                         C.c_void_p(stream) if stream else None), self._h)
+        return [{"current": tuple(o[0:3]), "modulus": tuple(o[3:6]), "acid": math.sqrt(max(o[6], 0.0)),
+                 "acid_sum": o[6]} for o in out.tolist()]
