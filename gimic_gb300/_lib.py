@@ -37,6 +37,9 @@ SIGNATURES = {
     "gimic_get_gauss_points": (None, [_dp, _dp, _ip, _ip, _dp, _dp]),
     "mkgausspoints": (None, [_dp, _dp, _ip, _ip, _dp, _dp]),
     "gg_ctx_create": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_double, C.POINTER(C.c_void_p)]),
+    "gg_ctx_create_ex": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_double, C.c_int,
+                                   C.POINTER(C.c_void_p)]),
+    "gg_spherical_projection": (C.c_int, [C.c_int, _dp]),
     "gg_ctx_destroy": (C.c_int, [C.c_void_p]),
     "gg_last_error": (C.c_char_p, [C.c_void_p]),
     "gg_set_spin": (C.c_int, [C.c_void_p, C.c_char_p]),

@@ -64,15 +64,19 @@ class Gimic:
     magnetic field zero until set.
     """
 
-    def __init__(self, mol, xdens, uhf=False, screening=1e-6, precision="split16"):
+    def __init__(self, mol, xdens, uhf=False, screening=1e-6, precision="split16", spherical=False):
+        """``spherical``: the XDENS densities are over spherical functions
+        (the gimic.inp keyword Advanced.spherical); the basis values are
+        their projections from the Cartesian functions."""
         L = _lib.load()
         h = C.c_void_p()
-        rc = L.gg_ctx_create(str(mol).encode(), str(xdens).encode(), int(bool(uhf)),
-                             float(screening) if screening else -1.0, C.byref(h))
+        rc = L.gg_ctx_create_ex(str(mol).encode(), str(xdens).encode(), int(bool(uhf)),
+                                float(screening) if screening else -1.0, int(bool(spherical)), C.byref(h))
         check(rc, None)
         self._h = h
         self._L = L
         self.uhf = bool(uhf)
+        self.spherical = bool(spherical)
         nbf, nat, nsh, tm = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         L.gg_basis_info(h, C.byref(nbf), C.byref(nat), C.byref(nsh), C.byref(tm))
         self.nbf, self.natoms, self.nshells, self.turbomole = nbf.value, nat.value, nsh.value, bool(tm.value)

@@ -902,7 +902,8 @@ struct gg_ctx {
 
 extern "C" {
 
-int gg_ctx_create(const char* molfile, const char* xdens, int uhf, double screening, gg_ctx** out) {
+int gg_ctx_create_ex(const char* molfile, const char* xdens, int uhf, double screening, int spherical,
+                     gg_ctx** out) {
   if (!out) return GG_EINVAL;
   *out = nullptr;
   if (!molfile || !xdens) {
@@ -915,7 +916,9 @@ int gg_ctx_create(const char* molfile, const char* xdens, int uhf, double screen
   c->uhf = uhf != 0;
   c->screening = screening;
   std::string e = gg::read_intgrl(molfile, screening, &c->basis);
-  if (e.empty()) e = gg::read_xdens(xdens, c->basis, c->uhf, &c->dens);
+  if (e.empty())
+    e = spherical ? gg::read_xdens_spherical(xdens, c->basis, c->uhf, &c->dens)
+                  : gg::read_xdens(xdens, c->basis, c->uhf, &c->dens);
   if (!e.empty()) {
     g_create_error = e;
     delete c;
@@ -926,6 +929,10 @@ int gg_ctx_create(const char* molfile, const char* xdens, int uhf, double screen
   cudaGetLastError();
   *out = c;
   return GG_OK;
+}
+
+int gg_ctx_create(const char* molfile, const char* xdens, int uhf, double screening, gg_ctx** out) {
+  return gg_ctx_create_ex(molfile, xdens, uhf, screening, 0, out);
 }
 
 int gg_ctx_destroy(gg_ctx* ctx) {
@@ -1268,6 +1275,13 @@ int gg_gauss_data(double a, double b, int order, int npts, int type, double* pts
 }
 
 double gg_au2si(double au) { return gg::au2si(au); }
+
+int gg_spherical_projection(int l, double* out) {
+  if (l < 0 || l > gg::kMaxL || !out) return GG_EINVAL;
+  const std::vector<double> op = gg::spherical_projection(l);
+  std::copy(op.begin(), op.end(), out);
+  return GG_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Reference-compatible interface (src/libgimic/gimic_interface.f90:26-163)

@@ -277,6 +277,147 @@ std::string read_xdens(const std::string& path, const Basis& basis, bool uhf, De
 }
 
 // ---------------------------------------------------------------------------
+// Spherical basis (Advanced.spherical, src/fgimic/gimic.F90:85-87).  The
+// reference evaluates Cartesian functions and projects them per point,
+// sbf = po . bf (src/libgimic/bfeval.f90:116-117, dfdr :330-333), with po
+// block diagonal per shell (cao2sao.f90:64-101).  Every output is a bilinear
+// form in the basis values and their derivatives, and the GIAO factors
+// depend only on the function's atom, which po never mixes, so
+//   sbf^T M sbf' = bf^T (po^T M po) bf'
+// exactly: the densities are projected once to the Cartesian basis and the
+// evaluation stays Cartesian.
+// ---------------------------------------------------------------------------
+namespace {
+long factorial(int n) {
+  long m = 1;
+  for (int i = 2; i <= n; ++i) m *= i;
+  return m;
+}
+long binomial(int a, int b) { return factorial(a) / (factorial(b) * factorial(a - b)); }
+
+// integer-rescaled row, as cao2sao.f90:205-235 (renorm): divide by the
+// smallest magnitude, then multiply by the largest reciprocal needed to
+// clear the fractions
+void integer_row(std::vector<double>& row) {
+  double amin = 1e10;
+  for (double v : row)
+    if (std::fabs(v) > 0.0) amin = std::min(amin, std::fabs(v));
+  for (double& v : row) v /= amin;
+  double mult = 1.0;
+  for (double v : row) {
+    double a = std::fabs(v);
+    if (!(a > 0.0)) continue;
+    double f = std::fmod(a, 1.0);
+    if (f > 1e-10) {
+      a = 1.0 / f;
+      while (std::fmod(a, 1.0) > 1e-10) {
+        f = std::fmod(a, 1.0);
+        if (f > 1e-10) a /= f;
+      }
+      mult = std::max(mult, a);
+    }
+  }
+  for (double& v : row) v *= mult;
+}
+}  // namespace
+
+std::vector<double> spherical_projection(int l) {
+  // rows m = -l..l over the shell's Cartesian components (standard order):
+  // the solid-harmonic expansion of cao2sao.f90:153-201 (clmtuv, mkc2sop),
+  // each (t, u, v) term assigned to its component x^i y^j z^k
+  const int nc = (l + 1) * (l + 2) / 2;
+  std::vector<double> op(static_cast<size_t>(2 * l + 1) * nc, 0.0);
+  for (int m = -l; m <= l; ++m) {
+    std::vector<double> row(nc, 0.0);
+    const int am = std::abs(m);
+    const int half = m < 0 ? 1 : 0;  // v runs over half-integers for m < 0
+    for (int t = 0; t <= (l - am) / 2; ++t)
+      for (int u = 0; u <= t; ++u)
+        for (int v = 0; 2 * v + half <= am; ++v) {
+          const int two_v = 2 * v + half;  // 2 (v + v_m)
+          const int i = 2 * t + am - (2 * u + two_v), j = 2 * u + two_v, k = l - 2 * t - am;
+          double q = std::ldexp(1.0, -2 * t) *
+                     static_cast<double>(binomial(l, t) * binomial(l - t, am + t) * binomial(t, u) * binomial(am, two_v));
+          if ((t + v) & 1) q = -q;
+          for (int c = 0; c < nc; ++c) {
+            int e[3];
+            component_exponents(l, c, false, e);
+            if (e[0] == i && e[1] == j && e[2] == k) row[c] = q;
+          }
+        }
+    integer_row(row);
+    std::copy(row.begin(), row.end(), op.begin() + static_cast<size_t>(m + l) * nc);
+  }
+  return op;
+}
+
+int spherical_count(const Basis& b) {
+  int n = 0;
+  for (const Shell& s : b.shells) n += 2 * s.l + 1;
+  return n;
+}
+
+std::string read_xdens_spherical(const std::string& path, const Basis& basis, bool uhf, Density* out) {
+  if (basis.turbomole) return "spherical basis with the TURBOMOLE component order is not supported";
+  const int ns = spherical_count(basis), nc = basis.nbf;
+  // the file holds ns x ns blocks: read them through a basis-sized stand-in
+  Basis sb;
+  sb.nbf = ns;
+  Density ds;
+  std::string e = read_xdens(path, sb, uhf, &ds);
+  if (!e.empty()) return e;
+  // per Cartesian function: the spherical rows of its shell and their weights
+  std::vector<int> srow0(basis.shells.size());
+  for (size_t k = 0, r = 0; k < basis.shells.size(); ++k) {
+    srow0[k] = static_cast<int>(r);
+    r += 2 * basis.shells[k].l + 1;
+  }
+  std::vector<std::vector<double>> ops(kMaxL + 1);
+  for (int l = 0; l <= kMaxL; ++l) ops[l] = spherical_projection(l);
+  auto weight = [&](int s_row, int mu) -> double {  // po(s_row, mu), zero off the shell
+    const int k = basis.func_shell[mu];
+    const Shell& sh = basis.shells[k];
+    const int ls = s_row - srow0[k];
+    if (ls < 0 || ls > 2 * sh.l) return 0.0;
+    return ops[sh.l][static_cast<size_t>(ls) * sh.ncomp + basis.func_comp[mu]];
+  };
+  Density d;
+  d.nbf = nc;
+  d.uhf = uhf;
+  const size_t nn = static_cast<size_t>(nc) * nc, ss = static_cast<size_t>(ns) * ns;
+  d.a.assign(4 * nn, 0.0);
+  if (uhf) d.b.assign(4 * nn, 0.0);
+  std::vector<double> x(static_cast<size_t>(ns) * nc);  // M po, column-major ns x nc
+  for (int spin = 0; spin < (uhf ? 2 : 1); ++spin) {
+    const std::vector<double>& src = spin == 0 ? ds.a : ds.b;
+    std::vector<double>& dst = spin == 0 ? d.a : d.b;
+    for (int blk = 0; blk < 4; ++blk) {
+      const double* m = src.data() + blk * ss;
+      double* o = dst.data() + blk * nn;
+      for (int nu = 0; nu < nc; ++nu) {
+        const int k = basis.func_shell[nu];
+        const int r0 = srow0[k], nr = 2 * basis.shells[k].l + 1;
+        for (int s = 0; s < ns; ++s) {
+          double acc = 0.0;
+          for (int t = r0; t < r0 + nr; ++t) acc += m[s + static_cast<size_t>(t) * ns] * weight(t, nu);
+          x[s + static_cast<size_t>(nu) * ns] = acc;
+        }
+      }
+      for (int nu = 0; nu < nc; ++nu)
+        for (int mu = 0; mu < nc; ++mu) {
+          const int k = basis.func_shell[mu];
+          const int r0 = srow0[k], nr = 2 * basis.shells[k].l + 1;
+          double acc = 0.0;
+          for (int s = r0; s < r0 + nr; ++s) acc += weight(s, mu) * x[s + static_cast<size_t>(nu) * ns];
+          o[mu + static_cast<size_t>(nu) * nc] = acc;
+        }
+    }
+  }
+  *out = std::move(d);
+  return "";
+}
+
+// ---------------------------------------------------------------------------
 // Quadrature, src/libgimic/gaussint.f90:21-112 (gaussl, lobattomy) and
 // :144-222 (Legendre recurrences).  Newton tolerance 3e-12, at most 10 steps.
 // ---------------------------------------------------------------------------

@@ -66,6 +66,16 @@ struct Density {
 // (reorder.f90:54-96, dens.f90:210-234).
 std::string read_xdens(const std::string& path, const Basis& basis, bool uhf, Density* out);
 
+// Spherical basis: rows m = -l..l of the integer-rescaled projection of a
+// shell's Cartesian components (standard order) onto real solid harmonics,
+// (2l+1) x ncomp row-major (src/libgimic/cao2sao.f90:153-235).
+std::vector<double> spherical_projection(int l);
+int spherical_count(const Basis& b);
+// XDENS over the spherical functions (2l+1 per shell), projected to the
+// Cartesian basis: M_cart = po^T M_sph po per block.  Standard component
+// order only.
+std::string read_xdens_spherical(const std::string& path, const Basis& basis, bool uhf, Density* out);
+
 // Shell order for the screened split path.  Tile screening skips the
 // 64-function K blocks and 32-function column chunks in which no shell
 // reaches a tile, so the work falls when the shells that are in range of the

@@ -55,15 +55,13 @@ class Driver:
         self.workdir = workdir or os.path.dirname(os.path.abspath(inp_path))
         self.kw = inp.read(inp_path)
         kw = self.kw
-        if kw.get("Advanced.spherical"):
-            raise inp.InputError("Advanced.spherical=on is not supported: set spherical=off "
-                                 "(Cartesian basis functions, as in every reference test)")
         if not kw.get("Advanced.diamag") and not kw.get("Advanced.paramag"):
             raise inp.InputError("PLEASE SEEK PROFESSIONAL HELP, ASAP!  (diamag and paramag both off)")
         self.uhf = bool(kw.get("openshell"))
         path = lambda k: os.path.join(self.workdir, kw.get(k))
         thr = kw.get("Advanced.screening_thrs") if kw.get("Advanced.screening") else -1.0
-        self.g = api.Gimic(path("basis"), path("xdens"), uhf=self.uhf, screening=thr, precision=precision)
+        self.g = api.Gimic(path("basis"), path("xdens"), uhf=self.uhf, screening=thr, precision=precision,
+                           spherical=bool(kw.get("Advanced.spherical")))
         self.g.set_flags(kw.get("Advanced.GIAO"), kw.get("Advanced.diamag"), kw.get("Advanced.paramag"))
         self.atoms = self.g.atoms()[0]
         self.grid = ggrid.new_grid(kw, self.atoms, workdir=self.workdir)

@@ -53,6 +53,11 @@ class Molecule:
     def nbf(self):
         return sum(sum(ncomp(l) for l, _, _ in self.basis[s]) for s in self.symbols)
 
+    @property
+    def nsph(self):
+        """Functions of the spherical basis (2l + 1 per shell)."""
+        return sum(sum(2 * l + 1 for l, _, _ in self.basis[s]) for s in self.symbols)
+
     def function_atoms(self):
         out = []
         for a, s in enumerate(self.symbols):
@@ -288,12 +293,15 @@ def make_batch_molecule(outdir, index, seed=77):
     return mol_path, xd_path, mol
 
 
-def make_workload(name, outdir, seed=2024, uhf=False):
+def make_workload(name, outdir, seed=2024, uhf=False, spherical=False):
     """Write MOL and XDENS for a named workload; returns (mol_path, xdens_path,
-    Molecule).  Files are reused when already present for the same seed."""
+    Molecule).  Files are reused when already present for the same seed.
+    With ``spherical`` the densities are over the spherical functions (2l + 1
+    per shell, as a producer run with a spherical basis writes them); the MOL
+    file is the same."""
     geo, with_f, nocc = WORKLOADS[name]
     os.makedirs(outdir, exist_ok=True)
-    tag = "%s_s%d%s" % (name, seed, "_uhf" if uhf else "")
+    tag = "%s_s%d%s%s" % (name, seed, "_uhf" if uhf else "", "_sph" if spherical else "")
     mol_path = os.path.join(outdir, tag + ".mol")
     xd_path = os.path.join(outdir, tag + ".xdens")
     rng = np.random.default_rng(seed)
@@ -301,7 +309,7 @@ def make_workload(name, outdir, seed=2024, uhf=False):
     mol = Molecule(sym, xyz, random_basis(rng, with_f))
     if os.path.exists(mol_path) and os.path.exists(xd_path):
         return mol_path, xd_path, mol  # the MOL file is written last
-    n = mol.nbf
+    n = mol.nsph if spherical else mol.nbf
     blocks = []
     for _ in range(2 if uhf else 1):
         d, pert = random_densities(rng, n, nocc if not uhf else max(1, nocc // 2))

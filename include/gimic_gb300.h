@@ -67,6 +67,23 @@ typedef struct gg_ctx gg_ctx;
  * dens.f90:56-127); screening <= 0 disables screening.  Uses the current CUDA
  * device.  On failure *out is NULL and gg_last_error(NULL) has the reason. */
 int gg_ctx_create(const char *molfile, const char *xdens, int uhf, double screening, gg_ctx **out);
+/* As gg_ctx_create, with the basis choice of the gimic.inp keyword
+ * Advanced.spherical (src/fgimic/gimic.F90:85-87, src/gimic.in:79): with
+ * spherical != 0 the XDENS blocks are over the spherical functions (2l+1 per
+ * shell, m = -l..l, the integer-rescaled solid harmonics of
+ * src/libgimic/cao2sao.f90:153-235) and the basis values are their
+ * projections (bfeval.f90:116-117).  The projection is folded into the
+ * densities once (D_cart = po^T D_sph po), so evaluation costs the same as
+ * for the Cartesian basis.  Standard (non-TURBOMOLE) component order only;
+ * returns GG_EIO with a message otherwise. */
+int gg_ctx_create_ex(const char *molfile, const char *xdens, int uhf, double screening, int spherical,
+                     gg_ctx **out);
+/* The projection of one shell of angular momentum l (0..5) used by
+ * gg_ctx_create_ex: (2l+1) x (l+1)(l+2)/2 row-major, rows m = -l..l, columns
+ * the standard Cartesian component order (the operator of mkc2sop and
+ * renorm, src/libgimic/cao2sao.f90:173-235; for l >= 4 the reference's
+ * term-by-term assignment is kept).  No device work. */
+int gg_spherical_projection(int l, double *out);
 int gg_ctx_destroy(gg_ctx *ctx);
 const char *gg_last_error(const gg_ctx *ctx);
 

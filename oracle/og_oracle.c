@@ -74,6 +74,12 @@ typedef struct {
     int natoms, ncgto, ngto, turbomole, uhf;
     og_atom *atoms;
     int *fatom;      /* atom of each function */
+    /* spherical basis (Advanced.spherical): nfun = nsph functions of 2l+1
+     * components per shell; c2s[s * ncgto + c] projects Cartesian component
+     * c onto spherical function s (cao2sao_t%po, cao2sao.f90:64-101) */
+    int spherical, nfun;
+    double *c2s;
+    int *fatom_s;
     double *da, *db; /* [4][n*n] column-major: D, dD/dBx, dD/dBy, dD/dBz */
     int giao, dia, para;
     char err[512];
@@ -345,7 +351,7 @@ static void turbo_sv(const og_ctx *x, int *sv) {
 
 /* src/libgimic/dens.f90:56-135 (read_dens, read_array), :210-234 (reorder_dens) */
 static int read_dens(og_ctx *x, const char *fname) {
-    int n = x->ncgto;
+    int n = x->nfun;
     size_t nn = (size_t)n * n;
     og_rd r = {0};
     r.f = fopen(fname, "r");
@@ -452,10 +458,13 @@ static void basis_point(const og_ctx *x, const double r[3], double *bf, double *
  * ------------------------------------------------------------------------- */
 typedef struct {
     double *bf, *dr, *db, *d2, *denbf, *dendb, *pdbf;
+    double *bfc, *drc; /* Cartesian values before the spherical projection */
 } og_work;
 
-static og_work work_new(int n) {
+static og_work work_new(int n, int ncart) {
     og_work w;
+    w.bfc = calloc((size_t)ncart, sizeof(double));
+    w.drc = calloc(3 * (size_t)ncart, sizeof(double));
     w.bf = calloc((size_t)n, sizeof(double));
     w.dr = calloc(3 * (size_t)n, sizeof(double));
     w.db = calloc(3 * (size_t)n, sizeof(double));
@@ -466,6 +475,8 @@ static og_work work_new(int n) {
     return w;
 }
 static void work_free(og_work *w) {
+    free(w->bfc);
+    free(w->drc);
     free(w->bf);
     free(w->dr);
     free(w->db);
@@ -490,15 +501,33 @@ static double dot(int n, const double *a, const double *b) {
 }
 
 static void jtensor_spin(const og_ctx *x, og_work *w, const double r[3], int spin, double ct[9], double *rho_out) {
-    int n = x->ncgto;
+    int n = x->nfun;
     size_t nn = (size_t)n * n;
     const double *dens = spin == 1 ? x->db : x->da;
     double rho[3] = {0.5 * r[0], 0.5 * r[1], 0.5 * r[2]};
-    basis_point(x, r, w->bf, w->dr);
+    const int *fatom = x->spherical ? x->fatom_s : x->fatom;
+    if (x->spherical) {
+        /* bfeval.f90:116-117 and dfdr, :330-333: sbf = matmul(po, bf) */
+        int nc = x->ncgto;
+        basis_point(x, r, w->bfc, w->drc);
+        for (int s = 0; s < n; s++) {
+            const double *row = x->c2s + (size_t)s * nc;
+            double v = 0.0, g[3] = {0.0, 0.0, 0.0};
+            for (int c = 0; c < nc; c++) {
+                if (row[c] == 0.0) continue;
+                v += row[c] * w->bfc[c];
+                for (int ax = 0; ax < 3; ax++) g[ax] += row[c] * w->drc[c + (size_t)ax * nc];
+            }
+            w->bf[s] = v;
+            for (int ax = 0; ax < 3; ax++) w->dr[s + (size_t)ax * n] = g[ax];
+        }
+    } else {
+        basis_point(x, r, w->bf, w->dr);
+    }
     if (x->giao) {
         /* mkdbop + dfdb + d2fdrdb */
         for (int mu = 0; mu < n; mu++) {
-            const double *R = x->atoms[x->fatom[mu]].coord;
+            const double *R = x->atoms[fatom[mu]].coord;
             double dbop[3] = {r[1] * R[2] - r[2] * R[1], r[2] * R[0] - r[0] * R[2], r[0] * R[1] - r[1] * R[0]};
             double bfv = w->bf[mu];
             double dx = w->dr[mu], dy = w->dr[mu + n], dz = w->dr[mu + 2 * (size_t)n];
@@ -716,6 +745,107 @@ int og_gauss_data(double a, double b, int ngp, int npts, int quadr, double *pts,
 }
 
 /* ---------------------------------------------------------------------------
+ * Cartesian -> spherical projection, src/libgimic/cao2sao.f90: mkc2sop
+ * (:173-201), clmtuv (:153-170), renorm (:205-235), assembled per shell by
+ * new_c2sop (:64-101).  Rows run over m = -l..l (the sphmap reordering is
+ * commented out in the reference, :187).  As in the reference each (t, u, v)
+ * term is ASSIGNED to its Cartesian component; for l <= 3 no two terms share
+ * a component, so the rows are the exact real solid harmonics, rescaled by
+ * renorm to integer coefficients (d: xy, yz, 2zz - xx - yy, xz, xx - yy).
+ * The normalisation nslm drops out in renorm and is not restated.
+ * ------------------------------------------------------------------------- */
+static long og_fact(int n) {
+    long m = 1;
+    for (int i = 2; i <= n; i++) m *= i;
+    return m;
+}
+static long og_binom(int a, int b) { return og_fact(a) / (og_fact(b) * og_fact(a - b)); }
+
+static int gt_index(int l, int i, int j, int k) {
+    for (int c = 0; c < (l + 1) * (l + 2) / 2; c++)
+        if (GT_STD[l][c][0] == i && GT_STD[l][c][1] == j && GT_STD[l][c][2] == k) return c;
+    return -1;
+}
+
+static void renorm_row(double *row, int nc) {
+    double amin = 1e10;
+    for (int j = 0; j < nc; j++) {
+        double ava = fabs(row[j]);
+        if (ava > 0.0 && ava < amin) amin = ava;
+    }
+    for (int j = 0; j < nc; j++) row[j] /= amin;
+    double sim = 1.0;
+    for (int j = 0; j < nc; j++) {
+        double ava = fabs(row[j]);
+        if (!(ava > 0.0)) continue;
+        double avb = fmod(ava, 1.0);
+        if (avb > 1e-10) {
+            ava = 1.0 / avb;
+            while (fmod(ava, 1.0) > 1e-10) {
+                avb = fmod(ava, 1.0);
+                if (avb > 1e-10) ava = ava / avb;
+            }
+            if (ava > sim) sim = ava;
+        }
+    }
+    for (int j = 0; j < nc; j++) row[j] *= sim;
+}
+
+/* xop[(2l+1) x ncart] row-major */
+static void mkc2sop(int l, double *xop) {
+    int nc = (l + 1) * (l + 2) / 2;
+    memset(xop, 0, (size_t)(2 * l + 1) * nc * sizeof(double));
+    for (int m = -l; m <= l; m++) {
+        double *row = xop + (size_t)(m + l) * nc;
+        int am = m < 0 ? -m : m;
+        double vm = m < 0 ? 0.5 : 0.0;
+        for (int t = 0; t <= (l - am) / 2; t++)
+            for (int u = 0; u <= t; u++)
+                for (int v = 0; v <= (int)(am * 0.5 - vm); v++) {
+                    double vr = v + vm;
+                    int i = 2 * t + am - (int)(2.0 * (u + vr));
+                    int j = (int)(2.0 * (u + vr));
+                    int k = l - 2 * t - am;
+                    double q = 1.0 / pow(4.0, t);
+                    if (fmod((double)t + vr - vm, 2.0) > 0.0) q = -q;
+                    q *= (double)(og_binom(l, t) * og_binom(l - t, am + t) * og_binom(t, u) * og_binom(am, (int)(2.0 * vr)));
+                    int n = gt_index(l, i, j, k);
+                    if (n >= 0) row[n] = q;
+                }
+        renorm_row(row, nc);
+    }
+}
+
+static int setup_spherical(og_ctx *x) {
+    if (x->turbomole) {
+        snprintf(x->err, sizeof x->err, "spherical basis with TURBOMOLE component order is not supported");
+        return -1;
+    }
+    int ns = 0;
+    for (int a = 0; a < x->natoms; a++)
+        for (int k = 0; k < x->atoms[a].nctr; k++) ns += 2 * x->atoms[a].ctr[k].l + 1;
+    x->nfun = ns;
+    x->c2s = calloc((size_t)ns * x->ncgto, sizeof(double));
+    x->fatom_s = malloc((size_t)ns * sizeof(int));
+    double xop[11 * 21];
+    int srow = 0, ccol = 0;
+    for (int a = 0; a < x->natoms; a++) {
+        const og_atom *at = &x->atoms[a];
+        for (int k = 0; k < at->nctr; k++) {
+            int l = at->ctr[k].l, nc = (l + 1) * (l + 2) / 2;
+            mkc2sop(l, xop);
+            for (int s = 0; s < 2 * l + 1; s++) {
+                for (int c = 0; c < nc; c++) x->c2s[(size_t)(srow + s) * x->ncgto + ccol + at->ctr[k].pos + c] = xop[s * nc + c];
+                x->fatom_s[srow + s] = a;
+            }
+            srow += 2 * l + 1;
+        }
+        ccol += at->ncgto;
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------------------------
  * Public API (ctypes)
  * ------------------------------------------------------------------------- */
 static void og_free_atoms(og_ctx *x) {
@@ -737,6 +867,8 @@ void og_free(og_ctx *x) {
     if (!x) return;
     og_free_atoms(x);
     free(x->fatom);
+    free(x->fatom_s);
+    free(x->c2s);
     free(x->da);
     free(x->db);
     free(x);
@@ -744,11 +876,15 @@ void og_free(og_ctx *x) {
 
 /* Load MOL (+ XDENS unless xdens is NULL).  screen_thrs <= 0 disables
  * screening (basis%thrs = 1e10), as in basis.f90:69-73. */
-og_ctx *og_load(const char *mol, const char *xdens, int uhf, double screen_thrs, char *err, int errlen) {
+og_ctx *og_load_sph(const char *mol, const char *xdens, int uhf, double screen_thrs, int spherical, char *err,
+                    int errlen) {
     og_ctx *x = calloc(1, sizeof(og_ctx));
     x->uhf = uhf != 0;
     x->giao = x->dia = x->para = 1;
     int rc = read_intgrl(x, mol, screen_thrs);
+    x->nfun = x->ncgto;
+    x->spherical = spherical != 0;
+    if (rc == 0 && x->spherical) rc = setup_spherical(x);
     if (rc == 0 && xdens) rc = read_dens(x, xdens);
     if (rc != 0) {
         if (err && errlen > 0) snprintf(err, (size_t)errlen, "%s", x->err);
@@ -758,7 +894,19 @@ og_ctx *og_load(const char *mol, const char *xdens, int uhf, double screen_thrs,
     return x;
 }
 
+og_ctx *og_load(const char *mol, const char *xdens, int uhf, double screen_thrs, char *err, int errlen) {
+    return og_load_sph(mol, xdens, uhf, screen_thrs, 0, err, errlen);
+}
+
 int og_ncgto(const og_ctx *x) { return x->ncgto; }
+/* functions the densities are given in: spherical or Cartesian */
+int og_nfun(const og_ctx *x) { return x->nfun; }
+/* the projection, nfun x ncgto row-major (spherical contexts only) */
+int og_c2s(const og_ctx *x, double *out) {
+    if (!x->spherical) return -1;
+    memcpy(out, x->c2s, (size_t)x->nfun * x->ncgto * sizeof(double));
+    return 0;
+}
 int og_ngto(const og_ctx *x) { return x->ngto; }
 int og_natoms(const og_ctx *x) { return x->natoms; }
 int og_is_turbomole(const og_ctx *x) { return x->turbomole; }
@@ -775,7 +923,7 @@ void og_set_flags(og_ctx *x, int giao, int dia, int para) {
 int og_get_dens(const og_ctx *x, int spin, int b, double *out) {
     const double *d = spin == 1 ? x->db : x->da;
     if (!d) return -1;
-    size_t nn = (size_t)x->ncgto * x->ncgto;
+    size_t nn = (size_t)x->nfun * x->nfun;
     memcpy(out, d + (size_t)b * nn, nn * sizeof(double));
     return 0;
 }
@@ -820,7 +968,7 @@ int og_jtensor_batch(const og_ctx *x, const char *spin, long npts, const double 
 #pragma omp parallel num_threads(nthreads) reduction(| : err)
 #endif
     {
-        og_work w = work_new(x->ncgto);
+        og_work w = work_new(x->nfun, x->ncgto);
 #ifdef _OPENMP
 #pragma omp for schedule(static)
 #endif
@@ -889,7 +1037,7 @@ int og_integrate(const og_ctx *x, const char *spin, const og_grid *g, const doub
 #pragma omp parallel num_threads(nthreads)
 #endif
         {
-            og_work w = work_new(x->ncgto);
+            og_work w = work_new(x->nfun, x->ncgto);
 #ifdef _OPENMP
 #pragma omp for schedule(static)
 #endif

@@ -37,8 +37,12 @@ def lib():
         L = C.CDLL(_LIB_PATH)
         L.og_load.restype = C.c_void_p
         L.og_load.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_double, C.c_char_p, C.c_int]
+        L.og_load_sph.restype = C.c_void_p
+        L.og_load_sph.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_double, C.c_int, C.c_char_p, C.c_int]
+        L.og_c2s.argtypes = [C.c_void_p, _dp]
+        L.og_c2s.restype = C.c_int
         L.og_free.argtypes = [C.c_void_p]
-        for f in ("og_ncgto", "og_ngto", "og_natoms", "og_is_turbomole", "og_nctr_total"):
+        for f in ("og_ncgto", "og_nfun", "og_ngto", "og_natoms", "og_is_turbomole", "og_nctr_total"):
             getattr(L, f).argtypes = [C.c_void_p]
             getattr(L, f).restype = C.c_int
         L.og_atom_info.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
@@ -84,17 +88,20 @@ def gauss_data(a, b, order, npts, quadrature="gauss"):
 class Oracle:
     """One molecule + density, evaluated on the CPU in FP64."""
 
-    def __init__(self, mol, xdens=None, uhf=False, screening=1e-8, giao=True, dia=True, para=True):
+    def __init__(self, mol, xdens=None, uhf=False, screening=1e-8, giao=True, dia=True, para=True,
+                 spherical=False):
         L = lib()
         err = C.create_string_buffer(512)
-        h = L.og_load(mol.encode(), xdens.encode() if xdens else None, int(bool(uhf)),
-                      float(screening) if screening else -1.0, err, 512)
+        h = L.og_load_sph(mol.encode(), xdens.encode() if xdens else None, int(bool(uhf)),
+                          float(screening) if screening else -1.0, int(bool(spherical)), err, 512)
         if not h:
             raise RuntimeError(err.value.decode())
         self._h = C.c_void_p(h)
         self.uhf = bool(uhf)
         L.og_set_flags(self._h, int(giao), int(dia), int(para))
-        self.nbf = L.og_ncgto(self._h)
+        self.nbf = L.og_nfun(self._h)        # functions of the densities (spherical or Cartesian)
+        self.ncart = L.og_ncgto(self._h)     # Cartesian functions
+        self.spherical = bool(spherical)
         self.natoms = L.og_natoms(self._h)
         self.turbomole = bool(L.og_is_turbomole(self._h))
 
@@ -120,6 +127,13 @@ class Oracle:
             raise ValueError("no such density block")
         return out.reshape(self.nbf, self.nbf, order="F")
 
+    def c2s(self):
+        """The Cartesian -> spherical projection (nfun x ncart) of a spherical context."""
+        out = np.zeros(self.nbf * self.ncart)
+        if lib().og_c2s(self._h, _p(out)) != 0:
+            raise ValueError("not a spherical context")
+        return out.reshape(self.nbf, self.ncart)
+
     def shells(self, maxprim=16):
         L = lib()
         ns = L.og_nctr_total(self._h)
@@ -133,10 +147,10 @@ class Oracle:
 
     def basis(self, r):
         r = np.ascontiguousarray(r, dtype=np.float64)
-        bf = np.zeros(self.nbf)
-        dr = np.zeros(3 * self.nbf)
+        bf = np.zeros(self.ncart)
+        dr = np.zeros(3 * self.ncart)
         lib().og_basis_eval(self._h, _p(r), _p(bf), _p(dr))
-        return bf, dr.reshape(3, self.nbf)
+        return bf, dr.reshape(3, self.ncart)
 
     def jtensor(self, points, spin="total", nthreads=0, with_rho=False):
         """ctensor at points (N,3) -> (N,9) column-major tensors (+ rho)."""
