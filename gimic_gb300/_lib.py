@@ -59,6 +59,8 @@ SIGNATURES = {
     "gg_jvector_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "gg_plane_integral": (C.c_int, [C.c_void_p, C.POINTER(GridSpec), _dp, C.c_void_p]),
     "gg_plane_integrals": (C.c_int, [C.c_void_p, C.POINTER(GridSpec), C.c_int, _dp, C.c_void_p]),
+    "gg_plane_integrals_enqueue": (C.c_int, [C.c_void_p, C.POINTER(GridSpec), C.c_int, C.c_void_p]),
+    "gg_plane_integrals_collect": (C.c_int, [C.c_void_p, _dp, _dp]),
     "gg_gauss_data": (C.c_int, [C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "gg_au2si": (C.c_double, [C.c_double]),
     "gg_profile": (C.c_int, [C.c_void_p, C.c_int]),

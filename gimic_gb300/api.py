@@ -262,27 +262,72 @@ class Gimic:
     def plane_integrals(self, planes, stream=None):
         """Many planes (origin, basv, axes, radius) in one device pass, e.g. a
         bond-current profile scan; returns one dict per plane."""
+        specs, flat = _grid_records(planes)
         n = len(planes)
-        # the gg_grid records are filled as one numpy structured array (a
-        # per-field ctypes loop cost about 25 us per plane); the axis
-        # arrays are concatenated, and the records point into that buffer
-        lens = np.array([[len(ax[0]) for ax in pl[2]] for pl in planes], dtype=np.int64).reshape(n, 3)
-        flat = np.concatenate([np.asarray(v, dtype=np.float64).reshape(-1)
-                               for pl in planes for ax in pl[2] for v in ax])
-        specs = np.zeros(n, dtype=_GRID_DTYPE)
-        specs["origin"] = np.asarray([pl[0] for pl in planes], dtype=np.float64).reshape(n, 3)
-        # basv[3 d + c] = basv[c, d]
-        specs["basv"] = np.asarray([pl[1] for pl in planes], dtype=np.float64).reshape(n, 3, 3).transpose(0, 2, 1).reshape(n, 9)
-        specs["npts"] = lens
-        specs["radius"] = np.asarray([pl[3] for pl in planes], dtype=np.float64)
-        # layout of flat: per plane, per axis d, the points then the weights
-        sizes = np.repeat(lens.reshape(-1), 2)
-        starts = np.concatenate([[0], np.cumsum(sizes)[:-1]]).reshape(n, 3, 2)
-        base = flat.ctypes.data
-        specs["pts"] = base + 8 * starts[:, :, 0]
-        specs["wgt"] = base + 8 * starts[:, :, 1]  # flat stays referenced until the call returns
         out = np.zeros((n, 7))
         check(self._L.gg_plane_integrals(self._h, specs.ctypes.data_as(C.POINTER(_lib.GridSpec)), n, _dptr(out),
                                          C.c_void_p(stream) if stream else None), self._h)
-        return [{"current": tuple(o[0:3]), "modulus": tuple(o[3:6]), "acid": math.sqrt(max(o[6], 0.0)),
-                 "acid_sum": o[6]} for o in out.tolist()]
+        return _plane_results(out)
+
+
+def _plane_results(out):
+    return [{"current": tuple(o[0:3]), "modulus": tuple(o[3:6]), "acid": math.sqrt(max(o[6], 0.0)),
+             "acid_sum": o[6]} for o in out.tolist()]
+
+
+def _grid_records(planes):
+    """gg_grid records of (origin, basv, axes, radius) planes, and the buffer
+    of axis points and weights they point into (keep it referenced until the
+    library call returns)."""
+    n = len(planes)
+    # the gg_grid records are filled as one numpy structured array (a
+    # per-field ctypes loop cost about 25 us per plane); the axis
+    # arrays are concatenated, and the records point into that buffer
+    lens = np.array([[len(ax[0]) for ax in pl[2]] for pl in planes], dtype=np.int64).reshape(n, 3)
+    flat = np.concatenate([np.asarray(v, dtype=np.float64).reshape(-1)
+                           for pl in planes for ax in pl[2] for v in ax])
+    specs = np.zeros(n, dtype=_GRID_DTYPE)
+    specs["origin"] = np.asarray([pl[0] for pl in planes], dtype=np.float64).reshape(n, 3)
+    # basv[3 d + c] = basv[c, d]
+    specs["basv"] = np.asarray([pl[1] for pl in planes], dtype=np.float64).reshape(n, 3, 3).transpose(0, 2, 1).reshape(n, 9)
+    specs["npts"] = lens
+    specs["radius"] = np.asarray([pl[3] for pl in planes], dtype=np.float64)
+    # layout of flat: per plane, per axis d, the points then the weights
+    sizes = np.repeat(lens.reshape(-1), 2)
+    starts = np.concatenate([[0], np.cumsum(sizes)[:-1]]).reshape(n, 3, 2)
+    base = flat.ctypes.data
+    specs["pts"] = base + 8 * starts[:, :, 0]
+    specs["wgt"] = base + 8 * starts[:, :, 1]
+    return specs, flat
+
+
+def plane_integrals_multi(jobs, stream=None, timings=False):
+    """Plane batches of many molecules, queued one after the other on one
+    stream and collected at the end (gg_plane_integrals_enqueue / _collect):
+    the host work of molecule i+1 overlaps the device work of molecule i.
+    jobs = [(Gimic, planes), ...] with distinct contexts.  Returns one list of
+    result dicts per molecule, and with ``timings`` also each molecule's
+    stream milliseconds."""
+    st = C.c_void_p(stream) if stream else None
+    queued = []
+    try:
+        for g, planes in jobs:
+            specs, flat = _grid_records(planes)
+            check(g._L.gg_plane_integrals_enqueue(g._h, specs.ctypes.data_as(C.POINTER(_lib.GridSpec)), len(planes),
+                                                  st), g._h)
+            queued.append((g, len(planes)))
+    finally:
+        # every queued pass is collected, also when a later one failed
+        res, ms, err = [], [], None
+        for g, n in queued:
+            out = np.zeros((n, 7))
+            t = C.c_double()
+            try:
+                check(g._L.gg_plane_integrals_collect(g._h, _dptr(out), C.byref(t)), g._h)
+            except Exception as e:  # keep collecting; report the first failure
+                err = err or e
+            res.append(_plane_results(out))
+            ms.append(t.value)
+    if err is not None:
+        raise err
+    return (res, ms) if timings else res

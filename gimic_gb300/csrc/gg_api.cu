@@ -158,6 +158,13 @@ struct gg_ctx {
   cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
   DevBuf phi, gx, gy, gz, lap, w64;
   DevBuf plane_rows, plane_out;
+  void* plane_host = nullptr;  // pinned staging of the plane uploads
+  size_t plane_host_bytes = 0;
+  // a queued plane pass (gg_plane_integrals_enqueue until _collect)
+  bool plane_pending = false;
+  int plane_n = 0;
+  const double* plane_dres = nullptr;
+  cudaEvent_t plane_ev[2] = {nullptr, nullptr};  // start and end of the queued pass
   int* d_err = nullptr;
 
   // optional per-kernel timing with CUDA events on the launching stream
@@ -216,6 +223,9 @@ struct gg_ctx {
     if (aux_stream) cudaStreamDestroy(aux_stream);
     if (copy_stream) cudaStreamDestroy(copy_stream);
     if (out_stream) cudaStreamDestroy(out_stream);
+    for (cudaEvent_t ev : plane_ev)
+      if (ev) cudaEventDestroy(ev);
+    if (plane_host) cudaFreeHost(plane_host);
     if (prof.d_blocks) cudaFree(prof.d_blocks);
     for (auto& e : prof.pool) {
       cudaEventDestroy(e.first);
@@ -744,6 +754,12 @@ struct gg_ctx {
   int check_device_error(cudaStream_t st) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "device execution");
+    return device_error_word();
+  }
+
+  // the error word and profile events of work known to be complete
+  int device_error_word() {
+    cudaError_t e;
     prof_collect();
     if (d_err) {
       int h = 0;
@@ -1124,9 +1140,11 @@ int gg_jvector_batch(gg_ctx* ctx, const double* pts, int64_t n, double* jv, void
   return GG_OK;
 }
 
-int gg_plane_integrals(gg_ctx* ctx, const gg_grid* grids, int nplanes, double* out, void* stream) {
-  if (!ctx || !grids || !out || nplanes <= 0) return GG_EINVAL;
-  std::lock_guard<std::mutex> g(ctx->mu);
+// Everything of a plane-integral pass up to and including the reduction,
+// queued on `st` without waiting: the nplanes x 7 sums are left in the
+// context's device scratch at *d_result.  The caller holds ctx->mu.
+static int plane_enqueue(gg_ctx* ctx, const gg_grid* grids, int nplanes, cudaStream_t st, const double** d_result) {
+  if (!grids || nplanes <= 0) return GG_EINVAL;
   int64_t npts = 0, nrows = 0, nw = 0;
   for (int q = 0; q < nplanes; ++q) {
     const gg_grid& gr = grids[q];
@@ -1179,27 +1197,40 @@ int gg_plane_integrals(gg_ctx* ctx, const gg_grid* grids, int nplanes, double* o
   }
   int rc = ctx->prepare();
   if (rc) return rc;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const size_t aux = 2 * hw.size() * sizeof(double) + desc.size() * sizeof(gg::PlaneDesc) +
-                     row_plane.size() * sizeof(int) + static_cast<size_t>(nrows) * 7 * sizeof(double) +
-                     static_cast<size_t>(nplanes) * 7 * sizeof(double) + 64;
+  // device layout: [descs | weights | axis points | row -> plane] uploaded in
+  // one copy from pinned staging, then [row partials | plane sums]
+  auto up8 = [](size_t x) { return (x + 7) & ~static_cast<size_t>(7); };
+  const size_t o_w = up8(desc.size() * sizeof(gg::PlaneDesc));
+  const size_t o_x = o_w + hw.size() * sizeof(double);
+  const size_t o_rp = o_x + hx.size() * sizeof(double);
+  const size_t upload = o_rp + row_plane.size() * sizeof(int);
+  const size_t o_row = up8(upload);
+  const size_t o_out = o_row + static_cast<size_t>(nrows) * 7 * sizeof(double);
+  const size_t aux = o_out + static_cast<size_t>(nplanes) * 7 * sizeof(double);
   cudaError_t e = ctx->pts.reserve(static_cast<size_t>(npts) * 3 * sizeof(double));
   if (e == cudaSuccess) e = ctx->jt.reserve(static_cast<size_t>(npts) * 9 * sizeof(double));
   if (e == cudaSuccess) e = ctx->plane_rows.reserve(aux);
+  if (e == cudaSuccess && ctx->plane_host_bytes < upload) {
+    if (ctx->plane_host) cudaFreeHost(ctx->plane_host);
+    ctx->plane_host = nullptr;
+    ctx->plane_host_bytes = 0;
+    e = cudaMallocHost(&ctx->plane_host, upload);
+    if (e == cudaSuccess) ctx->plane_host_bytes = upload;
+  }
   if (e != cudaSuccess) return ctx->cuda_fail(e, "plane scratch");
+  char* hb = static_cast<char*>(ctx->plane_host);
+  std::memcpy(hb, desc.data(), desc.size() * sizeof(gg::PlaneDesc));
+  std::memcpy(hb + o_w, hw.data(), hw.size() * sizeof(double));
+  std::memcpy(hb + o_x, hx.data(), hx.size() * sizeof(double));
+  std::memcpy(hb + o_rp, row_plane.data(), row_plane.size() * sizeof(int));
   char* ab = ctx->plane_rows.as<char>();
-  double* dw = reinterpret_cast<double*>(ab);
-  double* dx = dw + hw.size();
-  double* drow = dx + hx.size();
-  double* dout = drow + static_cast<size_t>(nrows) * 7;
-  gg::PlaneDesc* ddesc = reinterpret_cast<gg::PlaneDesc*>(dout + static_cast<size_t>(nplanes) * 7);
-  int* drp = reinterpret_cast<int*>(ddesc + nplanes);
-  e = cudaMemcpyAsync(dw, hw.data(), hw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, hx.data(), hx.size() * sizeof(double), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(ddesc, desc.data(), desc.size() * sizeof(gg::PlaneDesc), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(drp, row_plane.data(), row_plane.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+  gg::PlaneDesc* ddesc = reinterpret_cast<gg::PlaneDesc*>(ab);
+  double* dw = reinterpret_cast<double*>(ab + o_w);
+  double* dx = reinterpret_cast<double*>(ab + o_x);
+  int* drp = reinterpret_cast<int*>(ab + o_rp);
+  double* drow = reinterpret_cast<double*>(ab + o_row);
+  double* dout = reinterpret_cast<double*>(ab + o_out);
+  e = cudaMemcpyAsync(ab, hb, upload, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane axes");
   gg::launch_plane_points(dx, ddesc, drp, nrows, ctx->pts.as<double>(), st);
   ctx->launches += 1;
@@ -1219,9 +1250,71 @@ int gg_plane_integrals(gg_ctx* ctx, const gg_grid* grids, int nplanes, double* o
   ctx->launches += 2;
   e = cudaGetLastError();
   if (e != cudaSuccess) return ctx->cuda_fail(e, "plane reduction launch");
-  e = cudaMemcpyAsync(out, dout, static_cast<size_t>(nplanes) * 7 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  *d_result = dout;
+  return GG_OK;
+}
+
+int gg_plane_integrals(gg_ctx* ctx, const gg_grid* grids, int nplanes, double* out, void* stream) {
+  if (!ctx || !grids || !out || nplanes <= 0) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const double* dout = nullptr;
+  int rc = plane_enqueue(ctx, grids, nplanes, st, &dout);
+  if (rc) return rc;
+  cudaError_t e =
+      cudaMemcpyAsync(out, dout, static_cast<size_t>(nplanes) * 7 * sizeof(double), cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane result");
   return ctx->check_device_error(st);
+}
+
+int gg_plane_integrals_enqueue(gg_ctx* ctx, const gg_grid* grids, int nplanes, void* stream) {
+  if (!ctx || !grids || nplanes <= 0) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (ctx->plane_pending) return ctx->fail(GG_EINVAL, "a queued plane pass has not been collected");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSetDevice(ctx->device);
+  for (cudaEvent_t& ev : ctx->plane_ev)
+    if (!ev && e == cudaSuccess) e = cudaEventCreate(&ev);
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->plane_ev[0], st);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "plane pass events");
+  const double* dout = nullptr;
+  int rc = plane_enqueue(ctx, grids, nplanes, st, &dout);
+  if (rc) {
+    cudaStreamSynchronize(st);  // nothing of this context may still run when it is used again
+    return rc;
+  }
+  e = cudaEventRecord(ctx->plane_ev[1], st);
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(st);
+    return ctx->cuda_fail(e, "plane pass events");
+  }
+  ctx->plane_pending = true;
+  ctx->plane_n = nplanes;
+  ctx->plane_dres = dout;
+  return GG_OK;
+}
+
+int gg_plane_integrals_collect(gg_ctx* ctx, double* out, double* ms) {
+  if (!ctx || !out) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (!ctx->plane_pending) return ctx->fail(GG_EINVAL, "no queued plane pass to collect");
+  ctx->plane_pending = false;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaEventSynchronize(ctx->plane_ev[1]);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "device execution");
+  // the pass is complete: the error word and the sums can be read
+  int rc = ctx->device_error_word();
+  if (rc) return rc;
+  e = cudaMemcpy(out, ctx->plane_dres, static_cast<size_t>(ctx->plane_n) * 7 * sizeof(double),
+                 cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane result");
+  if (ms) {
+    float t = 0.f;
+    e = cudaEventElapsedTime(&t, ctx->plane_ev[0], ctx->plane_ev[1]);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "plane pass timing");
+    *ms = t;
+  }
+  return GG_OK;
 }
 
 int gg_plane_integral(gg_ctx* ctx, const gg_grid* grid, double out[7], void* stream) {

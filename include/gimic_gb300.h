@@ -174,6 +174,20 @@ int gg_plane_integral(gg_ctx *ctx, const gg_grid *grid, double out[7], void *str
  * plane): out is nplanes x 7 in the layout of gg_plane_integral. */
 int gg_plane_integrals(gg_ctx *ctx, const gg_grid *grids, int nplanes, double *out, void *stream);
 
+/* gg_plane_integrals in two halves, so that one host thread can queue many
+ * molecules' passes before waiting for any (the reference runs one gimic
+ * process per molecule and slice, jobscripts/src/current-profile-header:
+ * 112-146).  _enqueue queues the pass on `stream` and returns without
+ * waiting; the host work of the next molecule then overlaps this one's
+ * device work.  _collect waits for that pass, checks the device error word,
+ * copies the nplanes x 7 sums to out and, when ms is given, stores the
+ * stream time from the pass's first to its last operation (waits for work
+ * queued ahead of it excluded).  Between the two calls the context must not
+ * evaluate anything else (its scratch holds the pending pass); a second
+ * _enqueue before _collect is rejected. */
+int gg_plane_integrals_enqueue(gg_ctx *ctx, const gg_grid *grids, int nplanes, void *stream);
+int gg_plane_integrals_collect(gg_ctx *ctx, double *out, double *ms);
+
 /* Composite quadrature (gaussint.f90:267-319); type 0 Gauss-Legendre,
  * 1 Gauss-Lobatto.  Returns GG_EINVAL if npts is not a multiple of order or
  * the Newton iteration fails. */

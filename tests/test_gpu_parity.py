@@ -331,3 +331,38 @@ def test_properties_against_oracle(c6h6, precision, tol):
     assert s1.shape == (len(xyz), 1, 5)
     assert np.allclose(s1[:, 0, :], sig.sum(axis=1), rtol=1e-9, atol=1e-12)
     assert np.allclose(c1[0], chi.sum(axis=0), rtol=1e-9, atol=1e-15)
+
+
+def test_queued_plane_passes_match_blocking_calls(c6h6, c6h6_uhf):
+    """gg_plane_integrals_enqueue / _collect over several contexts gives the
+    blocking call's sums; a second enqueue before collecting, and a collect
+    with nothing queued, are rejected."""
+    from gimic_gb300 import scan
+
+    jobs = []
+    for (mp, xp, mol), uhf in ((c6h6, False), (c6h6_uhf, True)):
+        g = api.Gimic(mp, xp, uhf=uhf, screening=1e-8)
+        bond = scan.first_cc_bond(mol.symbols, mol.coords)
+        planes, bb = scan.profile_planes(mol.coords, bond=bond, start=-2.0, out=8.0, nstrips=7, npts=(30, 30),
+                                         order=10, quadrature="lobatto",
+                                         fixcoord=tuple(scan.plane_fixcoord(mol.coords, bond)))
+        g.set_magnet(bb)
+        jobs.append((g, planes))
+    want = [g.plane_integrals(planes) for g, planes in jobs]
+    for _ in range(2):
+        got, ms = api.plane_integrals_multi(jobs, timings=True)
+        assert all(t > 0 for t in ms)
+        for a, b in zip(got, want):
+            for ra, rb in zip(a, b):
+                assert np.allclose(ra["current"], rb["current"], rtol=1e-12, atol=1e-15)
+                assert np.allclose(ra["modulus"], rb["modulus"], rtol=1e-12, atol=1e-15)
+    g, planes = jobs[0]
+    specs, flat = api._grid_records(planes)
+    L = g._L
+    p = specs.ctypes.data_as(C.POINTER(_lib.GridSpec))
+    assert L.gg_plane_integrals_enqueue(g._h, p, len(planes), None) == 0
+    assert L.gg_plane_integrals_enqueue(g._h, p, len(planes), None) != 0
+    out = np.zeros((len(planes), 7))
+    assert L.gg_plane_integrals_collect(g._h, out.ctypes.data_as(C.POINTER(C.c_double)), None) == 0
+    assert np.allclose(out[:, 0], [r["current"][0] for r in want[0]], rtol=1e-12, atol=1e-15)
+    assert L.gg_plane_integrals_collect(g._h, out.ctypes.data_as(C.POINTER(C.c_double)), None) != 0
