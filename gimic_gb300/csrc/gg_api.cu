@@ -481,24 +481,32 @@ struct gg_ctx {
       const int kpad = dB.kpad, nchunk = dB.nchunk;
       const size_t ncol = static_cast<size_t>(nchunk) * gg::kBlockN;
       std::vector<__half> hi(ncol * kpad, __float2half_rn(0.f)), lo(ncol * kpad, __float2half_rn(0.f));
-      std::vector<float> icol(ncol, 1.f);
+      // one power-of-two scale per matrix puts its largest entry just under
+      // 2^14; the epilogue applies the inverse to its finished sums, where
+      // every sum belongs to one matrix.  Entries far below the largest lose
+      // relative precision in fp16 (subnormal lo parts) but keep an absolute
+      // error below 2^-38 of the matrix's largest entry.
+      std::vector<float> icol(gg::kMats, 1.f);
+      std::vector<double> tscale(gg::kMats, 0.0);
+      for (int m = 0; m < gg::kMats; ++m) {
+        double mx = 0.0;
+        for (int nu = 0; nu < n; ++nu)
+          for (int mu = 0; mu < n; ++mu) mx = std::max(mx, std::fabs(M(m, mu, nu)));
+        int ex = 0;
+        if (mx > 0.0) std::frexp(mx, &ex);
+        if (mx == 0.0 || ex < -100) continue;  // negligible matrix: keep zeros
+        tscale[m] = std::ldexp(1.0, 14 - ex);
+        icol[m] = static_cast<float>(std::ldexp(1.0, ex - 14));
+      }
       std::vector<double> col(n);
       for (int c = 0; c < nchunk; ++c)
-        for (int m = 0; m < 7; ++m)
+        for (int m = 0; m < gg::kMats; ++m)
           for (int u = 0; u < gg::kChunkF; ++u) {
             const int nu = c * gg::kChunkF + u;
-            if (nu >= n) continue;
+            if (nu >= n || tscale[m] == 0.0) continue;
             const size_t cidx = static_cast<size_t>(c) * gg::kBlockN + m * gg::kChunkF + u;
-            double mx = 0.0;
-            for (int mu = 0; mu < n; ++mu) {
-              col[mu] = M(m, mu, nu);
-              mx = std::max(mx, std::fabs(col[mu]));
-            }
-            int ex = 0;
-            if (mx > 0.0) std::frexp(mx, &ex);
-            if (mx == 0.0 || ex < -100) continue;  // negligible column: keep zeros
-            const double t = std::ldexp(1.0, 14 - ex);
-            icol[cidx] = static_cast<float>(std::ldexp(1.0, ex - 14));
+            for (int mu = 0; mu < n; ++mu) col[mu] = M(m, mu, nu);
+            const double t = tscale[m];
             for (int mu = 0; mu < n; ++mu) {
               const double v = col[mu] * t;
               const __half h = __float2half_rn(static_cast<float>(v));

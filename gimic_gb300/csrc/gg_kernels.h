@@ -43,7 +43,7 @@ struct TcArgs {
   const void* tmap_b_hi;
   const void* tmap_b_lo;
   const float* inv_row_scale;  // per point
-  const float* inv_col_scale;  // [nchunk * 224]
+  const float* inv_col_scale;  // [7]: inverse power-of-two scale of each matrix
   const double* pts;
   int64_t npts;
   Flags flags;

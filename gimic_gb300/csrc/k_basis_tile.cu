@@ -193,8 +193,10 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
       float f1 = 0.f;
       const bool in_range = df_le(d2, __ldg(B.sh_rad2_df + sh));
       if (in_range) {
-        for (int k = 0; k < np; ++k)
-          f1 += __ldg(B.p_cc + pk.w + k) * gauss_df(__ldg(B.p_xp + pk.w + k), __ldg(B.p_xplo + pk.w + k), d2.h, d2.l);
+        for (int k = 0; k < np; ++k) {
+          const float4 pr = __ldg(B.p_pack + pk.w + k);  // exponent hi, exponent lo, coefficient
+          f1 += pr.z * gauss_df(pr.x, pr.y, d2.h, d2.l);
+        }
         f1 *= scale;
       }
       // a shell out of range for the whole warp only writes zeros

@@ -83,6 +83,16 @@ __device__ __forceinline__ void tmem_wait7(float* v) {
 // compensated fp32 sum (Kahan): hi + lo tracks the running total; lo holds
 // what the last addition lost.  The chunk's partial sum y starts from lo
 // (instead of zero), which feeds the loss into the next addition.
+// the matrix of each of the kNDots sums: 0..12 D (rho, X, E), 13..24 C_d
+// (Y_dm at 13 + 3d + m, Laplacian terms at 22 + d), 25..36 P_d (Z_dm at
+// 25 + 3d + m, Laplacian terms at 34 + d)
+__host__ __device__ constexpr int dot_matrix(int i) {
+  return i < 13 ? 0 : i < 22 ? 1 + (i - 13) / 3 : i < 25 ? 1 + (i - 22) : i < 34 ? 4 + (i - 25) / 3 : 4 + (i - 34);
+}
+static_assert(dot_matrix(12) == 0 && dot_matrix(13) == 1 && dot_matrix(21) == 3 && dot_matrix(24) == 3 &&
+                  dot_matrix(25) == 4 && dot_matrix(33) == 6 && dot_matrix(36) == 6 && kNDots == 37,
+              "sum layout");
+
 __device__ __forceinline__ void kahan_add(float& hi, float& lo, float y) {
   const float t = hi + y;
   lo = y - (t - hi);
@@ -333,20 +343,17 @@ __global__ void __launch_bounds__(kThreads, 1)
           float v[kMats];
 #pragma unroll
           for (int m = 0; m < kMats; ++m) tmem_ld1(tcol + m * kChunkF + u, v[m]);
-          // while the loads are in flight: the column scales and the
-          // function's value, gradient and Laplacian (all zero on lanes
-          // whose shell is screened, as f1 = f2 = f3 = 0 there)
-          const float* cs = icol + c * kBlockN + u;
-          float sc[kMats];
-#pragma unroll
-          for (int m = 0; m < kMats; ++m) sc[m] = cs[m * kChunkF];
+          // while the loads are in flight: the function's value, gradient
+          // and Laplacian (all zero on lanes whose shell is screened, as
+          // f1 = f2 = f3 = 0 there).  The sums stay in the matrices' scaled
+          // units until the combination.
           float ph, gx, gy, gz, lp;
           cart_case(fp & 0xfff, cp, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
           tmem_wait7(v);
           {
-            const float w0 = v[0] * sc[0];
-            const float wc[3] = {v[1] * sc[1], v[2] * sc[2], v[3] * sc[3]};
-            const float qq[3] = {v[4] * sc[4], v[5] * sc[5], v[6] * sc[6]};
+            const float w0 = v[0];
+            const float wc[3] = {v[1], v[2], v[3]};
+            const float qq[3] = {v[4], v[5], v[6]};
             const float wp = w0 * ph;
             part[0] = fmaf(w0, ph, part[0]);
             part[1] = fmaf(wp, sx, part[1]);
@@ -393,13 +400,18 @@ __global__ void __launch_bounds__(kThreads, 1)
       } else {
         if (!mbar_wait(xfull, tk & 1, err, 6)) break;
         if (valid) {
-          // the row scale is a power of two: scaling a double-float is exact
+          // the row scale and the matrix scales are powers of two: scaling
+          // a double-float is exact.  Sum i belongs to matrix dot_matrix(i).
           const float sc = inv_row[p];
+          float msc[kMats];
+#pragma unroll
+          for (int m = 0; m < kMats; ++m) msc[m] = sc * icol[m];
           const float2* h1 = redf + row * kNDots;
           auto tot = [&](int i) -> DFloat {
             const float2 o = h1[i];
             const DFloat t = df_add(DFloat{thi[i], tlo[i]}, DFloat{o.x, o.y});
-            return DFloat{t.h * sc, t.l * sc};
+            const float f = msc[dot_matrix(i)];
+            return DFloat{t.h * f, t.l * f};
           };
           const int64_t o = perm ? static_cast<int64_t>(perm[p]) : p;  // caller's point order
           if (fl.giao && fl.dia && fl.para) {
