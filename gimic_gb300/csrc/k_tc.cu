@@ -93,6 +93,9 @@ static_assert(dot_matrix(12) == 0 && dot_matrix(13) == 1 && dot_matrix(21) == 3 
                   dot_matrix(25) == 4 && dot_matrix(33) == 6 && dot_matrix(36) == 6 && kNDots == 37,
               "sum layout");
 
+// the Laplacian sums, used only by div j
+__host__ __device__ constexpr bool is_div_sum(int i) { return (i >= 22 && i < 25) || i >= 34; }
+
 __device__ __forceinline__ void kahan_add(float& hi, float& lo, float y) {
   const float t = hi + y;
   lo = y - (t - hi);
@@ -108,6 +111,11 @@ int tc_smem_bytes() { return kSmemBytes; }
 // small terms are added while the accumulator is still small, which keeps
 // their truncation error negligible (measured: max error of j 1.2e-6 with the
 // products interleaved, 4.6e-7 cross-first, for nbf = 720).
+//
+// kDiv: the divergence sums (Laplacian terms) are accumulated only when the
+// caller asked for div j; without them each function costs 6 FMAs, the
+// Laplacian and one FMA per primitive less.
+template <bool kDiv>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_fused_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_constant__ CUtensorMap tm_a_lo,
                     const __grid_constant__ CUtensorMap tm_b_hi, const __grid_constant__ CUtensorMap tm_b_lo,
@@ -335,7 +343,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const float e = pr.z * gauss_df(al, pr.y, d2a.h, d2a.l);
                 f1 += e;
                 f2 += al * e;
-                f3 += al * al * e;
+                if (kDiv) f3 += al * al * e;
               }
             }
           }
@@ -347,8 +355,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           // and Laplacian (all zero on lanes whose shell is screened, as
           // f1 = f2 = f3 = 0 there).  The sums stay in the matrices' scaled
           // units until the combination.
-          float ph, gx, gy, gz, lp;
-          cart_case(fp & 0xfff, cp, f1, f2, f3, &ph, &gx, &gy, &gz, &lp);
+          float ph, gx, gy, gz, lp = 0.f;
+          cart_case(fp & 0xfff, cp, f1, f2, f3, &ph, &gx, &gy, &gz, kDiv ? &lp : nullptr);
           tmem_wait7(v);
           {
             const float w0 = v[0];
@@ -374,8 +382,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 part[13 + 3 * d + m] = fmaf(wc[d], g[m], part[13 + 3 * d + m]);
                 part[25 + 3 * d + m] = fmaf(qq[d], g[m], part[25 + 3 * d + m]);
               }
-              part[22 + d] = fmaf(wc[d], lp, part[22 + d]);
-              part[34 + d] = fmaf(qq[d], lp, part[34 + d]);
+              if (kDiv) {
+                part[22 + d] = fmaf(wc[d], lp, part[22 + d]);
+                part[34 + d] = fmaf(qq[d], lp, part[34 + d]);
+              }
             }
           }
         }
@@ -384,7 +394,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(&accempty[b]);
 #pragma unroll
         for (int i = 0; i < kNDots; ++i)
-          if (i != 4 && i != 8 && i != 12) kahan_add(thi[i], tlo[i], part[i]);
+          if (i != 4 && i != 8 && i != 12 && (kDiv || !is_div_sum(i))) kahan_add(thi[i], tlo[i], part[i]);
       }
       if (!ok) break;
       // combine the two halves of every point through `red` (float pairs):
@@ -444,23 +454,33 @@ done:
   }
 }
 
+namespace {
+// shared-memory size and the register check, once per instantiation: the
+// register split assumes the launch allocation; with fewer registers per
+// thread the epilogue's setmaxnreg.inc could never be granted
+template <bool kDiv>
+cudaError_t tc_kernel_setup() {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(tc_fused_kernel<kDiv>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, tc_fused_kernel<kDiv>);
+  if (e != cudaSuccess) return e;
+  if (fa.numRegs < kRegsLaunch) return cudaErrorInvalidConfiguration;
+  done = true;
+  return cudaSuccess;
+}
+}  // namespace
+
 cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st) {
   if (a.npts <= 0) return cudaSuccess;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(tc_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-    if (e != cudaSuccess) return e;
-    // the register split assumes the launch allocation; with fewer registers
-    // per thread the epilogue's setmaxnreg.inc could never be granted
-    cudaFuncAttributes fa;
-    e = cudaFuncGetAttributes(&fa, tc_fused_kernel);
-    if (e != cudaSuccess) return e;
-    if (fa.numRegs < kRegsLaunch) return cudaErrorInvalidConfiguration;
-    attr_set = true;
-  }
+  const bool div = a.out.divt || a.out.divt32;
+  cudaError_t e = div ? tc_kernel_setup<true>() : tc_kernel_setup<false>();
+  if (e != cudaSuccess) return e;
   static int nsm[64] = {0};
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (!nsm[dev]) {
@@ -469,7 +489,8 @@ cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st)
   }
   const int64_t ntiles = (a.npts + kBlockM - 1) / kBlockM;
   const unsigned grid = static_cast<unsigned>(std::min<int64_t>(ntiles, nsm[dev]));
-  tc_fused_kernel<<<grid, kThreads, kSmemBytes, st>>>(
+  auto kernel = div ? tc_fused_kernel<true> : tc_fused_kernel<false>;
+  kernel<<<grid, kThreads, kSmemBytes, st>>>(
       *static_cast<const CUtensorMap*>(a.tmap_a_hi), *static_cast<const CUtensorMap*>(a.tmap_a_lo),
       *static_cast<const CUtensorMap*>(a.tmap_b_hi), *static_cast<const CUtensorMap*>(a.tmap_b_lo), B,
       a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err, a.tiles, a.tile_stride, a.perm,
