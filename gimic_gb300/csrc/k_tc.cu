@@ -282,6 +282,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
       for (int i = 0; i < kNDots; ++i) thi[i] = tlo[i] = 0.f;
       int cur_shell = -1, cur_atom = -1;
+      // the next shell's record and its screening radius, loaded when a
+      // shell starts (shells are contiguous in function order), so that a
+      // shell change does not wait on a chain of dependent loads
+      int sh_pre = -1;
+      int4 pk_pre = make_int4(0, 0, 0, 0);
+      float2 rad_pre = make_float2(0.f, 0.f);
       float sx = 0.f, sy = 0.f, sz = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
       CartPow cp = cart_pow(0.f, 0.f, 0.f);
       DFloat d2a{0.f, 0.f};
@@ -311,7 +317,14 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int sh = fp >> 12;
           if (sh != cur_shell) {
             cur_shell = sh;
-            const int4 pk = shp[sh];  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
+            const bool hit = sh == sh_pre;
+            const int4 pk = hit ? pk_pre : shp[sh];  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
+            const float2 rad = hit ? rad_pre : shr[sh];
+            if (sh + 1 < Bs.nshells) {
+              sh_pre = sh + 1;
+              pk_pre = shp[sh + 1];
+              rad_pre = shr[sh + 1];
+            }
             const int a = pk.x;
             if (a != cur_atom) {
               cur_atom = a;
@@ -322,7 +335,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               sz = s3[2];
               cp = cart_pow(sx, sy, sz);
             }
-            on = df_le(d2a, shr[sh]);
+            on = df_le(d2a, rad);
             // a shell screened for all 32 points of the warp contributes
             // nothing: skip its remaining functions in this range
             warp_on = __any_sync(0xffffffffu, on);
