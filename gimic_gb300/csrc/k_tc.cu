@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   auto chunk_at = [&](int64_t tile, int i) -> int { return tiles ? tiles[tile * tstride + 2 + i] : i; };
   auto kb_at = [&](int64_t tile, int i) -> int { return tiles ? tiles[tile * tstride + 2 + nchunk_all + i] : i; };
   auto failed = [&]() -> bool { return *reinterpret_cast<volatile int*>(err) != 0; };
-  // epilogue tables: column scales, per-function records (shell << 12 |
+  // epilogue tables: matrix scales, per-function records (shell << 12 |
   // Cartesian case), shell records, primitives, atoms
   const float* icol = inv_col;
   const int* fpack = Bs.f_pack;
