@@ -150,6 +150,66 @@ def cpu_baseline(mp, xp, sample, seed=7):
                       % (sample, cores, dt)}
 
 
+def oracle_errors(mp, xp, pts, got_j, got_rho):
+    """e_j = max |j_gpu - j_oracle| / max |j_oracle| over the sample, overall
+    and per tensor component (index m + 3 b), and the same for the density."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    cores = os.cpu_count() or 1
+    ref_j, ref_r = oracle.Oracle(mp, xp, screening=1e-8).jtensor(pts, nthreads=cores, with_rho=True)
+    scale = float(np.abs(ref_j).max())
+    comp = (np.abs(got_j - ref_j).max(axis=0) / scale).tolist()
+    return {"e_j": max(comp), "per_component": comp,
+            "e_rho": float(np.abs(got_rho - ref_r).max() / np.abs(ref_r).max()), "tolerance": 1e-6,
+            "sample": "4096 random points of the timed 128^3 cube (the step's own outputs) + 1024 points within "
+                      "~0.1 Bohr of the nuclei", "oracle": "oracle/og_oracle.c (FP64 restatement)"}
+
+
+def plane_errors(mp, xp, grd, bb, res):
+    """|I_gpu - I_oracle| in nA/T for the plane's current, signed modulus
+    and ACID (og_integrate, integral.f90:50-511)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    from gimic_gb300 import api
+
+    o = oracle.Oracle(mp, xp, screening=1e-8)
+    cores = os.cpu_count() or 1
+    out = {}
+    for kind in ("current", "modulus"):
+        ref = o.integrate(grd.origin, grd.basv, grd.axes(), grd.radius, bb, what=kind, nthreads=cores)
+        out[kind] = max(abs(api.au2si(a) - api.au2si(b)) for a, b in zip(res[kind], ref))
+    ref = o.integrate(grd.origin, grd.basv, grd.axes(), grd.radius, bb, what="acid", nthreads=cores)
+    out["acid"] = abs(api.au2si(res["acid"]) - api.au2si(ref[0]))
+    out["tolerance"] = 1e-4
+    return out
+
+
+def measured_fp64_peak(dev):
+    """FP64 GEMM throughput of this GPU (TFLOP/s): cuBLAS DGEMM 8192^3 through
+    torch.matmul, best of 3, timed with CUDA events."""
+    import torch
+
+    try:
+        a = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
+        b = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
+        torch.matmul(a, b)
+        best = None
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        del a, b
+        return 2.0 * 8192 ** 3 / (best * 1e-3) / 1e12
+    except Exception:
+        return None
+
+
 def run_reference(args, rank, world):
     """Reference arm: the reference's FP64 algorithm on the host cores.  The
     reference's Fortran cannot be built here (no gfortran), so the arm times
@@ -589,20 +649,32 @@ def main():
     e2e = {"value": npts * world / e2e_s, "unit": "points/s", "h2d_bytes_per_step": npts * 3 * 8,
            "d2h_bytes_per_step": npts * (9 + 1 + 3) * 8, "ms_per_step": e2e_s * 1e3}
 
-    # ---- plane integrals: 60x60 Gauss-Lobatto bond plane -------------------
-    text = ("calc=integral\nmagnet_axis=z\nGrid(bond) {\n type=lobatto\n bond=[1,2]\n fixcoord=[0.0,0.0,0.0]\n"
-            " distance=%.6f\n height=[-8.0, 8.0]\n width=[-4.0, 8.0]\n grid_points=[60, 60, 0]\n"
-            " gauss_order=10\n}\n" % (0.5 * np.linalg.norm(mol.coords[1] - mol.coords[0])))
-    pin = ginp.read(text, is_text=True)
-    grd = ggrid.new_grid(pin, mol.coords)
+    # ---- parity of the timed workload against the FP64 oracle ---------------
+    # 4096 points of the timed cube, read from one step's own outputs, and
+    # 1024 points within ~0.1 Bohr of the nuclei (where |j| is largest; they
+    # are not cube points, so they go through one more call)
+    prng = np.random.default_rng(17)
+    idx = np.sort(prng.choice(npts, 4096, replace=False))
+    near = mol.coords[prng.integers(0, len(mol.coords), 1024)] + prng.normal(0.0, 0.1, (1024, 3))
+    jt_all, rho_all, _ = step()
+    tidx = torch.as_tensor(idx, device=dev)
+    got_j = np.vstack([jt_all[tidx].cpu().numpy(), g.jtensor_batch(near)])
+    got_r = np.concatenate([rho_all[tidx].cpu().numpy(), g.jtensor_batch(near, rho=True)[1]])
+    del jt_all, rho_all
+
+    # ---- plane integrals: the C6H6 bond plane (60x60 Gauss-Lobatto) ---------
+    mp1, xp1, mol1 = synth.make_workload("c6h6", args.data, seed=2024)
+    g1 = api.Gimic(mp1, xp1, screening=1e-8, precision="split16")
+    pin = ginp.read(synth.ring_bond_plane_input(mol1), is_text=True)
+    grd = ggrid.new_grid(pin, mol1.coords)
     bb, _ = ggrid.get_magnet(grd, pin)
-    g.set_magnet(bb)
-    res = g.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)
-    reps = 20
+    g1.set_magnet(bb)
+    res = g1.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)
+    reps = 200
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for _ in range(reps):
-        g.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)
+        g1.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)
     plane_s = (time.perf_counter() - t0) / reps
 
     # ---- plain FP64 GPU path on a subset (the 10x reference point) --------
@@ -615,11 +687,14 @@ def main():
     torch.cuda.synchronize(dev)
     fp64_pts_s = len(sub) / (time.perf_counter() - t0)
 
+    fp64_peak = measured_fp64_peak(dev)
     if rank != 0:
         if dist is not None:
             dist.barrier()
         return
     cpu = cpu_baseline(mp, xp, args.cpu_sample)
+    errs = oracle_errors(mp, xp, np.vstack([pts_np[idx], near]), got_j, got_r)
+    plane_err = plane_errors(mp1, xp1, grd, bb, res)
     line = {
         "metric": METRIC,
         "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
@@ -629,11 +704,22 @@ def main():
                    "precision": "split-FP16 x3 tcgen05, FP32 accumulate, FP64 combine",
                    "l2": "inputs larger than L2 (points 50 MB, outputs 218 MB, operand scratch 3.2 GB per pass)",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "rel_err_vs_fp64_oracle": errs,
         "plane_integrals_per_s": 1.0 / plane_s,
-        "plane": {"points": int(np.prod(grd.npts)), "type": "60x60 Gauss-Lobatto (order 10), bond plane",
-                  "current_nAT": api.au2si(res["current"][0])},
+        "plane": {"workload": "C6H6 (nbf %d) bond plane through the C1-C2 midpoint: 60x60 Gauss-Lobatto (order 10), "
+                              "height -8..8 Bohr, from the ring centre to 8 Bohr outward, B along z" % mol1.nbf,
+                  "points": int(np.prod(grd.npts)), "what": "one gg_plane_integral call per plane, host wall time",
+                  "current_nAT": api.au2si(res["current"][0]), "modulus_nAT": api.au2si(res["modulus"][0]),
+                  "acid_nAT": api.au2si(res["acid"]), "abs_err_vs_fp64_oracle_nAT": plane_err},
         "fp64_gpu_points_per_s": fp64_pts_s,
         "speedup_vs_fp64_gpu": value / world / fp64_pts_s,
+        "fp64_gpu_roofline": {"bound": "fp64", "achieved": flops_per_point(n) * fp64_pts_s / 1e12,
+                              "peak": fp64_peak, "unit": "TFLOP/s",
+                              "frac": flops_per_point(n) * fp64_pts_s / 1e12 / fp64_peak if fp64_peak else None,
+                              "peak_source": "measured here: cuBLAS DGEMM 8192^3 (torch.matmul float64), best of 3, "
+                                             "CUDA events",
+                              "accounting": "(14 n^2 + 56 n) flops per point, dense (the FP64 path does not screen "
+                                            "tiles)"},
         "e2e": e2e,
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "achieved": exec_tflops, "peak": peak_tf, "unit": "TFLOP/s",

@@ -23,6 +23,8 @@ namespace {
 
 thread_local std::string g_create_error;
 
+constexpr int kSelftestWaitCode = 100;  // error code of the wait self-test
+
 // Device buffer that grows on demand.
 struct DevBuf {
   void* p = nullptr;
@@ -158,6 +160,7 @@ struct gg_ctx {
   cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
   DevBuf phi, gx, gy, gz, lap, w64;
   DevBuf plane_rows, plane_out;
+  DevBuf diag;  // the wait self-test's measured time
   void* plane_host = nullptr;  // pinned staging of the plane uploads
   size_t plane_host_bytes = 0;
   // a queued plane pass (gg_plane_integrals_enqueue until _collect)
@@ -239,7 +242,7 @@ struct gg_ctx {
     table_allocs.clear();
     tables_ready = false;
     for (DevBuf* b : {&b_fp64, &b_hi, &b_lo, &inv_col, &pts, &jt, &rho, &divt, &jv, &phi, &gx, &gy, &gz, &lap, &w64,
-                      &plane_rows, &plane_out, &pts2, &jt2, &rho2, &divt2, &tile_ctr})
+                      &plane_rows, &plane_out, &pts2, &jt2, &rho2, &divt2, &tile_ctr, &diag})
       b->release();
     for (SplitSlot& sl : slot) {
       for (DevBuf* b : {&sl.a_hi, &sl.a_lo, &sl.inv_row, &sl.sort_keys, &sl.sort_keys2, &sl.sort_idx, &sl.sort_perm,
@@ -251,6 +254,9 @@ struct gg_ctx {
     d_err = nullptr;
     mats_spin = -1;
   }
+
+  // get_magnet stops on a zero field (src/fgimic/magnet.f90:56-59)
+  bool zero_field() const { return magnet[0] == 0.0 && magnet[1] == 0.0 && magnet[2] == 0.0; }
 
   int fail(int code, const std::string& msg) {
     err = msg;
@@ -412,13 +418,23 @@ struct gg_ctx {
     if (e == cudaSuccess) e = upload(sh_radf, &d.sh_rad);
     d.env_bins = env_bins;
     if (e != cudaSuccess) return cuda_fail(e, "uploading basis tables");
-    if (!d_err) {
-      e = cudaMalloc(&d_err, sizeof(int));
-      if (e == cudaSuccess) e = cudaMemset(d_err, 0, sizeof(int));
-      if (e != cudaSuccess) return cuda_fail(e, "allocating error word");
-    }
+    int rc = error_word();
+    if (rc) return rc;
     dB = d;
     tables_ready = true;
+    return GG_OK;
+  }
+
+  // The device error word (0 = ok) that the kernels' bounded waits report to.
+  int error_word() {
+    if (d_err) return GG_OK;
+    cudaError_t e = cudaMalloc(&d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(d_err, 0, sizeof(int));
+    if (e != cudaSuccess) {
+      if (d_err) cudaFree(d_err);
+      d_err = nullptr;
+      return cuda_fail(e, "allocating error word");
+    }
     return GG_OK;
   }
 
@@ -1137,6 +1153,7 @@ int gg_jtensor_batch_f32(gg_ctx* ctx, const double* pts, int64_t n, float* jt, f
 
 int gg_jvector_batch(gg_ctx* ctx, const double* pts, int64_t n, double* jv, void* stream) {
   if (!ctx || !jv) return GG_EINVAL;
+  if (ctx->zero_field()) return ctx->fail(GG_EINVAL, "Magnetic field is zero, not wasting more CPU.");
   std::vector<double> t(static_cast<size_t>(std::max<int64_t>(n, 0)) * 9);
   const bool dev_out = is_device_ptr(jv);
   if (dev_out) return ctx->fail(GG_EUNSUPPORTED, "gg_jvector_batch writes host memory only");
@@ -1153,6 +1170,7 @@ int gg_jvector_batch(gg_ctx* ctx, const double* pts, int64_t n, double* jv, void
 // context's device scratch at *d_result.  The caller holds ctx->mu.
 static int plane_enqueue(gg_ctx* ctx, const gg_grid* grids, int nplanes, cudaStream_t st, const double** d_result) {
   if (!grids || nplanes <= 0) return GG_EINVAL;
+  if (ctx->zero_field()) return ctx->fail(GG_EINVAL, "Magnetic field is zero, not wasting more CPU.");
   int64_t npts = 0, nrows = 0, nw = 0;
   for (int q = 0; q < nplanes; ++q) {
     const gg_grid& gr = grids[q];
@@ -1370,6 +1388,48 @@ int gg_profile_blocks(const gg_ctx* ctx, int64_t* issued, int64_t* dense) {
   return GG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Self-tests of the failure paths (no reference counterpart).  Neither
+// faults, traps or hangs the GPU: the first runs a wait that nothing
+// satisfies until its time limit, the second makes the next evaluation's
+// kernels find an error already recorded and leave their pipelines early.
+// ---------------------------------------------------------------------------
+int gg_selftest_wait_timeout(gg_ctx* ctx, double limit_ms, double* waited_ms, void* stream) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (!(limit_ms > 0.0) || limit_ms > 2000.0) return ctx->fail(GG_EINVAL, "limit_ms must be in (0, 2000]");
+  if (ctx->plane_pending) return ctx->fail(GG_EINVAL, "a queued plane pass has not been collected");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
+  int rc = ctx->error_word();
+  if (rc) return rc;
+  e = ctx->diag.reserve(sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->diag.p, 0, sizeof(unsigned long long), st);
+  if (e == cudaSuccess)
+    e = gg::launch_wait_timeout(ctx->d_err, static_cast<uint64_t>(limit_ms * 1e6), kSelftestWaitCode,
+                                ctx->diag.as<unsigned long long>(), st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  unsigned long long ns = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&ns, ctx->diag.p, sizeof(ns), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "wait self-test");
+  ctx->launches += 1;
+  if (waited_ms) *waited_ms = static_cast<double>(ns) * 1e-6;
+  return ctx->device_error_word();
+}
+
+int gg_selftest_fail_next(gg_ctx* ctx, int code) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  if (code == 0) return ctx->fail(GG_EINVAL, "the error code must be nonzero");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
+  int rc = ctx->error_word();
+  if (rc) return rc;
+  e = cudaMemcpy(ctx->d_err, &code, sizeof(int), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? GG_OK : ctx->cuda_fail(e, "writing the error word");
+}
+
 int gg_gauss_data(double a, double b, int order, int npts, int type, double* pts, double* wgts) {
   if (!pts || !wgts || npts <= 0 || (type != 0 && type != 1)) return GG_EINVAL;
   return gg::gauss_data(a, b, order, npts, type, pts, wgts) == 0 ? GG_OK : GG_EINVAL;
@@ -1449,6 +1509,12 @@ void gimic_calc_jtensor(const double* r, double* jt) {
 
 void gimic_calc_jvector(const double* r, double* jv) {
   if (!g_ctx) gimic_stop("gimic_calc_jvector(): gimic_init() has not been called");
+  if (g_ctx->zero_field()) {  // jvector (jtensor.F90:125-135) gives T . 0 = 0; it does not stop
+    double jt[9];
+    if (gg_jtensor_batch(g_ctx, r, 1, jt, nullptr, nullptr, nullptr) != GG_OK) gimic_stop(gg_last_error(g_ctx));
+    jv[0] = jv[1] = jv[2] = 0.0;
+    return;
+  }
   if (gg_jvector_batch(g_ctx, r, 1, jv, nullptr) != GG_OK) gimic_stop(gg_last_error(g_ctx));
 }
 
@@ -1594,6 +1660,11 @@ extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t 
   if (n == 0) return GG_OK;
   if (ctx->precision != GG_PREC_SPLIT16)
     return ctx->fail(GG_EUNSUPPORTED, "gg_jtensor_batch_noalloc runs the split-FP16 path only");
+  if (ctx->plane_pending)  // its error word is read only by _collect
+    return ctx->fail(GG_EINVAL, "a queued plane pass has not been collected");
+  if (ctx->tables_ready && ctx->dB.kpad > 64 * gg::kBlockK)
+    return ctx->fail(GG_EUNSUPPORTED, "the split-FP16 path handles at most 4096 basis functions (nbf=" +
+                                          std::to_string(ctx->basis.nbf) + "); use the FP64 precision");
   if (!ctx->tables_ready || !ctx->d_err || ctx->mats_spin != ctx->spin || ctx->mats_prec != ctx->precision)
     return ctx->fail(GG_EINVAL,
                      "context not prepared for this spin case: call gg_jtensor_batch once first (it builds the "
@@ -1633,13 +1704,26 @@ extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t 
       !encode_fp16_2d(&tms_hi, a_hi, n, ctx->dB.kpad, gg::kBlockM, true) ||
       !encode_fp16_2d(&tms_lo, a_lo, n, ctx->dB.kpad, gg::kBlockM, true))
     return ctx->fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
+  size_t ps = 0;
+  ctx->prof_begin(GG_PROF_BASIS, st, &ps);
   e = gg::launch_basis_tile(ctx->dB, &tms_hi, &tms_lo, pts, n, nullptr, 0, inv_row, st);
+  ctx->prof_end(st, ps);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "basis kernel launch");
   gg::TcArgs ta{&tma_hi, &tma_lo, &ctx->tm_b_hi, &ctx->tm_b_lo, inv_row, ctx->inv_col.as<float>(),
                 pts,     n,       ctx->flags,     gg::Outputs{jt, rho, divt}, ctx->d_err};
   ta.tile_counter = tile_counter;
+  if (ctx->prof.on) {  // no tile screening here: every dense block is issued
+    const unsigned long long blocks = static_cast<unsigned long long>((n + gg::kBlockM - 1) / gg::kBlockM) *
+                                      ctx->dB.nchunk * (ctx->dB.kpad / gg::kBlockK);
+    ctx->prof.dense_blocks += blocks;
+    ctx->prof_add_blocks(blocks, st);
+  }
   e = cudaMemsetAsync(tile_counter, 0, sizeof(int), st);
-  if (e == cudaSuccess) e = gg::launch_tc_fused(ctx->dB, ta, st);
+  if (e == cudaSuccess) {
+    ctx->prof_begin(GG_PROF_TC, st, &ps);
+    e = gg::launch_tc_fused(ctx->dB, ta, st);
+    ctx->prof_end(st, ps);
+  }
   if (e != cudaSuccess) return ctx->cuda_fail(e, "tensor-core kernel launch");
   ctx->launches += 2;
   return ctx->check_device_error(st);

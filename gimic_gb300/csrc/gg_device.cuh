@@ -277,20 +277,41 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Bounded wait: gives up after ~4 s (or 2^26 polls), or as soon as another
-// thread of the grid has reported an error; sets *err and returns false.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+// Bounded wait: gives up after limit_ns (or 2^26 polls), or as soon as
+// another thread of the grid has reported an error; sets *err (to `code`,
+// unless an error is already recorded) and returns false.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, int* err, int code, uint64_t limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   for (int it = 1; it < (1 << 26); ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 255) == 0) {
       if (*reinterpret_cast<volatile int*>(err) != 0) return false;
-      if (global_ns() - t0 > 4000000000ull) break;
+      if (global_ns() - t0 > limit_ns) break;
     }
   }
   atomicCAS(err, 0, code);
   return false;
+}
+
+// Bounded wait that ignores the error word, for the way out after an error:
+// it lets this thread's own copies or MMAs in flight land before the CTA's
+// shared memory and TMEM are released.  Returns false if they did not land
+// within limit_ns.
+__device__ __forceinline__ bool mbar_drain(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+  const uint64_t t0 = global_ns();
+  for (int it = 0; it < (1 << 26); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255) == 255 && global_ns() - t0 > limit_ns) return false;
+  }
+  return false;
+}
+constexpr uint64_t kDrainLimitNs = 1000000000ull;
+
+// The pipeline kernels' wait: about 4 s at most.
+constexpr uint64_t kWaitLimitNs = 4000000000ull;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+  return mbar_wait_for(bar, parity, err, code, kWaitLimitNs);
 }
 
 __device__ __forceinline__ void fence_barrier_init() {

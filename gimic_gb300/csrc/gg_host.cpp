@@ -246,7 +246,24 @@ std::string read_xdens(const std::string& path, const Basis& basis, bool uhf, De
     for (size_t i = 0; i < 4 * nn; ++i) {
       rd.begin();
       if (!rd.number(&m[i])) return "XDENS file too short for nbf=" + std::to_string(n) + ": " + path;
+      // the reference reads whatever is there (read_array, src/libgimic/
+      // dens.f90:125-131); a NaN or infinity would reach every point's
+      // tensor, so it is refused here with its position
+      if (!std::isfinite(m[i]))
+        return "XDENS value " + std::to_string(spin * 4 * nn + i + 1) + " is not finite: " + path;
     }
+  }
+  // The reference stops reading after the blocks it needs and ignores the
+  // rest, so a density of a larger basis (or an open-shell file read as
+  // closed shell) would silently give wrong currents.  Trailing numbers are
+  // therefore an error.
+  {
+    double extra = 0.0;
+    rd.begin();
+    if (rd.number(&extra))
+      return "XDENS holds more values than the " + std::to_string((uhf ? 2 : 1) * 4 * nn) + " that nbf=" +
+             std::to_string(n) + (uhf ? " (open shell)" : " (closed shell)") +
+             " needs: the density belongs to another basis or spin treatment: " + path;
   }
   if (uhf) {
     for (size_t i = nn; i < 4 * nn; ++i) {

@@ -102,6 +102,12 @@ void launch_plane_batch(const double* jt, const double* pts, const double* w, co
 void launch_properties(const double* jt, const double* pts, const double* w, const double* centres, int ncentres,
                        const int64_t* block_off, int nblocks, double* sigma_out, double* chi_out, cudaStream_t st);
 
+// Self-test of the bounded waits (k_diag.cu): one thread waits limit_ns on
+// an mbarrier that nothing arrives at and records `code` in *err; the time
+// it waited goes to *waited_ns (device memory, may be null).
+cudaError_t launch_wait_timeout(int* err, uint64_t limit_ns, int code, unsigned long long* waited_ns,
+                                cudaStream_t st);
+
 // Integration proposal network (k_mlp.cu): 5 -> 64 -> 64 -> 1, SiLU.
 constexpr int kMlpIn = 5;
 constexpr int kMlpHidden = 64;

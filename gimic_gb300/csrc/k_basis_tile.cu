@@ -35,6 +35,7 @@
 
 #include "gg_device.cuh"
 #include "gg_kernels.h"
+#include "gg_once.h"
 
 namespace gg {
 
@@ -224,12 +225,12 @@ cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* 
                               int64_t npts, const int* tiles, int stride, float* inv_scale, cudaStream_t st) {
   if (npts <= 0) return cudaSuccess;
   if (B.kpad / kBlockK > 64) return cudaErrorInvalidValue;  // K-block mask is 64 bits
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(basis_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  // the shared-memory attribute, once per device (it applies to the current one)
+  static PerDevice pd;
+  cudaError_t e = once_per_device(pd, nullptr, [](int, int*) {
+    return cudaFuncSetAttribute(basis_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+  });
+  if (e != cudaSuccess) return e;
   const unsigned grid = static_cast<unsigned>((npts + kBlockM - 1) / kBlockM);
   basis_tile_kernel<<<grid, kTileThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
                                                             *static_cast<const CUtensorMap*>(tm_lo), B, pts, npts,

@@ -33,6 +33,7 @@
 #include "gg_cart.cuh"
 #include "gg_combine.cuh"
 #include "gg_kernels.h"
+#include "gg_once.h"
 
 namespace gg {
 
@@ -135,7 +136,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* xempty = xfull + 1;     // half-0 has read them
   uint64_t* ring_full = xempty + 1;          // tile steps handed from the producer to the other roles
   uint64_t* ring_empty = ring_full + kRing;
-  int* ring = reinterpret_cast<int*>(ring_empty + kRing);
+  uint64_t* drain = ring_empty + kRing;      // the MMA issuer's last MMAs, after an error
+  int* ring = reinterpret_cast<int*>(drain + 1);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ring + kRing);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -172,6 +174,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&ring_full[k], 1);
       mbar_init(&ring_empty[k], 1 + kEpiWarps);
     }
+    mbar_init(drain, 1);
     fence_barrier_init();
   }
   if (warp == 1) tmem_alloc(tmem_slot, kTmemCols);
@@ -185,15 +188,19 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     reg_dealloc_ctl();
     if (lane == 0) {
-      int it = 0;
+      int it = 0;  // stages issued
+      bool clean = false;
       for (int step = 0;; ++step) {
         // next tile step from the global queue, handed to the other roles
         const int slot = step % kRing;
-        if (!mbar_wait(&ring_empty[slot], ((step / kRing) & 1) ^ 1, err, 7)) goto done;
+        if (!mbar_wait(&ring_empty[slot], ((step / kRing) & 1) ^ 1, err, 7)) goto producer_exit;
         const int64_t t = failed() ? ntiles : static_cast<int64_t>(atomicAdd(tile_counter, 1));
         ring[slot] = t < ntiles ? static_cast<int>(t) : -1;
         mbar_arrive(&ring_full[slot]);
-        if (t >= ntiles) break;
+        if (t >= ntiles) {
+          clean = true;
+          break;
+        }
         const int64_t tile = tile_of(t);
         const int m0 = static_cast<int>(tile * kBlockM);
         const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
@@ -205,7 +212,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int kb = kb_at(tile, q < 2 * nkb ? q >> 1 : q - 2 * nkb);
             const bool a_lo = q < 2 * nkb && (q & 1), b_lo = q < 2 * nkb && !(q & 1);
             const int s = it % kStages, round = it / kStages;
-            if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto done;
+            if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto producer_exit;
             unsigned char* st = base + s * kStageBytes;
             mbar_expect_tx(&full[s], kStageBytes);
             tma_load_2d(st, a_lo ? &tm_a_lo : &tm_a_hi, &full[s], kb * kBlockK, m0);
@@ -213,29 +220,38 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
       }
+    producer_exit:
+      // after an error: the loads still in flight (at most one per stage)
+      // land before the CTA's shared memory is released
+      if (!clean)
+        for (int j = max(0, it - kStages); j < it; ++j) mbar_drain(&full[j % kStages], (j / kStages) & 1, kDrainLimitNs);
     }
   } else if (warp == 1) {
     reg_dealloc_ctl();
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_f16(kBlockM, kBlockN);
       int it = 0, acc = 0;
+      bool clean = false;
       for (int step = 0;; ++step) {
         const int slot = step % kRing;
-        if (!mbar_wait(&ring_full[slot], (step / kRing) & 1, err, 8)) goto done;
+        if (!mbar_wait(&ring_full[slot], (step / kRing) & 1, err, 8)) goto mma_exit;
         const int t = ring[slot];
         mbar_arrive(&ring_empty[slot]);
-        if (t < 0) break;
+        if (t < 0) {
+          clean = true;
+          break;
+        }
         const int64_t tile = tile_of(t);
         const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
         for (int ci = 0; ci < nchunk; ++ci, ++acc) {
           const int b = acc & 1, rb = acc >> 1;
-          if (!mbar_wait(&accempty[b], (rb & 1) ^ 1, err, 2)) goto done;
+          if (!mbar_wait(&accempty[b], (rb & 1) ^ 1, err, 2)) goto mma_exit;
           tc_fence_after();
           const uint32_t d_tmem = tmem_base + b * kAccStride;
           // the stage sequence of the producer: 2 nkb cross pieces, then nkb main
           for (int q = 0; q < 3 * nkb; ++q, ++it) {
             const int s = it % kStages, round = it / kStages;
-            if (!mbar_wait(&full[s], round & 1, err, 3)) goto done;
+            if (!mbar_wait(&full[s], round & 1, err, 3)) goto mma_exit;
             tc_fence_after();
             unsigned char* st = base + s * kStageBytes;
             const uint64_t a = smem_desc_sw128(st), b = smem_desc_sw128(st + kTileA);
@@ -248,6 +264,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           mma_commit(&accfull[b]);
         }
+      }
+    mma_exit:
+      // after an error: the MMAs already issued finish before TMEM is freed
+      if (!clean) {
+        mma_commit(drain);
+        mbar_drain(drain, 0, kDrainLimitNs);
       }
     }
   } else if (warp >= kCtlWarps) {
@@ -458,7 +480,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else {
     reg_dealloc_ctl();  // warps 2 and 3: no role
   }
-done:
   tc_fence_before();
   __syncthreads();
   if (warp == 1) {
@@ -468,40 +489,35 @@ done:
 }
 
 namespace {
-// shared-memory size and the register check, once per instantiation: the
-// register split assumes the launch allocation; with fewer registers per
-// thread the epilogue's setmaxnreg.inc could never be granted
+// Per device and instantiation, once: the shared-memory size attribute and
+// the register check (the register split assumes the launch allocation;
+// with fewer registers per thread the epilogue's setmaxnreg.inc could never
+// be granted).  Stores the device's SM count.
 template <bool kDiv>
-cudaError_t tc_kernel_setup() {
-  static bool done = false;
-  if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(tc_fused_kernel<kDiv>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-  if (e != cudaSuccess) return e;
-  cudaFuncAttributes fa;
-  e = cudaFuncGetAttributes(&fa, tc_fused_kernel<kDiv>);
-  if (e != cudaSuccess) return e;
-  if (fa.numRegs < kRegsLaunch) return cudaErrorInvalidConfiguration;
-  done = true;
-  return cudaSuccess;
+cudaError_t tc_kernel_setup(int* nsm) {
+  static PerDevice pd;
+  return once_per_device(pd, nsm, [](int dev, int* sms) {
+    cudaError_t e =
+        cudaFuncSetAttribute(tc_fused_kernel<kDiv>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, tc_fused_kernel<kDiv>);
+    if (e != cudaSuccess) return e;
+    if (fa.numRegs < kRegsLaunch) return cudaErrorInvalidConfiguration;
+    return cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
+  });
 }
 }  // namespace
 
 cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st) {
   if (a.npts <= 0) return cudaSuccess;
   const bool div = a.out.divt || a.out.divt32;
-  cudaError_t e = div ? tc_kernel_setup<true>() : tc_kernel_setup<false>();
+  int nsm = 0;
+  cudaError_t e = div ? tc_kernel_setup<true>(&nsm) : tc_kernel_setup<false>(&nsm);
   if (e != cudaSuccess) return e;
-  static int nsm[64] = {0};
-  int dev = 0;
-  e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (!nsm[dev]) {
-    e = cudaDeviceGetAttribute(&nsm[dev], cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-  }
+  if (nsm <= 0) return cudaErrorInvalidDevice;
   const int64_t ntiles = (a.npts + kBlockM - 1) / kBlockM;
-  const unsigned grid = static_cast<unsigned>(std::min<int64_t>(ntiles, nsm[dev]));
+  const unsigned grid = static_cast<unsigned>(std::min<int64_t>(ntiles, nsm));
   auto kernel = div ? tc_fused_kernel<true> : tc_fused_kernel<false>;
   kernel<<<grid, kThreads, kSmemBytes, st>>>(
       *static_cast<const CUtensorMap*>(a.tmap_a_hi), *static_cast<const CUtensorMap*>(a.tmap_a_lo),

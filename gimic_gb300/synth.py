@@ -320,3 +320,26 @@ def make_workload(name, outdir, seed=2024, uhf=False, spherical=False):
     os.replace(xd_path + tmp, xd_path)
     os.replace(mol_path + tmp, mol_path)
     return mol_path, xd_path, mol
+
+
+def ring_bond_plane_input(mol, bond=(1, 2), height=8.0, reach=8.0, npts=60, order=10):
+    """gimic.inp text of the bond plane of the C6H6 workload: a Grid(bond)
+    Gauss-Lobatto plane (``npts`` x ``npts`` points, composite order
+    ``order``) through the midpoint of the C-C bond ``bond`` (1-based atom
+    numbers), perpendicular to it, from ``height`` Bohr below to ``height``
+    above the ring plane and from the ring centre to ``reach`` Bohr from it
+    outward; magnet_axis=z.  The ring centre is the mean of the carbon
+    positions; the width keyword is measured from the bond midpoint
+    (src/fgimic/grid.f90:165-276), so it starts at minus the centre-midpoint
+    distance."""
+    c = np.asarray(mol.coords, dtype=np.float64)
+    carbons = [i for i, s in enumerate(mol.symbols) if s == "C"]
+    centre = c[carbons].mean(axis=0)
+    a1, a2 = bond
+    mid = 0.5 * (c[a1 - 1] + c[a2 - 1])
+    dc = float(np.linalg.norm(mid - centre))
+    half = 0.5 * float(np.linalg.norm(c[a2 - 1] - c[a1 - 1]))
+    return ("calc=integral\nmagnet_axis=z\nGrid(bond) {\n type=lobatto\n bond=[%d,%d]\n fixcoord=[%r, %r, %r]\n"
+            " distance=%r\n height=[%r, %r]\n width=[%r, %r]\n grid_points=[%d, %d, 0]\n gauss_order=%d\n}\n"
+            % (a1, a2, float(centre[0]), float(centre[1]), float(centre[2]), half, -float(height), float(height),
+               -dc, float(reach) - dc, npts, npts, order))

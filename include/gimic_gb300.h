@@ -213,6 +213,24 @@ int gg_profile_read(const gg_ctx *ctx, double ms[GG_NPROF], int64_t launches[GG_
  * a dense contraction would have issued. */
 int gg_profile_blocks(const gg_ctx *ctx, int64_t *issued, int64_t *dense);
 
+/* Self-tests of the failure paths (no counterpart in the reference, whose
+ * Fortran stops the process on an error).  Every device-side wait of the
+ * library is bounded: on expiry the kernel records a code in the context's
+ * device error word and returns, and the next host check reports
+ * GG_ETIMEDOUT; the context stays usable.  Neither entry faults, traps or
+ * hangs the GPU.
+ * gg_selftest_wait_timeout: runs a one-thread kernel that waits on an
+ *   mbarrier nothing arrives at, with a limit of limit_ms (0 < limit_ms <=
+ *   2000), through the pipeline kernels' own wait routine; returns
+ *   GG_ETIMEDOUT (error code 100 in gg_last_error) and, when waited_ms is
+ *   given, the time the wait took.
+ * gg_selftest_fail_next: records `code` (nonzero) in the device error word,
+ *   as a failed wait of another thread would; the next evaluation's kernels
+ *   leave their pipelines without work and the call returns GG_ETIMEDOUT with
+ *   that code, after which the word is clear again. */
+int gg_selftest_wait_timeout(gg_ctx *ctx, double limit_ms, double *waited_ms, void *stream);
+int gg_selftest_fail_next(gg_ctx *ctx, int code);
+
 /* Integration proposal network (no counterpart in the reference, which
  * integrates on fixed grids, src/fgimic/integral.f90:50-511).  A 5 -> 64 ->
  * 64 -> 1 multilayer perceptron with SiLU activations predicts ln|j| at a
@@ -255,7 +273,11 @@ int gg_mlp_infer(const float *params, const float *x, int64_t n, float *y, void 
  * call allocates the device tables).  The first call on a device looks up the
  * array's address, so make it before any stream capture.  Every call reuses
  * the same array: calls that overlap on the GPU (other streams, other
- * contexts, other threads) race on it and must be serialised by the caller. */
+ * contexts, other threads) race on it and must be serialised by the caller.
+ * As on the other split-FP16 entry points nbf is at most 4096, and a plane
+ * pass queued with gg_plane_integrals_enqueue must be collected first.  With
+ * gg_profile on, its two kernels are timed as the basis and contraction
+ * groups and counted as dense (unscreened) GEMM blocks. */
 int gg_jtensor_batch_noalloc(gg_ctx *ctx, const double *pts, int64_t n, double *jt, double *rho, double *divt,
                              void *stream);
 

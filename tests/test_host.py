@@ -250,3 +250,69 @@ def test_shell_order_permutation(synth_dir):
         g.set_shell_order(2)
     g0 = api.Gimic(mp, xp, screening=0.0)
     assert g0.shell_order()[1] == list(range(g0.nshells))
+
+
+def test_density_injections_rejected_at_creation(tmp_path, c6h6, golden_dir):
+    """A non-finite density value, or an XDENS that holds more values than
+    the basis needs (a density of another basis, an open-shell file read as
+    closed shell), is an error when the context is created: the reference
+    would read past or stop short of the right blocks silently
+    (src/libgimic/dens.f90:72-131)."""
+    mp, xp, _ = c6h6
+    L = _lib.load()
+    lines = open(xp).read().splitlines()
+    nan = tmp_path / "nan.xdens"
+    bad = list(lines)
+    assert lines[0].strip() == ""  # the file opens with a blank record
+    bad[4321] = "NaN"  # the 4321st value
+    nan.write_text("\n".join(bad) + "\n")
+    rc, h = _ctx(mp, str(nan))
+    assert rc == -2 and not h.value and b"value 4321 is not finite" in L.gg_last_error(None)
+    inf = tmp_path / "inf.xdens"
+    bad = list(lines)
+    bad[17] = "-inf"
+    inf.write_text("\n".join(bad) + "\n")
+    rc, h = _ctx(mp, str(inf))
+    assert rc == -2 and b"not finite" in L.gg_last_error(None)
+    # one value too many: the density of a basis one function larger would
+    # hold far more, but a single extra value already shows the mismatch
+    extra = tmp_path / "extra.xdens"
+    extra.write_text("\n".join(lines + ["0.5"]) + "\n")
+    rc, h = _ctx(mp, str(extra))
+    assert rc == -2 and b"more values" in L.gg_last_error(None)
+    # the open-shell golden read as closed shell: the beta blocks are left over
+    d = golden_dir / "open-shell"
+    rc, h = _ctx(str(d / "MOL"), str(d / "XDENS"), uhf=False)
+    assert rc == -2 and b"more values" in L.gg_last_error(None)
+    rc, h = _ctx(str(d / "MOL"), str(d / "XDENS"), uhf=True)
+    assert rc == 0
+    L.gg_ctx_destroy(h)
+    # trailing blank lines are not data
+    blank = tmp_path / "blank.xdens"
+    blank.write_text("\n".join(lines) + "\n\n   \n")
+    rc, h = _ctx(mp, str(blank))
+    assert rc == 0
+    L.gg_ctx_destroy(h)
+
+
+def test_zero_field_rejected_before_compute(c6h6):
+    """A zero magnetic field stops the reference's driver ("Magnetic field is
+    zero, not wasting more CPU.", src/fgimic/magnet.f90:56-59); the plane
+    integrals and jvector evaluation refuse it before any device work, the
+    driver's grid set-up raises it, and the reference C ABI keeps its
+    behaviour (no stop there)."""
+    mp, xp, mol = c6h6
+    g = api.Gimic(mp, xp, screening=1e-8)
+    assert np.all(g.get_magnet() == 0.0)
+    ax = (np.array([0.0, 1.0]), np.array([0.5, 0.5]))
+    with pytest.raises(_lib.GimicError, match="Magnetic field is zero"):
+        g.plane_integral(np.zeros(3), np.eye(3), (ax, ax, (np.zeros(1), np.ones(1))))
+    jv = np.zeros((1, 3))
+    rc = g._L.gg_jvector_batch(g._h, C.c_void_p(np.zeros((1, 3)).ctypes.data), 1, C.c_void_p(jv.ctypes.data), None)
+    assert rc == -1 and b"Magnetic field is zero" in g._L.gg_last_error(g._h)
+    text = ("calc=integral\nmagnet=[0.0, 0.0, 0.0]\nGrid(bond) {\n type=gauss\n bond=[1,2]\n fixcoord=[0.0,0.0,0.0]\n"
+            " distance=1.0\n height=[-2.0, 2.0]\n width=[-2.0, 2.0]\n grid_points=[9, 9, 0]\n gauss_order=9\n}\n")
+    i = ginp.read(text, is_text=True)
+    grd = ggrid.new_grid(i, mol.coords)
+    with pytest.raises(ValueError, match="Magnetic field is zero"):
+        ggrid.get_magnet(grd, i)
