@@ -670,12 +670,28 @@ def main():
     bb, _ = ggrid.get_magnet(grd, pin)
     g1.set_magnet(bb)
     res = g1.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)
-    reps = 200
+    reps = 300
+    # through the C ABI (gg_plane_integral, one blocking call per plane) ...
+    import ctypes as C
+    from gimic_gb300 import _lib
+
+    specs, keep = api._grid_records([(grd.origin, grd.basv, grd.axes(), grd.radius)])
+    sp = specs.ctypes.data_as(C.POINTER(_lib.GridSpec))
+    pout = np.zeros(7)
+    pop = pout.ctypes.data_as(C.POINTER(C.c_double))
+    for _ in range(3):
+        _lib.check(g1._L.gg_plane_integral(g1._h, sp, pop, None), g1._h)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for _ in range(reps):
-        g1.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)
+        g1._L.gg_plane_integral(g1._h, sp, pop, None)
     plane_s = (time.perf_counter() - t0) / reps
+    assert pout[0] == res["current"][0]
+    # ... and through the Python API (Gimic.plane_integral)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        g1.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)
+    plane_py_s = (time.perf_counter() - t0) / reps
 
     # ---- plain FP64 GPU path on a subset (the 10x reference point) --------
     g64 = api.Gimic(mp, xp, screening=1e-8, precision="fp64")
@@ -708,7 +724,10 @@ def main():
         "plane_integrals_per_s": 1.0 / plane_s,
         "plane": {"workload": "C6H6 (nbf %d) bond plane through the C1-C2 midpoint: 60x60 Gauss-Lobatto (order 10), "
                               "height -8..8 Bohr, from the ring centre to 8 Bohr outward, B along z" % mol1.nbf,
-                  "points": int(np.prod(grd.npts)), "what": "one gg_plane_integral call per plane, host wall time",
+                  "points": int(np.prod(grd.npts)),
+                  "what": "one blocking gg_plane_integral call per plane through the C ABI, host wall time "
+                          "(replayed as a CUDA graph after the first calls)",
+                  "python_api_per_s": 1.0 / plane_py_s,
                   "current_nAT": api.au2si(res["current"][0]), "modulus_nAT": api.au2si(res["modulus"][0]),
                   "acid_nAT": api.au2si(res["acid"]), "abs_err_vs_fp64_oracle_nAT": plane_err},
         "fp64_gpu_points_per_s": fp64_pts_s,

@@ -280,6 +280,22 @@ def _grid_records(planes):
     of axis points and weights they point into (keep it referenced until the
     library call returns)."""
     n = len(planes)
+    if n <= 4:
+        # a few planes: the records point straight into the callers' axis
+        # arrays (half the time of the concatenation below for one plane)
+        specs = np.zeros(n, dtype=_GRID_DTYPE)
+        keep = []
+        for q, (origin, basv, axes, radius) in enumerate(planes):
+            arrs = [np.ascontiguousarray(v, dtype=np.float64).reshape(-1) for ax in axes for v in ax]
+            keep.append(arrs)
+            addr = [a.__array_interface__["data"][0] for a in arrs]
+            specs["origin"][q] = origin
+            specs["basv"][q] = np.asarray(basv, dtype=np.float64).T.reshape(9)
+            specs["npts"][q] = (arrs[0].shape[0], arrs[2].shape[0], arrs[4].shape[0])
+            specs["pts"][q] = (addr[0], addr[2], addr[4])
+            specs["wgt"][q] = (addr[1], addr[3], addr[5])
+            specs["radius"][q] = radius
+        return specs, keep
     # the gg_grid records are filled as one numpy structured array (a
     # per-field ctypes loop cost about 25 us per plane); the axis
     # arrays are concatenated, and the records point into that buffer

@@ -25,21 +25,26 @@ thread_local std::string g_create_error;
 
 constexpr int kSelftestWaitCode = 100;  // error code of the wait self-test
 
-// Device buffer that grows on demand.
+// Device buffer that grows on demand.  Every move of the buffer bumps the
+// owner's generation counter (*gen), which tells a captured CUDA graph that
+// the addresses it holds are stale.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  uint64_t* gen = nullptr;
   cudaError_t reserve(size_t n) {
     if (n <= bytes) return cudaSuccess;
     if (p) cudaFree(p);
     p = nullptr;
     bytes = 0;
+    if (gen) ++*gen;
     cudaError_t e = cudaMalloc(&p, n);
     if (e == cudaSuccess) bytes = n;
     return e;
   }
   void release() {
     if (p) cudaFree(p);
+    if (p && gen) ++*gen;
     p = nullptr;
     bytes = 0;
   }
@@ -136,6 +141,7 @@ struct gg_ctx {
   // scratch
   DevBuf pts, jt, rho, divt, jv;
   DevBuf tile_ctr;  // tile queue counter of the contraction kernel
+  DevBuf tc_part, tc_done;  // partial sums and counters of the chunk split
   // Per-batch scratch of the split path.  Two slots let the ordering,
   // screening and basis evaluation of batch b+1 (on the auxiliary stream) run
   // while the contraction of batch b runs on the caller's stream.
@@ -161,8 +167,22 @@ struct gg_ctx {
   DevBuf phi, gx, gy, gz, lap, w64;
   DevBuf plane_rows, plane_out;
   DevBuf diag;  // the wait self-test's measured time
-  void* plane_host = nullptr;  // pinned staging of the plane uploads
+  void* plane_host = nullptr;  // pinned staging of the plane uploads, then the sums and the error word
   size_t plane_host_bytes = 0;
+  // Generation of everything a captured graph holds by address or by value:
+  // device buffers (DevBuf::gen), tables, matrices and kernel flags.
+  uint64_t gen = 1;
+  // The blocking plane pass as a CUDA graph: captured on the second pass
+  // with the same layout and generation, replayed while both stay the same.
+  struct PlaneGraph {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t sig[7] = {0, 0, 0, 0, 0, 0, 0};
+    bool seen = false;    // an eager pass ran with this signature
+    bool failed = false;  // capture failed for this signature: stay eager
+    int64_t launches = 0; // kernels in the graph
+  } pgraph;
+  cudaStream_t cap_stream = nullptr;  // the capture stream (the caller's may be the legacy stream)
+  int nsm = 0;                        // SMs of the device
   // a queued plane pass (gg_plane_integrals_enqueue until _collect)
   bool plane_pending = false;
   int plane_n = 0;
@@ -216,7 +236,29 @@ struct gg_ctx {
     prof.used = 0;
   }
 
+  std::vector<DevBuf*> buffers() {
+    std::vector<DevBuf*> v = {&b_fp64, &b_hi, &b_lo, &inv_col, &pts, &jt, &rho, &divt, &jv, &phi, &gx, &gy, &gz,
+                              &lap, &w64, &plane_rows, &plane_out, &pts2, &jt2, &rho2, &divt2, &tile_ctr, &diag,
+                              &tc_part, &tc_done};
+    for (SplitSlot& sl : slot)
+      for (DevBuf* b : {&sl.a_hi, &sl.a_lo, &sl.inv_row, &sl.sort_keys, &sl.sort_keys2, &sl.sort_idx, &sl.sort_perm,
+                        &sl.sort_temp, &sl.pts_sorted, &sl.tile_lists, &sl.tile_ord})
+        v.push_back(b);
+    return v;
+  }
+
+  gg_ctx() {
+    for (DevBuf* b : buffers()) b->gen = &gen;
+  }
+
+  void drop_graph() {
+    if (pgraph.exec) cudaGraphExecDestroy(pgraph.exec);
+    pgraph = PlaneGraph{};
+  }
+
   ~gg_ctx() {
+    drop_graph();
+    if (cap_stream) cudaStreamDestroy(cap_stream);
     for (int i = 0; i < 2; ++i)
       for (cudaEvent_t ev : {ev_in[i], ev_done[i], ev_out[i]})
         if (ev) cudaEventDestroy(ev);
@@ -241,18 +283,12 @@ struct gg_ctx {
     for (void* p : table_allocs) cudaFree(p);
     table_allocs.clear();
     tables_ready = false;
-    for (DevBuf* b : {&b_fp64, &b_hi, &b_lo, &inv_col, &pts, &jt, &rho, &divt, &jv, &phi, &gx, &gy, &gz, &lap, &w64,
-                      &plane_rows, &plane_out, &pts2, &jt2, &rho2, &divt2, &tile_ctr, &diag})
-      b->release();
-    for (SplitSlot& sl : slot) {
-      for (DevBuf* b : {&sl.a_hi, &sl.a_lo, &sl.inv_row, &sl.sort_keys, &sl.sort_keys2, &sl.sort_idx, &sl.sort_perm,
-                        &sl.sort_temp, &sl.pts_sorted, &sl.tile_lists, &sl.tile_ord})
-        b->release();
-      sl.used = false;
-    }
+    for (DevBuf* b : buffers()) b->release();
+    for (SplitSlot& sl : slot) sl.used = false;
     if (d_err) cudaFree(d_err);
     d_err = nullptr;
     mats_spin = -1;
+    ++gen;
   }
 
   // get_magnet stops on a zero field (src/fgimic/magnet.f90:56-59)
@@ -422,6 +458,7 @@ struct gg_ctx {
     if (rc) return rc;
     dB = d;
     tables_ready = true;
+    ++gen;
     return GG_OK;
   }
 
@@ -544,6 +581,7 @@ struct gg_ctx {
     }
     mats_spin = spin;
     mats_prec = precision;
+    ++gen;
     return GG_OK;
   }
 
@@ -590,6 +628,10 @@ struct gg_ctx {
   int prepare() {
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    if (!nsm) {
+      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+      if (e != cudaSuccess) return cuda_fail(e, "SM count");
+    }
     int rc = build_tables();
     if (rc) return rc;
     return build_matrices();
@@ -600,7 +642,9 @@ struct gg_ctx {
     return run_batch(d_pts, n, gg::Outputs{d_jt, d_rho, d_divt}, st);
   }
 
-  int run_batch(const double* d_pts, int64_t n, gg::Outputs out, cudaStream_t st) {
+  // coherent: consecutive points are close to each other (plane rows), so
+  // a pass with no more tiles than SMs is screened without the spatial sort
+  int run_batch(const double* d_pts, int64_t n, gg::Outputs out, cudaStream_t st, bool coherent = false) {
     if (n <= 0) return GG_OK;
     if ((out.divt || out.divt32) && !(flags.giao && flags.dia && flags.para))
       return fail(GG_EUNSUPPORTED, "div j needs GIAO, diamagnetic and paramagnetic terms on");
@@ -632,7 +676,7 @@ struct gg_ctx {
     if (dB.kpad > 64 * gg::kBlockK)
       return fail(GG_EUNSUPPORTED, "the split-FP16 path handles at most 4096 basis functions (nbf=" +
                                        std::to_string(basis.nbf) + "); use the FP64 precision");
-    int rc = prep_split(slot[0], d_pts, n, st);
+    int rc = prep_split(slot[0], d_pts, n, st, coherent);
     if (rc) return rc;
     rc = tc_split(slot[0], out, st);
     if (rc == GG_OK) slot[0].used = false;  // ordered on `st` itself
@@ -640,7 +684,7 @@ struct gg_ctx {
   }
 
   // Ordering, tile screening and basis evaluation of one batch into a slot.
-  int prep_split(SplitSlot& sl, const double* d_pts, int64_t n, cudaStream_t st) {
+  int prep_split(SplitSlot& sl, const double* d_pts, int64_t n, cudaStream_t st, bool coherent = false) {
     cudaError_t e;
     const size_t abytes = static_cast<size_t>(n) * dB.kpad * sizeof(__half);
     e = sl.a_hi.reserve(abytes);
@@ -670,28 +714,39 @@ struct gg_ctx {
       if (e == cudaSuccess) e = sl.tile_lists.reserve(static_cast<size_t>(ntiles) * stride * sizeof(int));
       if (e == cudaSuccess) e = sl.tile_ord.reserve(static_cast<size_t>(ntiles) * sizeof(int));
       if (e != cudaSuccess) return cuda_fail(e, "tile-screening scratch");
-      double lo[3] = {0, 0, 0};
-      for (const gg::Atom& a : basis.atoms)
-        for (int d = 0; d < 3; ++d) lo[d] += a.coord[d] / static_cast<double>(basis.atoms.size());
-      for (int d = 0; d < 3; ++d) lo[d] -= 64.0;  // 1024 cells of 0.125 Bohr around the molecule
+      // every tile gets an SM of its own at once: no tile ordering, and
+      // points that come in coherent runs need no spatial sort either
+      const bool few = nsm > 0 && ntiles <= nsm;
+      const bool sort = !(few && coherent);
       prof_begin(GG_PROF_ORDER, st, &ps);
-      e = gg::launch_spatial_order(d_pts, n, lo, 0.125, sl.sort_keys.as<uint32_t>(), sl.sort_keys2.as<uint32_t>(),
-                                   sl.sort_idx.as<int>(), sl.sort_perm.as<int>(), sl.sort_temp.p, tb,
-                                   sl.pts_sorted.as<double>(), st);
-      if (e != cudaSuccess) return cuda_fail(e, "spatial ordering");
-      gg::launch_tile_screen(dB, sl.pts_sorted.as<double>(), n, sl.tile_lists.as<int>(), st);
-      // heaviest tiles first; the key/index scratch of the point sort is reused
-      e = gg::launch_tile_order(sl.tile_lists.as<int>(), ntiles, stride, sl.sort_keys.as<uint32_t>(),
-                                sl.sort_keys2.as<uint32_t>(), sl.sort_idx.as<int>(), sl.tile_ord.as<int>(),
-                                sl.sort_temp.p, tb, st);
-      if (e != cudaSuccess) return cuda_fail(e, "tile ordering");
+      if (sort) {
+        double lo[3] = {0, 0, 0};
+        for (const gg::Atom& a : basis.atoms)
+          for (int d = 0; d < 3; ++d) lo[d] += a.coord[d] / static_cast<double>(basis.atoms.size());
+        for (int d = 0; d < 3; ++d) lo[d] -= 64.0;  // 1024 cells of 0.125 Bohr around the molecule
+        e = gg::launch_spatial_order(d_pts, n, lo, 0.125, sl.sort_keys.as<uint32_t>(), sl.sort_keys2.as<uint32_t>(),
+                                     sl.sort_idx.as<int>(), sl.sort_perm.as<int>(), sl.sort_temp.p, tb,
+                                     sl.pts_sorted.as<double>(), st);
+        if (e != cudaSuccess) return cuda_fail(e, "spatial ordering");
+        launches += 3;
+      }
+      const double* tpts = sort ? sl.pts_sorted.as<double>() : d_pts;
+      gg::launch_tile_screen(dB, tpts, n, sl.tile_lists.as<int>(), st);
+      // heaviest tiles first (the key/index scratch of the point sort is reused)
+      const bool order = !few;
+      if (order) {
+        e = gg::launch_tile_order(sl.tile_lists.as<int>(), ntiles, stride, sl.sort_keys.as<uint32_t>(),
+                                  sl.sort_keys2.as<uint32_t>(), sl.sort_idx.as<int>(), sl.tile_ord.as<int>(),
+                                  sl.sort_temp.p, tb, st);
+        if (e != cudaSuccess) return cuda_fail(e, "tile ordering");
+      }
       prof_end(st, ps);
       if (prof.on && prof.d_blocks) gg::launch_tile_work(sl.tile_lists.as<int>(), ntiles, stride, prof.d_blocks, st);
-      launches += 6;
-      sl.tp = sl.pts_sorted.as<double>();
+      launches += order ? 3 : 1;
+      sl.tp = tpts;
       sl.tiles = sl.tile_lists.as<int>();
-      sl.perm = sl.sort_perm.as<int>();
-      sl.tord = sl.tile_ord.as<int>();
+      sl.perm = sort ? sl.sort_perm.as<int>() : nullptr;
+      sl.tord = order ? sl.tile_ord.as<int>() : nullptr;
     }
     if (!encode_fp16_2d(&sl.tma_hi, sl.a_hi.p, n, dB.kpad, gg::kBlockM) ||
         !encode_fp16_2d(&sl.tma_lo, sl.a_lo.p, n, dB.kpad, gg::kBlockM) ||
@@ -724,6 +779,21 @@ struct gg_ctx {
     if (e == cudaSuccess) e = cudaMemsetAsync(tile_ctr.p, 0, sizeof(int), st);
     if (e != cudaSuccess) return cuda_fail(e, "tile queue");
     ta.tile_counter = tile_ctr.as<int>();
+    // A short pass (no more tiles than SMs) would leave most SMs idle while
+    // each works through its tile's chunks one after the other: split every
+    // tile's chunks over steps of their own, whose partial sums the last
+    // step of each quarter tile adds in chunk order.  All short passes thus
+    // give the same results point by point, whatever their size.
+    const int64_t ntiles = (sl.n + gg::kBlockM - 1) / gg::kBlockM;
+    if (nsm > 0 && ntiles <= nsm && dB.nchunk > 1 && ntiles * dB.nchunk <= 8192) {
+      ta.csplit = dB.nchunk;
+      e = tc_part.reserve(static_cast<size_t>(ntiles) * dB.nchunk * gg::kNDots * gg::kBlockM * sizeof(float2));
+      if (e == cudaSuccess) e = tc_done.reserve(static_cast<size_t>(ntiles) * 4 * sizeof(unsigned));
+      if (e == cudaSuccess) e = cudaMemsetAsync(tc_done.p, 0, static_cast<size_t>(ntiles) * 4 * sizeof(unsigned), st);
+      if (e != cudaSuccess) return cuda_fail(e, "chunk-split scratch");
+      ta.part = tc_part.as<float2>();
+      ta.tile_done = tc_done.as<unsigned>();
+    }
     size_t ps = 0;
     prof_begin(GG_PROF_TC, st, &ps);
     e = gg::launch_tc_fused(dB, ta, st);
@@ -738,7 +808,7 @@ struct gg_ctx {
   // after the previous contraction of the same slot) and the contraction on
   // `st`, so batch b+1 is prepared while batch b is contracted.
   int pipe_batch(int b, const double* d_pts, int64_t n, gg::Outputs out, cudaStream_t st,
-                 cudaEvent_t input_ready = nullptr) {
+                 cudaEvent_t input_ready = nullptr, bool coherent = false) {
     cudaError_t e = cudaSuccess;
     if (precision == GG_PREC_FP64) {
       if (input_ready) e = cudaStreamWaitEvent(st, input_ready, 0);
@@ -761,7 +831,7 @@ struct gg_ctx {
     if (e == cudaSuccess) e = cudaEventRecord(sl.prepared, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(aux_stream, sl.prepared, 0);
     if (e != cudaSuccess) return cuda_fail(e, "batch pipeline");
-    int rc = prep_split(sl, d_pts, n, aux_stream);
+    int rc = prep_split(sl, d_pts, n, aux_stream, coherent);
     if (rc) return rc;
     e = cudaEventRecord(sl.prepared, aux_stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st, sl.prepared, 0);
@@ -1036,6 +1106,7 @@ int gg_set_flags(gg_ctx* ctx, int giao, int dia, int para) {
   std::lock_guard<std::mutex> g(ctx->mu);
   if (!dia && !para) return ctx->fail(GG_EINVAL, "both diamagnetic and paramagnetic contributions switched off");
   ctx->flags = gg::Flags{giao != 0, dia != 0, para != 0};
+  ++ctx->gen;
   return GG_OK;
 }
 
@@ -1044,6 +1115,7 @@ int gg_set_precision(gg_ctx* ctx, int mode) {
   std::lock_guard<std::mutex> g(ctx->mu);
   if (mode != GG_PREC_FP64 && mode != GG_PREC_SPLIT16) return ctx->fail(GG_EINVAL, "unknown precision mode");
   ctx->precision = mode;
+  ++ctx->gen;
   return GG_OK;
 }
 
@@ -1051,6 +1123,7 @@ int gg_set_tile_screening(gg_ctx* ctx, int enable) {
   if (!ctx) return GG_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   ctx->tile_screening = enable != 0;
+  ++ctx->gen;
   return GG_OK;
 }
 
@@ -1058,6 +1131,7 @@ int gg_set_max_batch(gg_ctx* ctx, int64_t npts) {
   if (!ctx || npts < 128) return GG_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   ctx->max_batch = npts;
+  ++ctx->gen;
   return GG_OK;
 }
 
@@ -1165,12 +1239,24 @@ int gg_jvector_batch(gg_ctx* ctx, const double* pts, int64_t n, double* jv, void
   return GG_OK;
 }
 
-// Everything of a plane-integral pass up to and including the reduction,
-// queued on `st` without waiting: the nplanes x 7 sums are left in the
-// context's device scratch at *d_result.  The caller holds ctx->mu.
-static int plane_enqueue(gg_ctx* ctx, const gg_grid* grids, int nplanes, cudaStream_t st, const double** d_result) {
+// Layout of a plane pass in the context's scratch: [descs | weights | axis
+// points | row -> plane | field] uploaded in one copy from pinned staging,
+// then [row partials | plane sums] on the device; the pinned staging ends
+// with room for the sums and the error word copied back.
+struct PlanePass {
+  int nplanes = 0;
+  int64_t npts = 0, nrows = 0, nw = 0;
+  size_t o_w = 0, o_x = 0, o_rp = 0, o_bb = 0, upload = 0, o_row = 0, o_out = 0, o_done = 0, aux = 0;
+  size_t h_out = 0, h_err = 0;  // offsets of the sums and the error word in the pinned staging
+};
+
+// Host part of a plane pass: checks, the staging contents, device tables
+// and scratch.  Nothing is queued on a stream.  The caller holds ctx->mu.
+static int plane_stage(gg_ctx* ctx, const gg_grid* grids, int nplanes, PlanePass* pp) {
   if (!grids || nplanes <= 0) return GG_EINVAL;
   if (ctx->zero_field()) return ctx->fail(GG_EINVAL, "Magnetic field is zero, not wasting more CPU.");
+  PlanePass& P = *pp;
+  P.nplanes = nplanes;
   int64_t npts = 0, nrows = 0, nw = 0;
   for (int q = 0; q < nplanes; ++q) {
     const gg_grid& gr = grids[q];
@@ -1181,23 +1267,55 @@ static int plane_enqueue(gg_ctx* ctx, const gg_grid* grids, int nplanes, cudaStr
     nrows += static_cast<int64_t>(gr.npts[1]) * gr.npts[2];
     nw += gr.npts[0] + gr.npts[1] + gr.npts[2];
   }
-  // points r(i,j,k) = origin + x1_i basv1 + x2_j basv2 + x3_k basv3, i fastest
-  // (gridpoint, src/fgimic/grid.f90:498-511), generated on the device from
-  // the axis coordinates; centre as grid_center (:529-541)
-  std::vector<double> hw(static_cast<size_t>(nw)), hx(static_cast<size_t>(nw));
-  std::vector<gg::PlaneDesc> desc(nplanes);
-  std::vector<int> row_plane(static_cast<size_t>(nrows));
+  P.npts = npts;
+  P.nrows = nrows;
+  P.nw = nw;
+  int rc = ctx->prepare();
+  if (rc) return rc;
+  auto up8 = [](size_t x) { return (x + 7) & ~static_cast<size_t>(7); };
+  P.o_w = up8(static_cast<size_t>(nplanes) * sizeof(gg::PlaneDesc));
+  P.o_x = P.o_w + static_cast<size_t>(nw) * sizeof(double);
+  P.o_rp = P.o_x + static_cast<size_t>(nw) * sizeof(double);
+  P.o_bb = up8(P.o_rp + static_cast<size_t>(nrows) * sizeof(int));
+  P.upload = P.o_bb + 3 * sizeof(double);
+  P.o_row = up8(P.upload);
+  P.o_out = P.o_row + static_cast<size_t>(nrows) * 7 * sizeof(double);
+  P.o_done = P.o_out + static_cast<size_t>(nplanes) * 7 * sizeof(double);
+  P.aux = P.o_done + static_cast<size_t>(nplanes) * sizeof(unsigned);
+  P.h_out = P.o_row;
+  P.h_err = P.h_out + static_cast<size_t>(nplanes) * 7 * sizeof(double);
+  const size_t host_bytes = P.h_err + 8;
+  cudaError_t e = ctx->pts.reserve(static_cast<size_t>(npts) * 3 * sizeof(double));
+  if (e == cudaSuccess) e = ctx->jt.reserve(static_cast<size_t>(npts) * 9 * sizeof(double));
+  if (e == cudaSuccess) e = ctx->plane_rows.reserve(P.aux);
+  if (e == cudaSuccess && ctx->plane_host_bytes < host_bytes) {
+    if (ctx->plane_host) cudaFreeHost(ctx->plane_host);
+    ctx->plane_host = nullptr;
+    ctx->plane_host_bytes = 0;
+    ++ctx->gen;
+    e = cudaMallocHost(&ctx->plane_host, host_bytes);
+    if (e == cudaSuccess) ctx->plane_host_bytes = host_bytes;
+  }
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "plane scratch");
+  // points r(i,j,k) = origin + x1_i basv1 + x2_j basv2 + x3_k basv3, i
+  // fastest (gridpoint, src/fgimic/grid.f90:498-511), generated on the
+  // device from the axis coordinates; centre as grid_center (:529-541)
+  char* hb = static_cast<char*>(ctx->plane_host);
+  gg::PlaneDesc* desc = reinterpret_cast<gg::PlaneDesc*>(hb);
+  double* hw = reinterpret_cast<double*>(hb + P.o_w);
+  double* hx = reinterpret_cast<double*>(hb + P.o_x);
+  int* row_plane = reinterpret_cast<int*>(hb + P.o_rp);
   int64_t po = 0, ro = 0, wo = 0;
   for (int q = 0; q < nplanes; ++q) {
     const gg_grid& gr = grids[q];
     const int p1 = gr.npts[0], p2 = gr.npts[1], p3 = gr.npts[2];
-    std::copy(gr.wgt[0], gr.wgt[0] + p1, hw.begin() + wo);
-    std::copy(gr.wgt[1], gr.wgt[1] + p2, hw.begin() + wo + p1);
-    std::copy(gr.wgt[2], gr.wgt[2] + p3, hw.begin() + wo + p1 + p2);
-    std::copy(gr.pts[0], gr.pts[0] + p1, hx.begin() + wo);
-    std::copy(gr.pts[1], gr.pts[1] + p2, hx.begin() + wo + p1);
-    std::copy(gr.pts[2], gr.pts[2] + p3, hx.begin() + wo + p1 + p2);
-    gg::PlaneDesc& d = desc[q];
+    std::copy(gr.wgt[0], gr.wgt[0] + p1, hw + wo);
+    std::copy(gr.wgt[1], gr.wgt[1] + p2, hw + wo + p1);
+    std::copy(gr.wgt[2], gr.wgt[2] + p3, hw + wo + p1 + p2);
+    std::copy(gr.pts[0], gr.pts[0] + p1, hx + wo);
+    std::copy(gr.pts[1], gr.pts[1] + p2, hx + wo + p1);
+    std::copy(gr.pts[2], gr.pts[2] + p3, hx + wo + p1 + p2);
+    gg::PlaneDesc d{};
     d.x_off = static_cast<int>(wo);
     for (int c = 0; c < 3; ++c) d.origin[c] = gr.origin[c];
     for (int c = 0; c < 9; ++c) d.basv[c] = gr.basv[c];
@@ -1216,81 +1334,146 @@ static int plane_enqueue(gg_ctx* ctx, const gg_grid* grids, int nplanes, cudaStr
       d.normal[c] = gr.basv[6 + c];
     }
     d.radius = gr.radius;
-    for (int64_t r = 0; r < static_cast<int64_t>(p2) * p3; ++r) row_plane[ro + r] = q;
+    std::memcpy(desc + q, &d, sizeof(d));
+    std::fill(row_plane + ro, row_plane + ro + static_cast<int64_t>(p2) * p3, q);
     po += static_cast<int64_t>(p1) * p2 * p3;
     ro += static_cast<int64_t>(p2) * p3;
     wo += p1 + p2 + p3;
   }
-  int rc = ctx->prepare();
-  if (rc) return rc;
-  // device layout: [descs | weights | axis points | row -> plane] uploaded in
-  // one copy from pinned staging, then [row partials | plane sums]
-  auto up8 = [](size_t x) { return (x + 7) & ~static_cast<size_t>(7); };
-  const size_t o_w = up8(desc.size() * sizeof(gg::PlaneDesc));
-  const size_t o_x = o_w + hw.size() * sizeof(double);
-  const size_t o_rp = o_x + hx.size() * sizeof(double);
-  const size_t upload = o_rp + row_plane.size() * sizeof(int);
-  const size_t o_row = up8(upload);
-  const size_t o_out = o_row + static_cast<size_t>(nrows) * 7 * sizeof(double);
-  const size_t aux = o_out + static_cast<size_t>(nplanes) * 7 * sizeof(double);
-  cudaError_t e = ctx->pts.reserve(static_cast<size_t>(npts) * 3 * sizeof(double));
-  if (e == cudaSuccess) e = ctx->jt.reserve(static_cast<size_t>(npts) * 9 * sizeof(double));
-  if (e == cudaSuccess) e = ctx->plane_rows.reserve(aux);
-  if (e == cudaSuccess && ctx->plane_host_bytes < upload) {
-    if (ctx->plane_host) cudaFreeHost(ctx->plane_host);
-    ctx->plane_host = nullptr;
-    ctx->plane_host_bytes = 0;
-    e = cudaMallocHost(&ctx->plane_host, upload);
-    if (e == cudaSuccess) ctx->plane_host_bytes = upload;
-  }
-  if (e != cudaSuccess) return ctx->cuda_fail(e, "plane scratch");
+  std::memcpy(hb + P.o_bb, ctx->magnet, 3 * sizeof(double));
+  return GG_OK;
+}
+
+// Device part of a plane pass, queued on `st` without waiting: upload,
+// points, evaluation, reduction; the nplanes x 7 sums stay in the context's
+// scratch at *d_result.  The caller holds ctx->mu.
+static int plane_launch(gg_ctx* ctx, const PlanePass& P, cudaStream_t st, const double** d_result) {
   char* hb = static_cast<char*>(ctx->plane_host);
-  std::memcpy(hb, desc.data(), desc.size() * sizeof(gg::PlaneDesc));
-  std::memcpy(hb + o_w, hw.data(), hw.size() * sizeof(double));
-  std::memcpy(hb + o_x, hx.data(), hx.size() * sizeof(double));
-  std::memcpy(hb + o_rp, row_plane.data(), row_plane.size() * sizeof(int));
   char* ab = ctx->plane_rows.as<char>();
-  gg::PlaneDesc* ddesc = reinterpret_cast<gg::PlaneDesc*>(ab);
-  double* dw = reinterpret_cast<double*>(ab + o_w);
-  double* dx = reinterpret_cast<double*>(ab + o_x);
-  int* drp = reinterpret_cast<int*>(ab + o_rp);
-  double* drow = reinterpret_cast<double*>(ab + o_row);
-  double* dout = reinterpret_cast<double*>(ab + o_out);
-  e = cudaMemcpyAsync(ab, hb, upload, cudaMemcpyHostToDevice, st);
+  const gg::PlaneDesc* ddesc = reinterpret_cast<const gg::PlaneDesc*>(ab);
+  const double* dw = reinterpret_cast<const double*>(ab + P.o_w);
+  const double* dx = reinterpret_cast<const double*>(ab + P.o_x);
+  const int* drp = reinterpret_cast<const int*>(ab + P.o_rp);
+  const double* dbb = reinterpret_cast<const double*>(ab + P.o_bb);
+  double* drow = reinterpret_cast<double*>(ab + P.o_row);
+  double* dout = reinterpret_cast<double*>(ab + P.o_out);
+  unsigned* ddone = reinterpret_cast<unsigned*>(ab + P.o_done);
+  cudaError_t e = cudaMemcpyAsync(ab, hb, P.upload, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ddone, 0, static_cast<size_t>(P.nplanes) * sizeof(unsigned), st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane axes");
-  gg::launch_plane_points(dx, ddesc, drp, nrows, ctx->pts.as<double>(), st);
+  gg::launch_plane_points(dx, ddesc, drp, P.nrows, ctx->pts.as<double>(), st);
   ctx->launches += 1;
   const int64_t batch = ctx->batch_points();
-  for (int64_t off = 0, b = 0; off < npts; off += batch, ++b) {
-    const int64_t m = std::min(batch, npts - off);
+  for (int64_t off = 0, b = 0; off < P.npts; off += batch, ++b) {
+    const int64_t m = std::min(batch, P.npts - off);
     const gg::Outputs out{ctx->jt.as<double>() + 9 * off, nullptr, nullptr};
-    rc = npts > batch ? ctx->pipe_batch(static_cast<int>(b), ctx->pts.as<double>() + 3 * off, m, out, st)
-                      : ctx->run_batch(ctx->pts.as<double>() + 3 * off, m, out, st);
+    // plane points come row by row: tiles of consecutive points are compact
+    // enough to skip the spatial sort when every tile has an SM of its own
+    const int rc = P.npts > batch
+                       ? ctx->pipe_batch(static_cast<int>(b), ctx->pts.as<double>() + 3 * off, m, out, st, nullptr, true)
+                       : ctx->run_batch(ctx->pts.as<double>() + 3 * off, m, out, st, true);
     if (rc) return rc;
   }
   size_t slot = 0;
   ctx->prof_begin(GG_PROF_PLANE, st, &slot);
-  gg::launch_plane_batch(ctx->jt.as<double>(), ctx->pts.as<double>(), dw, ddesc, nplanes, drp, nrows, ctx->magnet,
-                         drow, dout, st);
+  gg::launch_plane_batch(ctx->jt.as<double>(), ctx->pts.as<double>(), dw, ddesc, P.nplanes, drp, P.nrows, dbb, drow,
+                         dout, ddone, st);
   ctx->prof_end(st, slot);
-  ctx->launches += 2;
+  ctx->launches += 1;
   e = cudaGetLastError();
   if (e != cudaSuccess) return ctx->cuda_fail(e, "plane reduction launch");
   *d_result = dout;
   return GG_OK;
 }
 
+// The sums and the error word back into the pinned staging.
+static int plane_readback(gg_ctx* ctx, const PlanePass& P, const double* dout, cudaStream_t st) {
+  char* hb = static_cast<char*>(ctx->plane_host);
+  cudaError_t e = cudaMemcpyAsync(hb + P.h_out, dout, static_cast<size_t>(P.nplanes) * 7 * sizeof(double),
+                                  cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hb + P.h_err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+  return e == cudaSuccess ? GG_OK : ctx->cuda_fail(e, "copying plane result");
+}
+
+// Captures the device part and the read-back of a plane pass as a graph on
+// the context's capture stream; on any failure the capture is abandoned and
+// the caller runs the pass eagerly.
+static bool plane_capture(gg_ctx* ctx, const PlanePass& P) {
+  cudaError_t e = cudaSuccess;
+  if (!ctx->cap_stream) e = cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return false;
+  const uint64_t gen0 = ctx->gen;
+  const int64_t launches0 = ctx->launches;
+  if (cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+  const double* dout = nullptr;
+  int rc = plane_launch(ctx, P, ctx->cap_stream, &dout);
+  if (rc == GG_OK) rc = plane_readback(ctx, P, dout, ctx->cap_stream);
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(ctx->cap_stream, &graph);
+  bool ok = rc == GG_OK && e == cudaSuccess && graph && ctx->gen == gen0;
+  cudaGraphExec_t exec = nullptr;
+  if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+  if (graph) cudaGraphDestroy(graph);
+  cudaGetLastError();
+  const int64_t in_graph = ctx->launches - launches0;
+  ctx->launches = launches0;  // counted when the graph runs
+  if (!ok) {
+    if (exec) cudaGraphExecDestroy(exec);
+    return false;
+  }
+  ctx->pgraph.exec = exec;
+  ctx->pgraph.launches = in_graph;
+  return true;
+}
+
 int gg_plane_integrals(gg_ctx* ctx, const gg_grid* grids, int nplanes, double* out, void* stream) {
   if (!ctx || !grids || !out || nplanes <= 0) return GG_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (ctx->plane_pending) return ctx->fail(GG_EINVAL, "a queued plane pass has not been collected");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const double* dout = nullptr;
-  int rc = plane_enqueue(ctx, grids, nplanes, st, &dout);
+  PlanePass P;
+  int rc = plane_stage(ctx, grids, nplanes, &P);
   if (rc) return rc;
-  cudaError_t e =
-      cudaMemcpyAsync(out, dout, static_cast<size_t>(nplanes) * 7 * sizeof(double), cudaMemcpyDeviceToHost, st);
-  if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane result");
-  return ctx->check_device_error(st);
+  // one device batch, no profiling: the pass may run as a CUDA graph
+  const bool graphable = !ctx->prof.on && P.npts <= ctx->batch_points();
+  uint64_t sig[7] = {ctx->gen, static_cast<uint64_t>(nplanes), static_cast<uint64_t>(P.npts),
+                     static_cast<uint64_t>(P.nrows), static_cast<uint64_t>(P.nw),
+                     static_cast<uint64_t>(ctx->precision), graphable ? 1u : 0u};
+  auto& pg = ctx->pgraph;
+  const bool same = pg.seen && std::equal(sig, sig + 7, pg.sig);
+  if (graphable && same && !pg.exec && !pg.failed && !plane_capture(ctx, P)) pg.failed = true;
+  cudaError_t e;
+  if (graphable && same && pg.exec) {
+    e = cudaGraphLaunch(pg.exec, st);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "plane graph launch");
+    ctx->launches += pg.launches;
+  } else {
+    if (!same) ctx->drop_graph();
+    const double* dout = nullptr;
+    rc = plane_launch(ctx, P, st, &dout);
+    if (rc == GG_OK) rc = plane_readback(ctx, P, dout, st);
+    if (rc) {
+      cudaStreamSynchronize(st);
+      return rc;
+    }
+    // the signature after the pass (its own scratch growth included): a
+    // second pass like it is captured
+    sig[0] = ctx->gen;
+    std::copy(sig, sig + 7, pg.sig);
+    pg.seen = true;
+  }
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return ctx->cuda_fail(e, "device execution");
+  ctx->prof_collect();
+  const char* hb = static_cast<const char*>(ctx->plane_host);
+  int word = 0;
+  std::memcpy(&word, hb + P.h_err, sizeof(int));
+  if (word != 0) {
+    cudaMemset(ctx->d_err, 0, sizeof(int));
+    return ctx->fail(GG_ETIMEDOUT, "device pipeline wait gave up (code " + std::to_string(word) + ")");
+  }
+  std::memcpy(out, hb + P.h_out, static_cast<size_t>(nplanes) * 7 * sizeof(double));
+  return GG_OK;
 }
 
 int gg_plane_integrals_enqueue(gg_ctx* ctx, const gg_grid* grids, int nplanes, void* stream) {
@@ -1298,13 +1481,16 @@ int gg_plane_integrals_enqueue(gg_ctx* ctx, const gg_grid* grids, int nplanes, v
   std::lock_guard<std::mutex> g(ctx->mu);
   if (ctx->plane_pending) return ctx->fail(GG_EINVAL, "a queued plane pass has not been collected");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaSetDevice(ctx->device);
+  PlanePass P;
+  int rc = plane_stage(ctx, grids, nplanes, &P);
+  if (rc) return rc;
+  cudaError_t e = cudaSuccess;
   for (cudaEvent_t& ev : ctx->plane_ev)
     if (!ev && e == cudaSuccess) e = cudaEventCreate(&ev);
   if (e == cudaSuccess) e = cudaEventRecord(ctx->plane_ev[0], st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "plane pass events");
   const double* dout = nullptr;
-  int rc = plane_enqueue(ctx, grids, nplanes, st, &dout);
+  rc = plane_launch(ctx, P, st, &dout);
   if (rc) {
     cudaStreamSynchronize(st);  // nothing of this context may still run when it is used again
     return rc;

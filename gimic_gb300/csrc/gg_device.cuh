@@ -242,6 +242,18 @@ __device__ __forceinline__ void cart_eval(int packed, T x, T y, T z, T f1, T f2,
 // --------------------------------------------------------------------------
 // PTX wrappers
 // --------------------------------------------------------------------------
+// Pulls `bytes` of a read-only table into L1, one 128-byte line per thread
+// of the CTA at a time (only a hint: no data is returned).
+// Thread t of n threads takes lines t, t + n, ...
+__device__ __forceinline__ void prefetch_l1(const void* p, size_t bytes, int t, int n) {
+  const char* c = static_cast<const char*>(p);
+  for (size_t o = static_cast<size_t>(t) * 128; o < bytes; o += static_cast<size_t>(n) * 128)
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(c + o));
+}
+__device__ __forceinline__ void prefetch_l1(const void* p, size_t bytes) {
+  prefetch_l1(p, bytes, static_cast<int>(threadIdx.x), static_cast<int>(blockDim.x));
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }

@@ -54,6 +54,13 @@ struct TcArgs {
   const int* perm = nullptr;   // output index of each (sorted) point (null: identity)
   const int* tile_order = nullptr;  // tile of each queue step (null: step i -> tile i)
   int* tile_counter = nullptr;      // device int, zero at launch: the tile queue
+  // Chunk split for short passes (at most one tile per SM): every active
+  // chunk of a tile is its own step, on its own SM; csplit = the basis'
+  // chunk count, part = ntiles x csplit x kNDots x 128 float2 of partial
+  // sums, tile_done = ntiles x 4 counters (zero at launch, zero again after).
+  int csplit = 1;
+  float2* part = nullptr;
+  unsigned* tile_done = nullptr;
 };
 int tc_smem_bytes();
 
@@ -91,9 +98,11 @@ struct PlaneDesc {
 // block per plane row.
 void launch_plane_points(const double* xs, const PlaneDesc* planes, const int* row_plane, int64_t nrows, double* pts,
                          cudaStream_t st);
+// field: the magnetic field vector (3 doubles) in device memory; done:
+// nplanes counters, zero at launch (and zero again when it ends).
 void launch_plane_batch(const double* jt, const double* pts, const double* w, const PlaneDesc* planes, int nplanes,
-                        const int* row_plane, int64_t nrows, const double bb[3], double* row_out, double* out,
-                        cudaStream_t st);
+                        const int* row_plane, int64_t nrows, const double* field, double* row_out, double* out,
+                        unsigned* done, cudaStream_t st);
 
 // Shielding of every centre and magnetizability over a molecular grid whose
 // points come in nblocks consecutive blocks [block_off[l], block_off[l+1]):

@@ -1,7 +1,9 @@
 // Shell-blocked basis evaluation for the split-FP16 point operand.
 //
 // One CTA handles one tile of 128 consecutive points (the M tile of the
-// tensor-core contraction), one thread per point.  All threads walk the
+// tensor-core contraction), one thread per point; in passes with fewer
+// tiles than two per SM the tile's K range is split over several CTAs
+// (gridDim.y), each staging and storing only its half K blocks.  All threads walk the
 // shells in the same order (uniform control flow, shell data broadcast), so
 // each thread evaluates the radial factor of a shell once and then its
 // Cartesian components (bfeval.f90:81-122 with the per-shell screening of
@@ -32,6 +34,8 @@
 // for every point) are neither staged nor stored: the contraction never
 // reads them.
 #include <cuda.h>
+
+#include <algorithm>
 
 #include "gg_device.cuh"
 #include "gg_kernels.h"
@@ -79,6 +83,9 @@ struct Stager {
 
 }  // namespace
 
+// kSplit: the tile's K range is split over gridDim.y CTAs (small passes);
+// without it each CTA covers all K blocks and the range checks compile away.
+template <bool kSplit>
 __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_constant__ CUtensorMap tm_hi,
                                                                   const __grid_constant__ CUtensorMap tm_lo,
                                                                   DevBasis B, const double* __restrict__ pts,
@@ -91,6 +98,24 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
   const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBlockM;
   const int64_t p = min(m0 + row, npts - 1);  // rows past the end compute a copy; the TMA store clips them
   const int nkb = B.kpad / kBlockK;
+  // This CTA's half K blocks [hb0, hb1): a tile's K range is split over
+  // gridDim.y CTAs when there are few tiles (small passes), so that more SMs
+  // share the per-shell latency chain; with one CTA per tile it is all.
+  const int nhb = 2 * nkb;
+  const int hb0 = kSplit ? static_cast<int>(static_cast<int64_t>(blockIdx.y) * nhb / gridDim.y) : 0;
+  const int hb1 = kSplit ? static_cast<int>(static_cast<int64_t>(blockIdx.y + 1) * nhb / gridDim.y) : nhb;
+  const int mu_lo = hb0 * kHalfK, mu_hi = hb1 * kHalfK;
+
+  // Small passes run one CTA per SM on cold caches, where every shell's
+  // table loads would be a chain of L2 round trips: all threads first pull
+  // the tables into L1 (a few KB; in large passes they are resident anyway).
+  if (kSplit) {
+    prefetch_l1(B.sh_pack, B.nshells * sizeof(int4));
+    prefetch_l1(B.sh_rad2_df, B.nshells * sizeof(float2));
+    prefetch_l1(B.p_pack, B.nprim * sizeof(float4));
+    prefetch_l1(B.atom_df, B.natoms * 3 * sizeof(float2));
+    prefetch_l1(B.f_ijk, B.nbf * sizeof(int));
+  }
 
   // active K blocks of this tile (all when no screening lists are given)
   uint64_t kb_on = ~0ull;
@@ -128,13 +153,12 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
     const int e = static_cast<int>(floorf(lb + 0.05f)) + 1;
     scale = ldexpf(1.f, max(-120, min(120, 14 - e)));
   }
-  if (m0 + row < npts) inv_scale[m0 + row] = 1.f / scale;
+  if ((!kSplit || blockIdx.y == 0) && m0 + row < npts) inv_scale[m0 + row] = 1.f / scale;
 
   // ---- pass 2: values, staged per K block and stored with TMA -------------
   Stager st{base, row, __float2half_rn(0.f), __float2half_rn(0.f)};
-  int kb = 0;  // the half block being staged
-  const int nhb = 2 * nkb;
-  bool active = (kb_on & 1ull) != 0;
+  int kb = hb0;  // the half block being staged
+  bool active = hb0 < hb1 && ((kb_on >> (hb0 >> 1)) & 1ull);
   auto flush = [&](int k) {  // all threads: the K block k is complete in the buffer
     fence_proxy_async();
     __syncthreads();
@@ -150,10 +174,11 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
     while (kb < k) {
       if (active) flush(kb);
       ++kb;
-      active = kb < nhb && ((kb_on >> (kb >> 1)) & 1ull);
+      active = kb < hb1 && ((kb_on >> (kb >> 1)) & 1ull);
     }
   };
   auto emit = [&](int mu, float v, bool zero) {
+    if (kSplit && (mu < mu_lo || mu >= mu_hi)) return;  // another CTA's half blocks
     const int k = mu / kHalfK;
     if (k != kb) advance_to(k);
     if (!active) return;
@@ -174,6 +199,8 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
     for (int sh = 0; sh < B.nshells; ++sh) {
       const int4 pk = __ldg(B.sh_pack + sh);  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
       const int mu0 = pk.y, ncomp = pk.z & 0xff, np = (pk.z >> 8) & 0xff;
+      if (kSplit && mu0 + ncomp <= mu_lo) continue;  // shells are in function order
+      if (kSplit && mu0 >= mu_hi) break;
       const int k_first = mu0 >> 6, k_last = (mu0 + ncomp - 1) >> 6;
       // skip whole shells whose K blocks are inactive for the tile
       if (!((kb_on >> k_first) & 1ull) && !((kb_on >> k_last) & 1ull)) continue;
@@ -215,8 +242,8 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
       }
     }
     // padding columns nbf .. kpad-1 of the last K block are zero
-    for (int mu = B.nbf; mu < B.kpad; ++mu) emit(mu, 0.f, true);
-    advance_to(nhb);
+    for (int mu = max(B.nbf, mu_lo); mu < min(B.kpad, mu_hi); ++mu) emit(mu, 0.f, true);
+    advance_to(hb1);
   }
   if (threadIdx.x == 0) bulk_wait_all();
 }
@@ -225,14 +252,28 @@ cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* 
                               int64_t npts, const int* tiles, int stride, float* inv_scale, cudaStream_t st) {
   if (npts <= 0) return cudaSuccess;
   if (B.kpad / kBlockK > 64) return cudaErrorInvalidValue;  // K-block mask is 64 bits
-  // the shared-memory attribute, once per device (it applies to the current one)
+  // the shared-memory attribute (it applies to the current device) and the
+  // SM count, once per device
   static PerDevice pd;
-  cudaError_t e = once_per_device(pd, nullptr, [](int, int*) {
-    return cudaFuncSetAttribute(basis_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+  int nsm = 0;
+  cudaError_t e = once_per_device(pd, &nsm, [](int dev, int* sms) {
+    cudaError_t r = cudaFuncSetAttribute(basis_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+    if (r == cudaSuccess)
+      r = cudaFuncSetAttribute(basis_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+    if (r != cudaSuccess) return r;
+    return cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
   });
   if (e != cudaSuccess) return e;
-  const unsigned grid = static_cast<unsigned>((npts + kBlockM - 1) / kBlockM);
-  basis_tile_kernel<<<grid, kTileThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
+  const int64_t ntiles = (npts + kBlockM - 1) / kBlockM;
+  // fewer tiles than two per SM: split every tile's half K blocks over
+  // several CTAs, about two CTAs per SM in all (each CTA walks only the
+  // shells of its half blocks; the row-scale pass is repeated per CTA)
+  const int nhb = 2 * (B.kpad / kBlockK);
+  int kgroups = 1;
+  if (nsm > 0 && ntiles < 2 * nsm) kgroups = static_cast<int>(std::min<int64_t>(nhb, (2 * nsm + ntiles - 1) / ntiles));
+  const dim3 grid(static_cast<unsigned>(ntiles), static_cast<unsigned>(kgroups));
+  auto kernel = kgroups > 1 ? basis_tile_kernel<true> : basis_tile_kernel<false>;
+  kernel<<<grid, kTileThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
                                                             *static_cast<const CUtensorMap*>(tm_lo), B, pts, npts,
                                                             tiles, stride, inv_scale);
   return cudaGetLastError();

@@ -52,40 +52,64 @@ __device__ __forceinline__ void block_reduce_store(double acc[kQ], double wj, do
   if (threadIdx.x < kQ) dst[threadIdx.x] = red[threadIdx.x][0] * wj;
 }
 
-// One block per row of one plane of a batch.
-__global__ void __launch_bounds__(kRowThreads) plane_batch_rows_kernel(const double* __restrict__ jt,
-                                                                       const double* __restrict__ pts,
-                                                                       const double* __restrict__ w,
-                                                                       const PlaneDesc* __restrict__ planes,
-                                                                       const int* __restrict__ row_plane, double b0,
-                                                                       double b1, double b2, double* row_out) {
+// One block per row of one plane of a batch: the row's sums over i (fixed
+// tree), times w_j, to row_out.  The block that finishes a plane's last row
+// (counted in done[plane], zero at launch) then sums the plane's rows in
+// order, s2 over j and s3 += w_k s2 over k (integral.f90:107-165), so the
+// plane's result does not depend on which block came last.
+__global__ void __launch_bounds__(kRowThreads) plane_batch_kernel(const double* __restrict__ jt,
+                                                                  const double* __restrict__ pts,
+                                                                  const double* __restrict__ w,
+                                                                  const PlaneDesc* __restrict__ planes,
+                                                                  const int* __restrict__ row_plane,
+                                                                  const double* __restrict__ field, double* row_out,
+                                                                  double* __restrict__ out, unsigned* done) {
   const int64_t row = blockIdx.x;
-  const PlaneDesc& pl = planes[row_plane[row]];
+  const int q = row_plane[row];
+  const PlaneDesc& pl = planes[q];
   const int64_t r = row - pl.row_off;
   const int j = static_cast<int>(r % pl.p2), k = static_cast<int>(r / pl.p2);
-  const double bb[3] = {b0, b1, b2};
+  const double bb[3] = {field[0], field[1], field[2]};
   double acc[kQ] = {0, 0, 0, 0, 0, 0, 0};
   for (int i = threadIdx.x; i < pl.p1; i += kRowThreads) {
     const int64_t idx = pl.pt_off + i + static_cast<int64_t>(pl.p1) * (j + static_cast<int64_t>(pl.p2) * k);
     point_terms(jt + 9 * idx, pts + 3 * idx, pl.center, pl.normal, bb, pl.radius, w[pl.w_off + i], acc);
   }
   block_reduce_store(acc, w[pl.w_off + pl.p1 + j], row_out + row * kQ);
-}
-
-// One thread per (plane, sum): rows in order, then planes of k.
-__global__ void plane_batch_sum_kernel(const double* __restrict__ w, const PlaneDesc* __restrict__ planes, int nplanes,
-                                       const double* __restrict__ row_out, double* __restrict__ out) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nplanes * kQ) return;
-  const int q = t % kQ;
-  const PlaneDesc& pl = planes[t / kQ];
-  double s3 = 0.0;
-  for (int k = 0; k < pl.p3; ++k) {
-    double s2 = 0.0;
-    for (int j = 0; j < pl.p2; ++j) s2 += row_out[(pl.row_off + static_cast<int64_t>(k) * pl.p2 + j) * kQ + q];
-    s3 = s3 + w[pl.w_off + pl.p1 + pl.p2 + k] * s2;
+  __threadfence();  // this row's sums are visible before it is counted
+  __shared__ bool last;
+  __syncthreads();
+  const int64_t nr = static_cast<int64_t>(pl.p2) * pl.p3;
+  if (threadIdx.x == 0) last = atomicAdd(done + q, 1u) == static_cast<unsigned>(nr - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // rows of the plane in order, staged through shared memory in chunks
+  __shared__ double chunk[kRowThreads][kQ];
+  double s2 = 0.0, s3 = 0.0;
+  int jj = 0, kk = 0;  // row j within the rows of k
+  const double* wk = w + pl.w_off + pl.p1 + pl.p2;
+  for (int64_t base = 0; base < nr; base += kRowThreads) {
+    const int64_t rr = base + threadIdx.x;
+    if (rr < nr)
+      for (int c = 0; c < kQ; ++c) chunk[threadIdx.x][c] = __ldcg(row_out + (pl.row_off + rr) * kQ + c);
+    __syncthreads();
+    if (threadIdx.x < kQ) {
+      const int n = static_cast<int>(nr - base < kRowThreads ? nr - base : kRowThreads);
+      for (int t = 0; t < n; ++t) {
+        s2 += chunk[t][threadIdx.x];
+        if (++jj == pl.p2) {  // the rows of k are done
+          s3 = s3 + wk[kk] * s2;
+          s2 = 0.0;
+          jj = 0;
+          ++kk;
+        }
+      }
+    }
+    __syncthreads();
   }
-  out[t] = s3;
+  if (threadIdx.x < kQ) out[q * kQ + threadIdx.x] = s3;
+  if (threadIdx.x == 0) done[q] = 0;
 }
 
 __global__ void __launch_bounds__(kRowThreads) plane_points_kernel(const double* __restrict__ xs,
@@ -114,12 +138,11 @@ void launch_plane_points(const double* xs, const PlaneDesc* planes, const int* r
 }
 
 void launch_plane_batch(const double* jt, const double* pts, const double* w, const PlaneDesc* planes, int nplanes,
-                        const int* row_plane, int64_t nrows, const double bb[3], double* row_out, double* out,
-                        cudaStream_t st) {
+                        const int* row_plane, int64_t nrows, const double* field, double* row_out, double* out,
+                        unsigned* done, cudaStream_t st) {
   if (nplanes <= 0) return;
-  plane_batch_rows_kernel<<<static_cast<unsigned>(nrows), kRowThreads, 0, st>>>(jt, pts, w, planes, row_plane, bb[0],
-                                                                                 bb[1], bb[2], row_out);
-  plane_batch_sum_kernel<<<(nplanes * kQ + 127) / 128, 128, 0, st>>>(w, planes, nplanes, row_out, out);
+  plane_batch_kernel<<<static_cast<unsigned>(nrows), kRowThreads, 0, st>>>(jt, pts, w, planes, row_plane, field,
+                                                                            row_out, out, done);
 }
 
 // ---------------------------------------------------------------------------

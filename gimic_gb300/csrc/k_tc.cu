@@ -123,7 +123,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     DevBasis Bs, const float* __restrict__ inv_row, const float* __restrict__ inv_col,
                     const double* __restrict__ pts, int64_t npts, Flags fl, Outputs out, int* err,
                     const int* __restrict__ tiles, int tstride, const int* __restrict__ perm,
-                    const int* __restrict__ tile_order, int* __restrict__ tile_counter) {
+                    const int* __restrict__ tile_order, int* __restrict__ tile_counter, int csplit,
+                    float2* __restrict__ part, unsigned* __restrict__ tile_done) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                          ~static_cast<uintptr_t>(1023));
@@ -142,10 +143,28 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t ntiles = (npts + kBlockM - 1) / kBlockM;
+  // A step is one tile (csplit == 1) or one active chunk of a tile (the
+  // chunk split of short passes: step t is chunk t % csplit of tile
+  // t / csplit, and csplit is the chunk count of the basis).
+  const int64_t nsteps = ntiles * csplit;
   const int nchunk_all = Bs.nchunk, nkb_all = Bs.kpad / kBlockK;
   // the tile of step t, and its active column chunks and K blocks (all of
   // them without a screening list; no chunk at all without a K block)
-  auto tile_of = [&](int64_t t) -> int64_t { return tile_order ? static_cast<int64_t>(tile_order[t]) : t; };
+  auto tile_of = [&](int64_t t) -> int64_t {
+    const int64_t u = t / csplit;
+    return tile_order ? static_cast<int64_t>(tile_order[u]) : u;
+  };
+  // the chunks [c0, c1) of the tile's active list that step t covers
+  auto chunk_span = [&](int64_t t, int nchunk, int* c0, int* c1) {
+    if (csplit == 1) {
+      *c0 = 0;
+      *c1 = nchunk;
+    } else {
+      const int g = static_cast<int>(t % csplit);
+      *c0 = g;
+      *c1 = g < nchunk ? g + 1 : g;
+    }
+  };
   auto n_kb = [&](int64_t tile) -> int { return tiles ? tiles[tile * tstride + 1] : nkb_all; };
   auto n_chunk = [&](int64_t tile, int nk) -> int { return nk > 0 ? (tiles ? tiles[tile * tstride] : nchunk_all) : 0; };
   auto chunk_at = [&](int64_t tile, int i) -> int { return tiles ? tiles[tile * tstride + 2 + i] : i; };
@@ -194,17 +213,19 @@ __global__ void __launch_bounds__(kThreads, 1)
         // next tile step from the global queue, handed to the other roles
         const int slot = step % kRing;
         if (!mbar_wait(&ring_empty[slot], ((step / kRing) & 1) ^ 1, err, 7)) goto producer_exit;
-        const int64_t t = failed() ? ntiles : static_cast<int64_t>(atomicAdd(tile_counter, 1));
-        ring[slot] = t < ntiles ? static_cast<int>(t) : -1;
+        const int64_t t = failed() ? nsteps : static_cast<int64_t>(atomicAdd(tile_counter, 1));
+        ring[slot] = t < nsteps ? static_cast<int>(t) : -1;
         mbar_arrive(&ring_full[slot]);
-        if (t >= ntiles) {
+        if (t >= nsteps) {
           clean = true;
           break;
         }
         const int64_t tile = tile_of(t);
         const int m0 = static_cast<int>(tile * kBlockM);
         const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
-        for (int ci = 0; ci < nchunk; ++ci) {
+        int c0, c1;
+        chunk_span(t, nchunk, &c0, &c1);
+        for (int ci = c0; ci < c1; ++ci) {
           const int c = chunk_at(tile, ci);
           // cross pass: (A_hi, B_lo) then (A_lo, B_hi) of every K block;
           // main pass: (A_hi, B_hi) of every K block; one pair per stage
@@ -243,7 +264,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         const int64_t tile = tile_of(t);
         const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
-        for (int ci = 0; ci < nchunk; ++ci, ++acc) {
+        int c0, c1;
+        chunk_span(t, nchunk, &c0, &c1);
+        for (int ci = c0; ci < c1; ++ci, ++acc) {
           const int b = acc & 1, rb = acc >> 1;
           if (!mbar_wait(&accempty[b], (rb & 1) ^ 1, err, 2)) goto mma_exit;
           tc_fence_after();
@@ -315,7 +338,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       DFloat d2a{0.f, 0.f};
       bool on = false, warp_on = false;
       const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
-      for (int ci = 0; ci < nchunk; ++ci, ++acc) {
+      int c0, c1;
+      chunk_span(t, nchunk, &c0, &c1);
+      for (int ci = c0; ci < c1; ++ci, ++acc) {
         const int c = chunk_at(tile, ci);
         const int b = acc & 1, rb = acc >> 1;
         if (!mbar_wait(&accfull[b], rb & 1, err, 4)) {
@@ -444,17 +469,57 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(xfull);
       } else {
         if (!mbar_wait(xfull, tk & 1, err, 6)) break;
-        if (valid) {
+        const float2* h1 = redf + row * kNDots;
+        bool finish = true;  // this warp combines and stores its rows now
+        if (csplit > 1) {
+          // Chunk split: the step's sums of these 32 rows (both halves) go to
+          // the tile's partial slot g; the warp that completes this quarter
+          // of the tile (the last of the csplit steps to count) adds the
+          // slots in chunk order into thi/tlo, so the result does not depend
+          // on which step came last.
+          const int g = static_cast<int>(t % csplit);
+          const int64_t quarter = tile * 4 + q;
+          if (g < nchunk) {
+            float2* dst = part + (tile * csplit + g) * static_cast<int64_t>(kNDots * kBlockM) + row;
+#pragma unroll
+            for (int i = 0; i < kNDots; ++i) {
+              const DFloat v = df_add(DFloat{thi[i], tlo[i]}, DFloat{h1[i].x, h1[i].y});
+              dst[i * kBlockM] = make_float2(v.h, v.l);
+            }
+          }
+          __threadfence();
+          __syncwarp();
+          unsigned last = 0;
+          if (lane == 0) last = atomicAdd(tile_done + quarter, 1u) == static_cast<unsigned>(csplit - 1) ? 1u : 0u;
+          finish = __shfl_sync(0xffffffffu, last, 0) != 0;
+          if (finish) {
+            __threadfence();
+#pragma unroll
+            for (int i = 0; i < kNDots; ++i) thi[i] = tlo[i] = 0.f;
+            for (int gg = 0; gg < min(csplit, nchunk); ++gg) {
+              const float2* src = part + (tile * csplit + gg) * static_cast<int64_t>(kNDots * kBlockM) + row;
+#pragma unroll
+              for (int i = 0; i < kNDots; ++i) {
+                const float2 v = __ldcg(src + i * kBlockM);
+                const DFloat a = df_add(DFloat{thi[i], tlo[i]}, DFloat{v.x, v.y});
+                thi[i] = a.h;
+                tlo[i] = a.l;
+              }
+            }
+            if (lane == 0) tile_done[quarter] = 0;
+          }
+        }
+        if (finish && valid) {
           // the row scale and the matrix scales are powers of two: scaling
           // a double-float is exact.  Sum i belongs to matrix dot_matrix(i).
           const float sc = inv_row[p];
           float msc[kMats];
 #pragma unroll
           for (int m = 0; m < kMats; ++m) msc[m] = sc * icol[m];
-          const float2* h1 = redf + row * kNDots;
+          const bool own = csplit == 1;  // the other half's sums still to add
           auto tot = [&](int i) -> DFloat {
-            const float2 o = h1[i];
-            const DFloat t = df_add(DFloat{thi[i], tlo[i]}, DFloat{o.x, o.y});
+            const float2 o = own ? h1[i] : make_float2(0.f, 0.f);
+            const DFloat t = own ? df_add(DFloat{thi[i], tlo[i]}, DFloat{o.x, o.y}) : DFloat{thi[i], tlo[i]};
             const float f = msc[dot_matrix(i)];
             return DFloat{t.h * f, t.l * f};
           };
@@ -478,7 +543,16 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    reg_dealloc_ctl();  // warps 2 and 3: no role
+    reg_dealloc_ctl();  // warps 2 and 3: no pipeline role
+    // They pull the epilogue's tables into L1 while the first operands
+    // load: in a short pass each SM sees one or two tiles on cold caches,
+    // where every shell change would otherwise wait on a chain of L2 loads.
+    const int t = threadIdx.x - 64;
+    prefetch_l1(Bs.f_pack, Bs.nbf * sizeof(int), t, 64);
+    prefetch_l1(Bs.sh_pack, Bs.nshells * sizeof(int4), t, 64);
+    prefetch_l1(Bs.sh_rad2_df, Bs.nshells * sizeof(float2), t, 64);
+    prefetch_l1(Bs.p_pack, Bs.nprim * sizeof(float4), t, 64);
+    prefetch_l1(Bs.atom_df, Bs.natoms * 3 * sizeof(float2), t, 64);
   }
   tc_fence_before();
   __syncthreads();
@@ -517,13 +591,15 @@ cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st)
   if (e != cudaSuccess) return e;
   if (nsm <= 0) return cudaErrorInvalidDevice;
   const int64_t ntiles = (a.npts + kBlockM - 1) / kBlockM;
-  const unsigned grid = static_cast<unsigned>(std::min<int64_t>(ntiles, nsm));
+  const int csplit = std::max(1, a.csplit);
+  if (csplit > 1 && (!a.part || !a.tile_done)) return cudaErrorInvalidValue;
+  const unsigned grid = static_cast<unsigned>(std::min<int64_t>(ntiles * csplit, nsm));
   auto kernel = div ? tc_fused_kernel<true> : tc_fused_kernel<false>;
   kernel<<<grid, kThreads, kSmemBytes, st>>>(
       *static_cast<const CUtensorMap*>(a.tmap_a_hi), *static_cast<const CUtensorMap*>(a.tmap_a_lo),
       *static_cast<const CUtensorMap*>(a.tmap_b_hi), *static_cast<const CUtensorMap*>(a.tmap_b_lo), B,
       a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err, a.tiles, a.tile_stride, a.perm,
-      a.tile_order, a.tile_counter);
+      a.tile_order, a.tile_counter, csplit, a.part, a.tile_done);
   return cudaGetLastError();
 }
 

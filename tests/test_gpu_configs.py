@@ -102,8 +102,8 @@ def test_integral_driver_acid_block(tmp_path, synth_dir):
     d.mkdir()
     os.symlink(mp, d / "MOL")
     os.symlink(xp, d / "XDENS")
-    text = synth.ring_bond_plane_input(mol) + ("Advanced {\n screening=on\n screening_thrs=1.d-8\n}\n"
-                                              "Essential {\n acid=on\n}\n")
+    text = ('basis="MOL"\nxdens="XDENS"\n' + synth.ring_bond_plane_input(mol)
+            + "Advanced {\n spherical=off\n screening=on\n screening_thrs=1.d-8\n}\nEssential {\n acid=on\n}\n")
     (d / "gimic.inp").write_text(text)
     buf = io.StringIO()
     driver.Driver(str(d / "gimic.inp"), precision="split16", stream=buf).run()
@@ -131,9 +131,10 @@ def test_cdens_acid_field_against_oracle(tmp_path, synth_dir, precision, tol):
     os.symlink(mp, d / "MOL")
     os.symlink(xp, d / "XDENS")
     (d / "gimic.inp").write_text(
-        "calc=cdens\nmagnet_axis=z\nGrid(base) {\n type=even\n origin=[-6.0, -6.0, -3.0]\n ivec=[1.0, 0.0, 0.0]\n"
+        'calc=cdens\nbasis="MOL"\nxdens="XDENS"\nmagnet_axis=z\n'
+        "Grid(base) {\n type=even\n origin=[-6.0, -6.0, -3.0]\n ivec=[1.0, 0.0, 0.0]\n"
         " jvec=[0.0, 1.0, 0.0]\n lengths=[12.0, 12.0, 6.0]\n spacing=[0.75, 0.75, 0.75]\n}\n"
-        "Advanced {\n screening=on\n screening_thrs=1.d-8\n}\nEssential {\n acid=on\n jmod=off\n}\n")
+        "Advanced {\n spherical=off\n screening=on\n screening_thrs=1.d-8\n}\nEssential {\n acid=on\n jmod=off\n}\n")
     drv = driver.Driver(str(d / "gimic.inp"), precision=precision, stream=io.StringIO())
     drv.run()
     pts = drv.grid.points()
@@ -148,3 +149,66 @@ def test_cdens_acid_field_against_oracle(tmp_path, synth_dir, precision, tol):
     ax = np.abs(want)
     ulp = np.where(ax > 0, 10.0 ** (np.floor(np.log10(np.where(ax > 0, ax, 1.0))) + 1.0 - 6.0), 0.0)
     assert np.all(np.abs(got - want) <= tol * want.max() + 1.01 * ulp)
+
+
+def test_plane_graph_replay_matches_eager_passes(synth_dir):
+    """gg_plane_integrals captures a pass as a CUDA graph on the second call
+    with the same layout and replays it afterwards.  Replays with new plane
+    data, a new field, or after a flag change (which forces an eager pass
+    and a new capture) are bit-identical to eager passes in fresh contexts."""
+    mp, xp, mol = synth.make_workload("c6h6", str(synth_dir), seed=2024)
+    planes = []
+    for bond in ((1, 2), (2, 3)):
+        i = ginp.read(synth.ring_bond_plane_input(mol, bond=bond), is_text=True)
+        grd = ggrid.new_grid(i, mol.coords)
+        bb, _ = ggrid.get_magnet(grd, i)
+        planes.append(((grd.origin, grd.basv, grd.axes(), grd.radius), bb))
+
+    def fresh(plane, bb, flags=(1, 1, 1)):
+        h = api.Gimic(mp, xp, screening=1e-8)
+        h.set_flags(*flags)
+        h.set_magnet(bb)
+        return h.plane_integrals([plane])[0]
+
+    g = api.Gimic(mp, xp, screening=1e-8)
+    (pa, ba), (pb, bbb) = planes
+    g.set_magnet(ba)
+    want_a = fresh(pa, ba)
+    got = [g.plane_integrals([pa])[0] for _ in range(4)]  # eager, capture, replay, replay
+    assert all(r == want_a for r in got)
+    g.set_magnet(bbb)
+    assert g.plane_integrals([pb])[0] == fresh(pb, bbb)
+    tilted = np.array([0.3, -0.2, 0.9])
+    g.set_magnet(tilted)
+    assert g.plane_integrals([pa])[0] == fresh(pa, tilted)
+    g.set_flags(1, 1, 0)
+    for _ in range(3):
+        assert g.plane_integrals([pb])[0] == fresh(pb, tilted, flags=(1, 1, 0))
+    # the kernel count goes on through the replays
+    g.profile(False)
+    g.plane_integrals([pb])
+    assert g.profile_read()["kernels"] > 0
+
+
+@pytest.mark.parametrize("name", ["c6h6", "c24h24"])
+def test_short_and_long_passes_agree(synth_dir, name):
+    """A short pass (no more tiles than SMs) spreads each tile's column
+    chunks over SMs and adds their partial sums in chunk order; a long pass
+    accumulates the chunks of a tile on one SM, each chunk's fp32 sum
+    starting from the running compensation term.  The fp32 roundings of the
+    chunk sums therefore differ between the two (about 3e-8 of max |j|,
+    against the path's 1e-6 tolerance); both match the oracle."""
+    mp, xp, mol = synth.make_workload(name, str(synth_dir), seed=2024)
+    g = api.Gimic(mp, xp, screening=1e-8)
+    pts = cube_sample(mol.coords, 1800, 248, seed=23)  # 16 tiles: a short pass
+    short, rho_s, dv_s = g.jtensor_batch(pts, rho=True, divj=True)
+    rng = np.random.default_rng(5)
+    filler = rng.uniform(-16.0, 16.0, (160 * 128, 3))  # 160 more tiles: a long pass
+    long_, rho_l, dv_l = g.jtensor_batch(np.vstack([pts, filler]), rho=True, divj=True)
+    n = len(pts)
+    assert rel_max_err(short, long_[:n]) <= 1e-7
+    assert rel_max_err(rho_s, rho_l[:n]) <= 1e-7
+    assert rel_max_err(dv_s, dv_l[:n]) <= 1e-6
+    o = oracle.Oracle(mp, xp, screening=1e-8)
+    ref = o.jtensor(pts)
+    assert rel_max_err(short, ref) <= TOL_SPLIT and rel_max_err(long_[:n], ref) <= TOL_SPLIT
