@@ -137,7 +137,8 @@ class Driver:
             if self.kw.get("Essential.prop"):
                 # get_property (jfield.f90:404-405): shielding and magnetizability
                 # over the molecular grid of gridfile.grd / grid_w.grd
-                out[spin]["properties"] = properties.run(self.g, self.stream, self.workdir)
+                out[spin]["properties"] = properties.run(self.g, self.stream, self.workdir, grid_points=pts,
+                                                         grid_jt=jt)
         return out
 
     def _write_fields(self, tag, pts, jt, jv):

@@ -114,8 +114,42 @@ def report(stream, sigma, chi):
     contrib(chi)
 
 
-def run(gimic, stream, workdir="."):
-    """Read the grid files, evaluate, print; returns (sigma, chi) or None."""
+def integrand_file_name(kind, k=None):
+    """File names of jfield.f90:785-806 and :905-910: sigma<k>.vtu,
+    sigma_xx<k>.vtu, ... per nucleus k (1-based) and intchi*.vtu.  The
+    reference formats k with I1 or I2, so from nucleus 100 on all its files
+    share one name made of asterisks; here k is written in full instead."""
+    return ("%s%d.vtu" % (kind, k)) if k is not None else ("%s.vtu" % kind)
+
+
+def write_integrand_files(workdir, pts, jt, coord, cells):
+    """The per-point VTU files of get_property (written only when
+    grid.1.ele is present): for every nucleus the summed shielding
+    integrand and its three diagonal parts, then the same for the
+    magnetizability.  jt: (N, 9) tensors at pts (N, 3); returns the names."""
+    from . import vtk
+
+    sig, chi = per_point(jt, pts, coord)
+    names = []
+    for k, s3 in enumerate(sig, start=1):
+        for kind, vals in (("sigma", s3.sum(axis=1)), ("sigma_xx", s3[:, 0]), ("sigma_yy", s3[:, 1]),
+                           ("sigma_zz", s3[:, 2])):
+            name = integrand_file_name(kind, k)
+            vtk.write_scalar_unstructured(os.path.join(workdir, name), pts, vals, cells)
+            names.append(name)
+    for kind, vals in (("intchi", chi.sum(axis=1)), ("intchi_xx", chi[:, 0]), ("intchi_yy", chi[:, 1]),
+                       ("intchi_zz", chi[:, 2])):
+        name = integrand_file_name(kind)
+        vtk.write_scalar_unstructured(os.path.join(workdir, name), pts, vals, cells)
+        names.append(name)
+    return names
+
+
+def run(gimic, stream, workdir=".", grid_points=None, grid_jt=None):
+    """Read the grid files, evaluate, print and, with grid.1.ele present,
+    write the per-point integrand files; returns (sigma, chi) or None.
+    grid_points / grid_jt: tensors the caller already has (calc=cdens on
+    the same file grid), reused for the files when the points agree."""
     inputs = read_inputs(workdir)
     if inputs is None:
         stream.write(" at least one of the files coord.au, gridfile.grd, and grid_w.grd is missing. Therefore any "
@@ -124,4 +158,13 @@ def run(gimic, stream, workdir="."):
     coord, pts, w, blocks = inputs
     sigma, chi = gimic.properties(pts, w, coord, blocks)
     report(stream, sigma, chi)
+    ele = os.path.join(workdir, "grid.1.ele")
+    if os.path.exists(ele):
+        from . import vtk
+
+        if grid_jt is not None and grid_points is not None and np.array_equal(np.asarray(grid_points), pts):
+            jt = np.asarray(grid_jt)
+        else:
+            jt = gimic.jtensor_batch(pts)
+        write_integrand_files(workdir, pts, jt, coord, vtk.read_tetgen_ele(ele))
     return sigma, chi

@@ -145,6 +145,42 @@ def write_vector_unstructured(path, points, vec, cells):
         f.writelines(out)
 
 
+def write_scalar_unstructured(path, points, values, cells):
+    """write_vtk_scalar_unstructuredgrid (vtkplot.f90:318-390): tetrahedra
+    (VTK type 10) with 0-based connectivity, points in 3e20.10, one scalar
+    per point in e20.10, offsets in i10, types in i5 and an all-zero cell
+    array in f4.1, laid out as the reference writes them."""
+    pts = np.asarray(points, dtype=np.float64).reshape(-1, 3)
+    v = np.asarray(values, dtype=np.float64).reshape(-1)
+    cells = np.asarray(cells, dtype=np.int64).reshape(-1, 4)
+    nc = len(cells)
+    out = ['<?xml version="1.0"?>\n',
+           '<VTKFile type="UnstructuredGrid" version="0.1" byte_order="LittleEndian">\n',
+           '  <UnstructuredGrid>\n',
+           '    <Piece NumberOfPoints="%10d" NumberOfCells="%10d">\n' % (len(pts), nc),
+           '      <Points>\n',
+           '        <DataArray type="Float32" NumberOfComponents="3" Format="ascii">\n']
+    for p in pts:
+        out.append("        " + "".join(fortran_e(x, 20, 10) for x in p) + "\n")
+    out.append('        </DataArray>\n      </Points>\n      <PointData Scalars="scalars">\n'
+               '        <DataArray Name="scalars" type="Float64" NumberOfComponents="1" Format="ascii">\n')
+    for x in v:
+        out.append("        " + fortran_e(x, 20, 10) + "\n")
+    out.append('        </DataArray>\n      </PointData>\n      <Cells>\n'
+               '        <DataArray type="Int32" Name="connectivity" Format="ascii">\n')
+    for c in cells:
+        out.append("        " + "".join("%10d" % (x - 1) for x in c) + "\n")
+    out.append('        </DataArray>\n        <DataArray type="Int32" Name="offsets" Format="ascii">\n')
+    out.append("        " + "".join("%10d" % (4 * (i + 1)) for i in range(nc)) + "\n")
+    out.append('        </DataArray>\n        <DataArray type="Int32" Name="types" Format="ascii">\n')
+    out.append("        " + "%5d" % 10 * nc + "\n")
+    out.append('        </DataArray>\n      </Cells>\n      <CellData Scalars="foo">\n')
+    out.append("        " + " 0.0" * nc + "\n")
+    out.append("      </CellData>\n    </Piece>\n  </UnstructuredGrid>\n</VTKFile>\n")
+    with open(path, "w") as f:
+        f.writelines(out)
+
+
 def read_tetgen_ele(path):
     """grid.1.ele as read in jfield.f90:421-433: count on the first line, then
     'index n1 n2 n3 n4' per cell (1-based)."""

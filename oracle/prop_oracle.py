@@ -14,6 +14,27 @@ def _jvec(t, a):
     return -t[:, 3 * a:3 * a + 3]
 
 
+def integrands(jt, pts, centres):
+    """Per-point integrands of get_property (jfield.f90:693-711 intsigma,
+    :824-842 intchi): (ncentres, N, 3) shielding terms in ppm and (N, 3)
+    magnetizability terms."""
+    t = np.asarray(jt, dtype=np.float64).reshape(-1, 9)
+    pts = np.asarray(pts, dtype=np.float64).reshape(-1, 3)
+    j = [_jvec(t, a) for a in range(3)]
+
+    def terms(d, scale):
+        return np.stack([scale * (d[:, 1] * j[0][:, 2] - d[:, 2] * j[0][:, 1]),
+                         scale * (d[:, 2] * j[1][:, 0] - d[:, 0] * j[1][:, 2]),
+                         scale * (d[:, 0] * j[2][:, 1] - d[:, 1] * j[2][:, 0])], axis=1)
+
+    sig = []
+    for R in np.asarray(centres, dtype=np.float64).reshape(-1, 3):
+        d = pts - R
+        f = -1.0 / ((d * d).sum(axis=1) ** 1.5) / C_AU ** 2.0
+        sig.append(terms(d, 1.0) * (1.0e6 * f)[:, None])
+    return np.asarray(sig), terms(pts, 0.5)
+
+
 def properties(jt, pts, w, centres, block_npts=None):
     """(sigma (ncentres, nblocks, 5), chi (nblocks, 5)) as gg_properties."""
     t = np.asarray(jt, dtype=np.float64).reshape(-1, 9)

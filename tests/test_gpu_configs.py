@@ -212,3 +212,61 @@ def test_short_and_long_passes_agree(synth_dir, name):
     o = oracle.Oracle(mp, xp, screening=1e-8)
     ref = o.jtensor(pts)
     assert rel_max_err(short, ref) <= TOL_SPLIT and rel_max_err(long_[:n], ref) <= TOL_SPLIT
+
+
+@pytest.mark.parametrize("precision,tol", [("split16", 1e-6), ("fp64", 1e-11)])
+def test_property_integrand_files_against_oracle(tmp_path, synth_dir, precision, tol):
+    """calc=cdens with Essential.prop=on on the molecular grid of
+    gridfile.grd / grid_w.grd / coord.au / nelpts.info writes, when
+    grid.1.ele is present, the per-point files of get_property
+    (src/fgimic/jfield.f90:785-806, :905-910): sigma<k>.vtu and its three
+    diagonal parts for every nucleus k, and intchi*.vtu.  Their values are
+    the oracle's integrands (its tensors through the FP64 restatement)."""
+    import prop_oracle
+
+    mp, xp, mol = synth.make_workload("c6h6", str(synth_dir), seed=2024)
+    d = tmp_path / precision
+    d.mkdir()
+    os.symlink(mp, d / "MOL")
+    os.symlink(xp, d / "XDENS")
+    rng = np.random.default_rng(41)
+    xyz = mol.coords
+    blocks = rng.integers(30, 60, len(xyz))
+    pts = np.vstack([xyz[a] + rng.normal(0.0, 1.0, (blocks[a], 3)) for a in range(len(xyz))])
+    w = rng.uniform(0.01, 0.1, len(pts))
+    (d / "gridfile.grd").write_text("".join("%.15e %.15e %.15e\n" % tuple(p) for p in pts))
+    (d / "grid_w.grd").write_text("".join("%.15e\n" % v for v in w))
+    (d / "coord.au").write_text("".join("%.15e %.15e %.15e\n" % tuple(p) for p in xyz))
+    (d / "nelpts.info").write_text("".join("%d %d\n" % (a + 1, blocks[a]) for a in range(len(xyz))))
+    ncell = 40
+    cells = rng.integers(1, len(pts) + 1, (ncell, 4))
+    (d / "grid.1.ele").write_text("%d 4 0\n" % ncell + "".join("%d %d %d %d %d\n" % (i + 1, *c)
+                                                              for i, c in enumerate(cells)))
+    (d / "gimic.inp").write_text('calc=cdens\nbasis="MOL"\nxdens="XDENS"\nmagnet=[0.0, 0.0, 1.0]\n'
+                                 "Grid(file) {\n file=gridfile.grd\n}\n"
+                                 "Advanced {\n spherical=off\n screening=on\n screening_thrs=1.d-8\n}\n"
+                                 "Essential {\n prop=on\n}\n")
+    drv = driver.Driver(str(d / "gimic.inp"), precision=precision, stream=io.StringIO())
+    drv.run()
+    o = oracle.Oracle(mp, xp, screening=1e-8)
+    sig, chi = prop_oracle.integrands(o.jtensor(pts), pts, xyz)
+
+    def values(name):
+        text = open(d / name).read()
+        m = re.search(r'<DataArray Name="scalars"[^>]*>(.*?)</DataArray>', text, re.S)
+        return np.array(m.group(1).split(), dtype=np.float64)
+
+    def close(got, want):
+        # the path's error relative to the largest integrand, plus one unit
+        # of the e20.10 print (0.dddddddddd E+ee)
+        aw = np.abs(want)
+        ulp = np.where(aw > 0, 10.0 ** (np.floor(np.log10(np.where(aw > 0, aw, 1.0))) + 1.0 - 10.0), 0.0)
+        return np.all(np.abs(got - want) <= tol * aw.max() + ulp)
+
+    for k in range(len(xyz)):
+        assert close(values("sigma%d.vtu" % (k + 1)), sig[k].sum(axis=1)), k
+        for c, ax in enumerate(("xx", "yy", "zz")):
+            assert close(values("sigma_%s%d.vtu" % (ax, k + 1)), sig[k][:, c]), (k, ax)
+    assert close(values("intchi.vtu"), chi.sum(axis=1))
+    for c, ax in enumerate(("xx", "yy", "zz")):
+        assert close(values("intchi_%s.vtu" % ax), chi[:, c])

@@ -316,3 +316,39 @@ def test_zero_field_rejected_before_compute(c6h6):
     grd = ggrid.new_grid(i, mol.coords)
     with pytest.raises(ValueError, match="Magnetic field is zero"):
         ggrid.get_magnet(grd, i)
+
+
+def test_scalar_vtu_layout(tmp_path):
+    """write_scalar_unstructured follows write_vtk_scalar_unstructuredgrid
+    (src/fgimic/vtkplot.f90:318-390) record by record."""
+    from gimic_gb300 import vtk
+    pts = np.array([[0.0, 1.5, -2.25], [1e-3, 0.0, 3.0], [2.0, 2.0, 2.0], [-1.0, 0.5, 0.25], [0.0, 0.0, 0.0]])
+    val = np.array([1.25, -3.5e-7, 0.0, 42.0, -1.0])
+    cells = np.array([[1, 2, 3, 4], [2, 3, 4, 5]])
+    path = tmp_path / "s.vtu"
+    vtk.write_scalar_unstructured(str(path), pts, val, cells)
+    lines = path.read_text().split("\n")
+    assert lines[0] == '<?xml version="1.0"?>'
+    assert lines[3] == '    <Piece NumberOfPoints="         5" NumberOfCells="         2">'
+    pad = " " * 8  # the records' leading "(a, ...)" field
+    assert lines[6] == pad + "    0.0000000000E+00    0.1500000000E+01   -0.2250000000E+01"  # 3e20.10
+    assert lines[15] == pad + "    0.1250000000E+01"  # e20.10
+    assert lines[16] == pad + "   -0.3500000000E-06"
+    assert lines[24] == pad + "         0         1         2         3"  # 4i10, 0-based
+    assert lines[28] == pad + "         4         8"  # i10 offsets
+    assert lines[31] == pad + "   10   10"  # i5 types
+    assert lines[35] == pad + " 0.0 0.0"  # f4.1
+    assert lines[-2] == "</VTKFile>"
+
+
+def test_property_integrands_match_oracle_restatement():
+    """The per-point integrands written to the VTU files agree with the
+    oracle's restatement of jfield.f90:693-711 and :824-842."""
+    import prop_oracle
+    from gimic_gb300 import properties
+    rng = np.random.default_rng(0)
+    jt, pts, coord = rng.normal(size=(50, 9)), rng.normal(size=(50, 3)) * 3, rng.normal(size=(4, 3))
+    s1, c1 = properties.per_point(jt, pts, coord)
+    s2, c2 = prop_oracle.integrands(jt, pts, coord)
+    assert np.abs(s1 - s2).max() <= 1e-14 * np.abs(s2).max()
+    assert np.abs(c1 - c2).max() <= 1e-14 * np.abs(c2).max()
