@@ -1,9 +1,9 @@
 // Shell-blocked basis evaluation for the split-FP16 point operand.
 //
 // One CTA handles one tile of 128 consecutive points (the M tile of the
-// tensor-core contraction), one thread per point; in passes with fewer
-// tiles than two per SM the tile's K range is split over several CTAs
-// (gridDim.y), each staging and storing only its half K blocks.  All threads walk the
+// tensor-core contraction), one thread per point (passes with fewer tiles
+// than two per SM use basis_tile_short_kernel below, which splits a tile's
+// K range over several CTAs and a point's shells over four threads).  All threads walk the
 // shells in the same order (uniform control flow, shell data broadcast), so
 // each thread evaluates the radial factor of a shell once and then its
 // Cartesian components (bfeval.f90:81-122 with the per-shell screening of
@@ -83,9 +83,6 @@ struct Stager {
 
 }  // namespace
 
-// kSplit: the tile's K range is split over gridDim.y CTAs (small passes);
-// without it each CTA covers all K blocks and the range checks compile away.
-template <bool kSplit>
 __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_constant__ CUtensorMap tm_hi,
                                                                   const __grid_constant__ CUtensorMap tm_lo,
                                                                   DevBasis B, const double* __restrict__ pts,
@@ -98,24 +95,7 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
   const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBlockM;
   const int64_t p = min(m0 + row, npts - 1);  // rows past the end compute a copy; the TMA store clips them
   const int nkb = B.kpad / kBlockK;
-  // This CTA's half K blocks [hb0, hb1): a tile's K range is split over
-  // gridDim.y CTAs when there are few tiles (small passes), so that more SMs
-  // share the per-shell latency chain; with one CTA per tile it is all.
   const int nhb = 2 * nkb;
-  const int hb0 = kSplit ? static_cast<int>(static_cast<int64_t>(blockIdx.y) * nhb / gridDim.y) : 0;
-  const int hb1 = kSplit ? static_cast<int>(static_cast<int64_t>(blockIdx.y + 1) * nhb / gridDim.y) : nhb;
-  const int mu_lo = hb0 * kHalfK, mu_hi = hb1 * kHalfK;
-
-  // Small passes run one CTA per SM on cold caches, where every shell's
-  // table loads would be a chain of L2 round trips: all threads first pull
-  // the tables into L1 (a few KB; in large passes they are resident anyway).
-  if (kSplit) {
-    prefetch_l1(B.sh_pack, B.nshells * sizeof(int4));
-    prefetch_l1(B.sh_rad2_df, B.nshells * sizeof(float2));
-    prefetch_l1(B.p_pack, B.nprim * sizeof(float4));
-    prefetch_l1(B.atom_df, B.natoms * 3 * sizeof(float2));
-    prefetch_l1(B.f_ijk, B.nbf * sizeof(int));
-  }
 
   // active K blocks of this tile (all when no screening lists are given)
   uint64_t kb_on = ~0ull;
@@ -153,12 +133,12 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
     const int e = static_cast<int>(floorf(lb + 0.05f)) + 1;
     scale = ldexpf(1.f, max(-120, min(120, 14 - e)));
   }
-  if ((!kSplit || blockIdx.y == 0) && m0 + row < npts) inv_scale[m0 + row] = 1.f / scale;
+  if (m0 + row < npts) inv_scale[m0 + row] = 1.f / scale;
 
   // ---- pass 2: values, staged per K block and stored with TMA -------------
   Stager st{base, row, __float2half_rn(0.f), __float2half_rn(0.f)};
-  int kb = hb0;  // the half block being staged
-  bool active = hb0 < hb1 && ((kb_on >> (hb0 >> 1)) & 1ull);
+  int kb = 0;  // the half block being staged
+  bool active = (kb_on & 1ull) != 0;
   auto flush = [&](int k) {  // all threads: the K block k is complete in the buffer
     fence_proxy_async();
     __syncthreads();
@@ -174,11 +154,10 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
     while (kb < k) {
       if (active) flush(kb);
       ++kb;
-      active = kb < hb1 && ((kb_on >> (kb >> 1)) & 1ull);
+      active = kb < nhb && ((kb_on >> (kb >> 1)) & 1ull);
     }
   };
   auto emit = [&](int mu, float v, bool zero) {
-    if (kSplit && (mu < mu_lo || mu >= mu_hi)) return;  // another CTA's half blocks
     const int k = mu / kHalfK;
     if (k != kb) advance_to(k);
     if (!active) return;
@@ -199,8 +178,6 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
     for (int sh = 0; sh < B.nshells; ++sh) {
       const int4 pk = __ldg(B.sh_pack + sh);  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
       const int mu0 = pk.y, ncomp = pk.z & 0xff, np = (pk.z >> 8) & 0xff;
-      if (kSplit && mu0 + ncomp <= mu_lo) continue;  // shells are in function order
-      if (kSplit && mu0 >= mu_hi) break;
       const int k_first = mu0 >> 6, k_last = (mu0 + ncomp - 1) >> 6;
       // skip whole shells whose K blocks are inactive for the tile
       if (!((kb_on >> k_first) & 1ull) && !((kb_on >> k_last) & 1ull)) continue;
@@ -242,8 +219,145 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
       }
     }
     // padding columns nbf .. kpad-1 of the last K block are zero
-    for (int mu = max(B.nbf, mu_lo); mu < min(B.kpad, mu_hi); ++mu) emit(mu, 0.f, true);
-    advance_to(hb1);
+    for (int mu = B.nbf; mu < B.kpad; ++mu) emit(mu, 0.f, true);
+    advance_to(nhb);
+  }
+  if (threadIdx.x == 0) bulk_wait_all();
+}
+
+// Short passes (fewer tiles than two per SM): the row-by-row shell walk of
+// basis_tile_kernel is a latency chain that one CTA per SM cannot hide.
+// Here a tile's half K blocks are split over gridDim.y CTAs, and within a
+// CTA four threads share a point (512 threads): thread sub of the point walks
+// the shells sub, sub + 4, ... of each half block and stages its components
+// one fp16 at a time; every column of the half block is written by exactly
+// one thread.  The arithmetic of every value is that of basis_tile_kernel,
+// so both kernels give the same operand bit for bit.
+constexpr int kSubs = 4;
+constexpr int kShortThreads = kBlockM * kSubs;
+
+__global__ void __launch_bounds__(kShortThreads) basis_tile_short_kernel(
+    const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo, DevBasis B,
+    const double* __restrict__ pts, int64_t npts, const int* __restrict__ tiles, int stride,
+    float* __restrict__ inv_scale) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ float s_scale[kBlockM];
+  const int row = threadIdx.x & (kBlockM - 1), sub = threadIdx.x >> 7;  // sub is uniform in a warp
+  const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBlockM;
+  const int64_t p = min(m0 + row, npts - 1);  // rows past the end compute a copy; the TMA store clips them
+  const int nhb = 2 * (B.kpad / kBlockK);
+  const int hb0 = static_cast<int>(static_cast<int64_t>(blockIdx.y) * nhb / gridDim.y);
+  const int hb1 = static_cast<int>(static_cast<int64_t>(blockIdx.y + 1) * nhb / gridDim.y);
+  // one CTA per SM on cold caches: pull the tables into L1 first
+  prefetch_l1(B.sh_pack, B.nshells * sizeof(int4));
+  prefetch_l1(B.sh_rad2_df, B.nshells * sizeof(float2));
+  prefetch_l1(B.p_pack, B.nprim * sizeof(float4));
+  prefetch_l1(B.atom_df, B.natoms * 3 * sizeof(float2));
+  prefetch_l1(B.f_ijk, B.nbf * sizeof(int));
+  prefetch_l1(B.f_shell, B.nbf * sizeof(int));
+  uint64_t kb_on = ~0ull;
+  if (tiles) {
+    const int* tl = tiles + blockIdx.x * static_cast<int64_t>(stride);
+    const int nk = tl[1];
+    const int* kl = tl + 2 + B.nchunk;
+    kb_on = 0;
+    for (int i = 0; i < nk; ++i) kb_on |= 1ull << kl[i];
+  }
+  DFloat r[3];
+  for (int c = 0; c < 3; ++c) r[c] = df_split(pts[3 * p + c]);
+  // the row scale, as in basis_tile_kernel, by the first thread of each point
+  if (sub == 0) {
+    float lb = -INFINITY;
+    const float* __restrict__ env = B.atom_env;
+    const int nb = B.env_bins;
+    for (int a = 0; a < B.natoms; ++a) {
+      const float dx = r[0].h - __ldg(&B.atom_df[3 * a].x), dy = r[1].h - __ldg(&B.atom_df[3 * a + 1].x),
+                  dz = r[2].h - __ldg(&B.atom_df[3 * a + 2].x);
+      const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const float t = (__log2f(fmaxf(d2, 1e-30f)) + kEnvOffset) * kEnvPerOctave;
+      const int bin = t <= 0.f ? 0 : static_cast<int>(t);
+      if (bin < nb) lb = fmaxf(lb, __ldg(env + static_cast<int64_t>(a) * nb + bin));
+    }
+    float scale = 1.f;
+    if (lb > -INFINITY) {
+      const int e = static_cast<int>(floorf(lb + 0.05f)) + 1;
+      scale = ldexpf(1.f, max(-120, min(120, 14 - e)));
+    }
+    s_scale[row] = scale;
+    if (blockIdx.y == 0 && m0 + row < npts) inv_scale[m0 + row] = 1.f / scale;
+  }
+  __syncthreads();
+  const float scale = s_scale[row];
+  auto put = [&](int col, __half h, __half l) {
+    const uint32_t o = swz(row, col);
+    *reinterpret_cast<__half*>(base + o) = h;
+    *reinterpret_cast<__half*>(base + kStageBytes + o) = l;
+  };
+  const __half z = __float2half_rn(0.f);
+  int cur_atom = -1;
+  float px[4] = {1.f, 0.f, 0.f, 0.f}, py[4] = {1.f, 0.f, 0.f, 0.f}, pz[4] = {1.f, 0.f, 0.f, 0.f};
+  DFloat d2{0.f, 0.f};
+  for (int hb = hb0; hb < hb1; ++hb) {
+    if (!((kb_on >> (hb >> 1)) & 1ull)) continue;  // inactive for the tile: never read
+    const int lo = hb * kHalfK, hi = min(lo + kHalfK, B.nbf);
+    if (sub == 0)
+      for (int mu = max(lo, B.nbf); mu < lo + kHalfK; ++mu) put(mu - lo, z, z);  // padding columns
+    if (lo < B.nbf) {
+      for (int sh = __ldg(B.f_shell + lo) + sub; sh < B.nshells; sh += kSubs) {
+        const int4 pk = __ldg(B.sh_pack + sh);  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
+        const int mu0 = pk.y, ncomp = pk.z & 0xff, np = (pk.z >> 8) & 0xff;
+        if (mu0 >= hi) break;  // shells are in function order
+        const int c0 = max(0, lo - mu0), c1 = min(ncomp, hi - mu0);
+        if (pk.x != cur_atom) {
+          cur_atom = pk.x;
+          float s3[3];
+          d2 = atom_offset(r, B.atom_df, pk.x, s3);
+          px[1] = s3[0];
+          py[1] = s3[1];
+          pz[1] = s3[2];
+          px[2] = px[1] * px[1];
+          py[2] = py[1] * py[1];
+          pz[2] = pz[1] * pz[1];
+          px[3] = px[2] * px[1];
+          py[3] = py[2] * py[1];
+          pz[3] = pz[2] * pz[1];
+        }
+        float f1 = 0.f;
+        const bool in_range = df_le(d2, __ldg(B.sh_rad2_df + sh));
+        if (in_range) {
+          for (int k = 0; k < np; ++k) {
+            const float4 pr = __ldg(B.p_pack + pk.w + k);
+            f1 += pr.z * gauss_df(pr.x, pr.y, d2.h, d2.l);
+          }
+          f1 *= scale;
+        }
+        if (!__any_sync(0xffffffffu, in_range)) {
+          for (int c = c0; c < c1; ++c) put(mu0 + c - lo, z, z);
+          continue;
+        }
+        for (int c = c0; c < c1; ++c) {
+          const int ijk = __ldg(B.f_ijk + mu0 + c);
+          const int i = ijk & 15, j = (ijk >> 4) & 15, k = (ijk >> 8) & 15;
+          const float xi = i == 0 ? 1.f : (i == 1 ? px[1] : (i == 2 ? px[2] : px[3]));
+          const float yj = j == 0 ? 1.f : (j == 1 ? py[1] : (j == 2 ? py[2] : py[3]));
+          const float zk = k == 0 ? 1.f : (k == 1 ? pz[1] : (k == 2 ? pz[2] : pz[3]));
+          const float v = xi * yj * zk * f1;
+          const __half h = __float2half_rn(v);
+          put(mu0 + c - lo, h, __float2half_rn(v - __half2float(h)));
+        }
+      }
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store_2d(&tm_hi, base, hb * kHalfK, static_cast<int>(m0));
+      tma_store_2d(&tm_lo, base + kStageBytes, hb * kHalfK, static_cast<int>(m0));
+      bulk_commit();
+      bulk_wait_read_0();
+    }
+    __syncthreads();
   }
   if (threadIdx.x == 0) bulk_wait_all();
 }
@@ -257,9 +371,9 @@ cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* 
   static PerDevice pd;
   int nsm = 0;
   cudaError_t e = once_per_device(pd, &nsm, [](int dev, int* sms) {
-    cudaError_t r = cudaFuncSetAttribute(basis_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+    cudaError_t r = cudaFuncSetAttribute(basis_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
     if (r == cudaSuccess)
-      r = cudaFuncSetAttribute(basis_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+      r = cudaFuncSetAttribute(basis_tile_short_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
     if (r != cudaSuccess) return r;
     return cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
   });
@@ -272,8 +386,12 @@ cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* 
   int kgroups = 1;
   if (nsm > 0 && ntiles < 2 * nsm) kgroups = static_cast<int>(std::min<int64_t>(nhb, (2 * nsm + ntiles - 1) / ntiles));
   const dim3 grid(static_cast<unsigned>(ntiles), static_cast<unsigned>(kgroups));
-  auto kernel = kgroups > 1 ? basis_tile_kernel<true> : basis_tile_kernel<false>;
-  kernel<<<grid, kTileThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
+  if (kgroups > 1)
+    basis_tile_short_kernel<<<grid, kShortThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
+                                                                   *static_cast<const CUtensorMap*>(tm_lo), B, pts,
+                                                                   npts, tiles, stride, inv_scale);
+  else
+    basis_tile_kernel<<<grid, kTileThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
                                                             *static_cast<const CUtensorMap*>(tm_lo), B, pts, npts,
                                                             tiles, stride, inv_scale);
   return cudaGetLastError();

@@ -40,16 +40,24 @@ __device__ __forceinline__ void point_terms(const double* t, const double* rr, c
   acc[6] += (0.3333333 * (xx * xx + yy * yy + zz * zz) + 0.5 * (xy * xy + xz * xz + yz * yz)) * w;
 }
 
+// The block's sums of the seven quantities: a fixed butterfly within each
+// warp, then the warps' results in warp order (one barrier), times w_j.
 __device__ __forceinline__ void block_reduce_store(double acc[kQ], double wj, double* dst) {
-  __shared__ double red[kQ][kRowThreads];
-  for (int q = 0; q < kQ; ++q) red[q][threadIdx.x] = acc[q];
-  __syncthreads();
-  for (int s = kRowThreads / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s)
-      for (int q = 0; q < kQ; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + s];
-    __syncthreads();
+  __shared__ double red[kRowThreads / 32][kQ];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < kQ; ++q) {
+    double v = acc[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][q] = v;
   }
-  if (threadIdx.x < kQ) dst[threadIdx.x] = red[threadIdx.x][0] * wj;
+  __syncthreads();
+  if (threadIdx.x < kQ) {
+    double v = red[0][threadIdx.x];
+    for (int w = 1; w < kRowThreads / 32; ++w) v += red[w][threadIdx.x];
+    dst[threadIdx.x] = v * wj;
+  }
 }
 
 // One block per row of one plane of a batch: the row's sums over i (fixed
