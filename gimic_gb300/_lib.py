@@ -65,6 +65,8 @@ SIGNATURES = {
     "gg_au2si": (C.c_double, [C.c_double]),
     "gg_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "gg_profile_blocks": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "gg_plane_integrals_batch": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.POINTER(GridSpec)), _ip, C.c_int,
+                                           C.c_int, _dp, _dp, C.c_void_p]),
     "gg_selftest_wait_timeout": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double), C.c_void_p]),
     "gg_selftest_fail_next": (C.c_int, [C.c_void_p, C.c_int]),
     "gg_jtensor_batch_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,

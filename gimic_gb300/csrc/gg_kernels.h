@@ -64,6 +64,28 @@ struct TcArgs {
 };
 int tc_smem_bytes();
 
+// One job of a multi-job contraction launch: one molecule's pass, with the
+// operands, tables and outputs that a single-job launch takes as
+// arguments.  Lives in device memory (the tensor maps are read from there
+// by the TMA unit).  Steps of all jobs are numbered in table order: job j
+// owns its ntiles steps from step0 on.
+struct TcJob {
+  alignas(64) unsigned char tmap[4][128];  // CUtensorMap: point operand hi, lo; matrix operand hi, lo
+  DevBasis B;
+  const float* inv_row;
+  const float* inv_col;
+  const double* pts;
+  int64_t npts;
+  Outputs out;
+  const int* tiles;
+  int tstride;
+  const int* perm;
+  const int* tile_order;
+  int64_t step0;
+  int* left;                    // 4 x ntiles quarter tiles still to finish (null: no timing)
+  unsigned long long* done_ns;  // global timer (ns) when the last of them finished
+};
+
 // Spatial ordering and tile screening (k_tiles.cu)
 int tile_stride(const DevBasis& B);
 size_t sort_temp_bytes(int64_t n);
@@ -78,6 +100,10 @@ size_t tile_order_temp_bytes(int64_t ntiles);
 cudaError_t launch_tile_order(const int* tiles, int64_t ntiles, int stride, uint32_t* work, uint32_t* work_sorted,
                               int* ids, int* order, void* temp, size_t temp_bytes, cudaStream_t st);
 cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st);
+// One persistent launch over njobs jobs (device table), nsteps tiles in all;
+// div: the jobs' outputs include div j (all jobs alike).
+cudaError_t launch_tc_fused_multi(const TcJob* jobs, int njobs, int64_t nsteps, Flags flags, bool div, int* err,
+                                  int* tile_counter, cudaStream_t st);
 
 // Many planes at once: plane q owns points [pt_off, pt_off + p1*p2*p3) of jt
 // and pts, and weights w[w_off ..] (p1 values, then p2, then p3).
@@ -116,6 +142,9 @@ void launch_properties(const double* jt, const double* pts, const double* w, con
 // it waited goes to *waited_ns (device memory, may be null).
 cudaError_t launch_wait_timeout(int* err, uint64_t limit_ns, int code, unsigned long long* waited_ns,
                                 cudaStream_t st);
+
+// One global-timer stamp in *p (k_diag.cu).
+cudaError_t launch_stamp(unsigned long long* p, cudaStream_t st);
 
 // Integration proposal network (k_mlp.cu): 5 -> 64 -> 64 -> 1, SiLU.
 constexpr int kMlpIn = 5;

@@ -30,4 +30,13 @@ cudaError_t launch_wait_timeout(int* err, uint64_t limit_ns, int code, unsigned 
   return cudaGetLastError();
 }
 
+// One global-timer stamp (ns) on the stream, e.g. the start of a launch
+// whose kernels stamp their own completion.
+__global__ void stamp_kernel(unsigned long long* p) { *p = global_ns(); }
+
+cudaError_t launch_stamp(unsigned long long* p, cudaStream_t st) {
+  stamp_kernel<<<1, 1, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
 }  // namespace gg

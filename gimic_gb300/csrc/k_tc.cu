@@ -29,6 +29,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cstring>
 
 #include "gg_cart.cuh"
 #include "gg_combine.cuh"
@@ -97,6 +98,35 @@ static_assert(dot_matrix(12) == 0 && dot_matrix(13) == 1 && dot_matrix(21) == 3 
 // the Laplacian sums, used only by div j
 __host__ __device__ constexpr bool is_div_sum(int i) { return (i >= 22 && i < 25) || i >= 34; }
 
+// What a step needs of its job (one pass over one molecule's points): the
+// operands' tensor maps and the tile lists for the producer and the MMA
+// issuer, the tables, scales, points and outputs for the epilogue.  A
+// single-job launch takes them from the kernel parameters, a multi-job
+// launch from the job table in global memory.
+struct JobView {
+  const void *a_hi, *a_lo, *b_hi, *b_lo;  // CUtensorMap
+  const int* tiles;
+  int tstride, nchunk, nkb;
+  const int* tile_order;
+  int64_t step0, npts;
+};
+struct EpiView {
+  int nbf, nshells;
+  const int* fpack;
+  const int4* shp;
+  const float2* shr;
+  const float4* prm;
+  const float2* atm;
+  const float* icol;
+  const float* inv_row;
+  const double* pts;
+  const int* perm;
+  int64_t npts;
+  Outputs out;
+  int* left;
+  unsigned long long* done_ns;
+};
+
 __device__ __forceinline__ void kahan_add(float& hi, float& lo, float y) {
   const float t = hi + y;
   lo = y - (t - hi);
@@ -116,7 +146,13 @@ int tc_smem_bytes() { return kSmemBytes; }
 // kDiv: the divergence sums (Laplacian terms) are accumulated only when the
 // caller asked for div j; without them each function costs 6 FMAs, the
 // Laplacian and one FMA per primitive less.
-template <bool kDiv>
+//
+// kMulti: one launch over several jobs (the molecules of a batch), whose
+// operands and tables come from the job table `jobs` (njobs entries); steps
+// are numbered across the jobs in table order (job j owns the steps from
+// jobs[j].step0), so the persistent CTAs run on from one molecule into the
+// next.  The single-job parameters are then unused.
+template <bool kDiv, bool kMulti>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_fused_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_constant__ CUtensorMap tm_a_lo,
                     const __grid_constant__ CUtensorMap tm_b_hi, const __grid_constant__ CUtensorMap tm_b_lo,
@@ -124,7 +160,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const double* __restrict__ pts, int64_t npts, Flags fl, Outputs out, int* err,
                     const int* __restrict__ tiles, int tstride, const int* __restrict__ perm,
                     const int* __restrict__ tile_order, int* __restrict__ tile_counter, int csplit,
-                    float2* __restrict__ part, unsigned* __restrict__ tile_done) {
+                    float2* __restrict__ part, unsigned* __restrict__ tile_done, const TcJob* __restrict__ jobs,
+                    int njobs, int64_t multi_steps) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                          ~static_cast<uintptr_t>(1023));
@@ -139,20 +176,61 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* ring_empty = ring_full + kRing;
   uint64_t* drain = ring_empty + kRing;      // the MMA issuer's last MMAs, after an error
   int* ring = reinterpret_cast<int*>(drain + 1);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ring + kRing);
+  int* ring_job = ring + kRing;  // the job of each handed step
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ring_job + kRing);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t ntiles = (npts + kBlockM - 1) / kBlockM;
   // A step is one tile (csplit == 1) or one active chunk of a tile (the
   // chunk split of short passes: step t is chunk t % csplit of tile
-  // t / csplit, and csplit is the chunk count of the basis).
-  const int64_t nsteps = ntiles * csplit;
-  const int nchunk_all = Bs.nchunk, nkb_all = Bs.kpad / kBlockK;
+  // t / csplit, and csplit is the chunk count of the basis).  A multi-job
+  // launch has csplit == 1 and multi_steps tiles over all jobs.
+  const int64_t nsteps = kMulti ? multi_steps : ((npts + kBlockM - 1) / kBlockM) * csplit;
+  // the job of step t (a binary search over the jobs' first steps)
+  auto job_of = [&](int64_t t) -> int {
+    if (!kMulti) return 0;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].step0 <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  };
+  auto view = [&](int j) -> JobView {
+    JobView v;
+    if (kMulti) {
+      const TcJob& J = jobs[j];
+      v.a_hi = J.tmap[0];
+      v.a_lo = J.tmap[1];
+      v.b_hi = J.tmap[2];
+      v.b_lo = J.tmap[3];
+      v.tiles = J.tiles;
+      v.tstride = J.tstride;
+      v.nchunk = J.B.nchunk;
+      v.nkb = J.B.kpad / kBlockK;
+      v.tile_order = J.tile_order;
+      v.step0 = J.step0;
+      v.npts = J.npts;
+    } else {
+      v.a_hi = &tm_a_hi;
+      v.a_lo = &tm_a_lo;
+      v.b_hi = &tm_b_hi;
+      v.b_lo = &tm_b_lo;
+      v.tiles = tiles;
+      v.tstride = tstride;
+      v.nchunk = Bs.nchunk;
+      v.nkb = Bs.kpad / kBlockK;
+      v.tile_order = tile_order;
+      v.step0 = 0;
+      v.npts = npts;
+    }
+    return v;
+  };
   // the tile of step t, and its active column chunks and K blocks (all of
   // them without a screening list; no chunk at all without a K block)
-  auto tile_of = [&](int64_t t) -> int64_t {
-    const int64_t u = t / csplit;
-    return tile_order ? static_cast<int64_t>(tile_order[u]) : u;
+  auto tile_of = [&](const JobView& v, int64_t t) -> int64_t {
+    const int64_t u = (t - v.step0) / csplit;
+    return v.tile_order ? static_cast<int64_t>(v.tile_order[u]) : u;
   };
   // the chunks [c0, c1) of the tile's active list that step t covers
   auto chunk_span = [&](int64_t t, int nchunk, int* c0, int* c1) {
@@ -165,19 +243,58 @@ __global__ void __launch_bounds__(kThreads, 1)
       *c1 = g < nchunk ? g + 1 : g;
     }
   };
-  auto n_kb = [&](int64_t tile) -> int { return tiles ? tiles[tile * tstride + 1] : nkb_all; };
-  auto n_chunk = [&](int64_t tile, int nk) -> int { return nk > 0 ? (tiles ? tiles[tile * tstride] : nchunk_all) : 0; };
-  auto chunk_at = [&](int64_t tile, int i) -> int { return tiles ? tiles[tile * tstride + 2 + i] : i; };
-  auto kb_at = [&](int64_t tile, int i) -> int { return tiles ? tiles[tile * tstride + 2 + nchunk_all + i] : i; };
+  auto n_kb = [&](const JobView& v, int64_t tile) -> int { return v.tiles ? v.tiles[tile * v.tstride + 1] : v.nkb; };
+  auto n_chunk = [&](const JobView& v, int64_t tile, int nk) -> int {
+    return nk > 0 ? (v.tiles ? v.tiles[tile * v.tstride] : v.nchunk) : 0;
+  };
+  auto chunk_at = [&](const JobView& v, int64_t tile, int i) -> int {
+    return v.tiles ? v.tiles[tile * v.tstride + 2 + i] : i;
+  };
+  auto kb_at = [&](const JobView& v, int64_t tile, int i) -> int {
+    return v.tiles ? v.tiles[tile * v.tstride + 2 + v.nchunk + i] : i;
+  };
   auto failed = [&]() -> bool { return *reinterpret_cast<volatile int*>(err) != 0; };
   // epilogue tables: matrix scales, per-function records (shell << 12 |
-  // Cartesian case), shell records, primitives, atoms
-  const float* icol = inv_col;
-  const int* fpack = Bs.f_pack;
-  const int4* shp = Bs.sh_pack;
-  const float2* shr = Bs.sh_rad2_df;
-  const float4* prm = Bs.p_pack;
-  const float2* atm = Bs.atom_df;
+  // Cartesian case), shell records, primitives, atoms; the points, their
+  // scales and order, the outputs
+  auto epi_view = [&](int j) -> EpiView {
+    EpiView e;
+    if (kMulti) {
+      const TcJob& J = jobs[j];
+      e.nbf = J.B.nbf;
+      e.nshells = J.B.nshells;
+      e.fpack = J.B.f_pack;
+      e.shp = J.B.sh_pack;
+      e.shr = J.B.sh_rad2_df;
+      e.prm = J.B.p_pack;
+      e.atm = J.B.atom_df;
+      e.icol = J.inv_col;
+      e.inv_row = J.inv_row;
+      e.pts = J.pts;
+      e.perm = J.perm;
+      e.npts = J.npts;
+      e.out = J.out;
+      e.left = J.left;
+      e.done_ns = J.done_ns;
+    } else {
+      e.nbf = Bs.nbf;
+      e.nshells = Bs.nshells;
+      e.fpack = Bs.f_pack;
+      e.shp = Bs.sh_pack;
+      e.shr = Bs.sh_rad2_df;
+      e.prm = Bs.p_pack;
+      e.atm = Bs.atom_df;
+      e.icol = inv_col;
+      e.inv_row = inv_row;
+      e.pts = pts;
+      e.perm = perm;
+      e.npts = npts;
+      e.out = out;
+      e.left = nullptr;
+      e.done_ns = nullptr;
+    }
+    return e;
+  };
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
@@ -209,35 +326,46 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int it = 0;  // stages issued
       bool clean = false;
+      int cur_job = -1;
       for (int step = 0;; ++step) {
         // next tile step from the global queue, handed to the other roles
         const int slot = step % kRing;
         if (!mbar_wait(&ring_empty[slot], ((step / kRing) & 1) ^ 1, err, 7)) goto producer_exit;
         const int64_t t = failed() ? nsteps : static_cast<int64_t>(atomicAdd(tile_counter, 1));
+        const int j = t < nsteps ? job_of(t) : 0;
         ring[slot] = t < nsteps ? static_cast<int>(t) : -1;
+        ring_job[slot] = j;
         mbar_arrive(&ring_full[slot]);
         if (t >= nsteps) {
           clean = true;
           break;
         }
-        const int64_t tile = tile_of(t);
+        const JobView v = view(j);
+        if (kMulti && j != cur_job) {
+          // the job's tensor maps live in global memory (written by the
+          // host before the launch): acquire them for the TMA unit
+          cur_job = j;
+          for (const void* m : {v.a_hi, v.a_lo, v.b_hi, v.b_lo})
+            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(m) : "memory");
+        }
+        const int64_t tile = tile_of(v, t);
         const int m0 = static_cast<int>(tile * kBlockM);
-        const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
+        const int nkb = n_kb(v, tile), nchunk = n_chunk(v, tile, nkb);
         int c0, c1;
         chunk_span(t, nchunk, &c0, &c1);
         for (int ci = c0; ci < c1; ++ci) {
-          const int c = chunk_at(tile, ci);
+          const int c = chunk_at(v, tile, ci);
           // cross pass: (A_hi, B_lo) then (A_lo, B_hi) of every K block;
           // main pass: (A_hi, B_hi) of every K block; one pair per stage
           for (int q = 0; q < 3 * nkb; ++q, ++it) {
-            const int kb = kb_at(tile, q < 2 * nkb ? q >> 1 : q - 2 * nkb);
+            const int kb = kb_at(v, tile, q < 2 * nkb ? q >> 1 : q - 2 * nkb);
             const bool a_lo = q < 2 * nkb && (q & 1), b_lo = q < 2 * nkb && !(q & 1);
             const int s = it % kStages, round = it / kStages;
             if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto producer_exit;
             unsigned char* st = base + s * kStageBytes;
             mbar_expect_tx(&full[s], kStageBytes);
-            tma_load_2d(st, a_lo ? &tm_a_lo : &tm_a_hi, &full[s], kb * kBlockK, m0);
-            tma_load_2d(st + kTileA, b_lo ? &tm_b_lo : &tm_b_hi, &full[s], kb * kBlockK, c * kBlockN);
+            tma_load_2d(st, a_lo ? v.a_lo : v.a_hi, &full[s], kb * kBlockK, m0);
+            tma_load_2d(st + kTileA, b_lo ? v.b_lo : v.b_hi, &full[s], kb * kBlockK, c * kBlockN);
           }
         }
       }
@@ -256,14 +384,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int step = 0;; ++step) {
         const int slot = step % kRing;
         if (!mbar_wait(&ring_full[slot], (step / kRing) & 1, err, 8)) goto mma_exit;
-        const int t = ring[slot];
+        const int t = ring[slot], j = ring_job[slot];
         mbar_arrive(&ring_empty[slot]);
         if (t < 0) {
           clean = true;
           break;
         }
-        const int64_t tile = tile_of(t);
-        const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
+        const JobView v = view(j);
+        const int64_t tile = tile_of(v, t);
+        const int nkb = n_kb(v, tile), nchunk = n_chunk(v, tile, nkb);
         int c0, c1;
         chunk_span(t, nchunk, &c0, &c1);
         for (int ci = c0; ci < c1; ++ci, ++acc) {
@@ -309,18 +438,20 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int step = 0; ok; ++step, ++tk) {
       const int slot = step % kRing;
       if (!mbar_wait(&ring_full[slot], (step / kRing) & 1, err, 9)) break;
-      const int t = ring[slot];
+      const int t = ring[slot], j = ring_job[slot];
       __syncwarp();
       if (lane == 0) mbar_arrive(&ring_empty[slot]);
       if (t < 0) break;
-      const int64_t tile = tile_of(t);
+      const JobView v = view(j);
+      const EpiView ev = epi_view(j);
+      const int64_t tile = tile_of(v, t);
       const int64_t p = tile * kBlockM + row;
-      const bool valid = p < npts;
+      const bool valid = p < ev.npts;
       double r[3] = {0.0, 0.0, 0.0};
       if (valid) {
-        r[0] = pts[3 * p];
-        r[1] = pts[3 * p + 1];
-        r[2] = pts[3 * p + 2];
+        r[0] = ev.pts[3 * p];
+        r[1] = ev.pts[3 * p + 1];
+        r[2] = ev.pts[3 * p + 2];
       }
       const DFloat rdf[3] = {df_split(r[0]), df_split(r[1]), df_split(r[2])};
       float thi[kNDots], tlo[kNDots];
@@ -337,11 +468,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       CartPow cp = cart_pow(0.f, 0.f, 0.f);
       DFloat d2a{0.f, 0.f};
       bool on = false, warp_on = false;
-      const int nkb = n_kb(tile), nchunk = n_chunk(tile, nkb);
+      const int nkb = n_kb(v, tile), nchunk = n_chunk(v, tile, nkb);
       int c0, c1;
       chunk_span(t, nchunk, &c0, &c1);
       for (int ci = c0; ci < c1; ++ci, ++acc) {
-        const int c = chunk_at(tile, ci);
+        const int c = chunk_at(v, tile, ci);
         const int b = acc & 1, rb = acc >> 1;
         if (!mbar_wait(&accfull[b], rb & 1, err, 4)) {
           ok = false;
@@ -353,30 +484,30 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int i = 0; i < kNDots; ++i) part[i] = tlo[i];
         const int f0 = c * kChunkF;
         const int mb = f0 + half * (kChunkF / 2);
-        const int me = min(mb + kChunkF / 2, Bs.nbf);
+        const int me = min(mb + kChunkF / 2, ev.nbf);
         const uint32_t tcol = lane_base + b * kAccStride;
-        int fp_next = mb < me ? fpack[mb] : 0;
+        int fp_next = mb < me ? ev.fpack[mb] : 0;
 #pragma unroll 1
         for (int mu = mb; mu < me; ++mu) {
           const int u = mu - f0;
           const int fp = fp_next;
-          if (mu + 1 < me) fp_next = fpack[mu + 1];
+          if (mu + 1 < me) fp_next = ev.fpack[mu + 1];
           const int sh = fp >> 12;
           if (sh != cur_shell) {
             cur_shell = sh;
             const bool hit = sh == sh_pre;
-            const int4 pk = hit ? pk_pre : shp[sh];  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
-            const float2 rad = hit ? rad_pre : shr[sh];
-            if (sh + 1 < Bs.nshells) {
+            const int4 pk = hit ? pk_pre : ev.shp[sh];  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
+            const float2 rad = hit ? rad_pre : ev.shr[sh];
+            if (sh + 1 < ev.nshells) {
               sh_pre = sh + 1;
-              pk_pre = shp[sh + 1];
-              rad_pre = shr[sh + 1];
+              pk_pre = ev.shp[sh + 1];
+              rad_pre = ev.shr[sh + 1];
             }
             const int a = pk.x;
             if (a != cur_atom) {
               cur_atom = a;
               float s3[3];
-              d2a = atom_offset_t(rdf, atm, a, s3);
+              d2a = atom_offset_t(rdf, ev.atm, a, s3);
               sx = s3[0];
               sy = s3[1];
               sz = s3[2];
@@ -390,7 +521,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               const int last = min(me, pk.y + (pk.z & 0xff)) - 1;
               if (last > mu) {
                 mu = last;
-                fp_next = mu + 1 < me ? fpack[mu + 1] : 0;
+                fp_next = mu + 1 < me ? ev.fpack[mu + 1] : 0;
               }
               continue;
             }
@@ -398,7 +529,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (on) {
               const int np = (pk.z >> 8) & 0xff;
               for (int k = 0; k < np; ++k) {
-                const float4 pr = prm[pk.w + k];  // exponent hi, exponent lo, coefficient
+                const float4 pr = ev.prm[pk.w + k];  // exponent hi, exponent lo, coefficient
                 const float al = pr.x;
                 const float e = pr.z * gauss_df(al, pr.y, d2a.h, d2a.l);
                 f1 += e;
@@ -512,10 +643,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (finish && valid) {
           // the row scale and the matrix scales are powers of two: scaling
           // a double-float is exact.  Sum i belongs to matrix dot_matrix(i).
-          const float sc = inv_row[p];
+          const float sc = ev.inv_row[p];
           float msc[kMats];
 #pragma unroll
-          for (int m = 0; m < kMats; ++m) msc[m] = sc * icol[m];
+          for (int m = 0; m < kMats; ++m) msc[m] = sc * ev.icol[m];
           const bool own = csplit == 1;  // the other half's sums still to add
           auto tot = [&](int i) -> DFloat {
             const float2 o = own ? h1[i] : make_float2(0.f, 0.f);
@@ -523,20 +654,26 @@ __global__ void __launch_bounds__(kThreads, 1)
             const float f = msc[dot_matrix(i)];
             return DFloat{t.h * f, t.l * f};
           };
-          const int64_t o = perm ? static_cast<int64_t>(perm[p]) : p;  // caller's point order
+          const int64_t o = ev.perm ? static_cast<int64_t>(ev.perm[p]) : p;  // caller's point order
           if (fl.giao && fl.dia && fl.para) {
-            combine_point_df(tot, rdf, [&](int k, DFloat v) { store_output(out, o, k, df_to_double(v)); });
+            combine_point_df(tot, rdf, [&](int k, DFloat x) { store_output(ev.out, o, k, df_to_double(x)); });
           } else {
             double td[kNDots], ct[9], dv[3];
 #pragma unroll
             for (int i = 0; i < kNDots; ++i) td[i] = df_to_double(tot(i));
             combine_point(td, r, fl, ct, dv);
 #pragma unroll
-            for (int k = 0; k < 9; ++k) store_output(out, o, k, ct[k]);
+            for (int k = 0; k < 9; ++k) store_output(ev.out, o, k, ct[k]);
 #pragma unroll
-            for (int k = 0; k < 3; ++k) store_output(out, o, 9 + k, dv[k]);
+            for (int k = 0; k < 3; ++k) store_output(ev.out, o, 9 + k, dv[k]);
           }
-          store_density(out, o, df_to_double(tot(0)));
+          store_density(ev.out, o, df_to_double(tot(0)));
+        }
+        if (kMulti && ev.left) {
+          // per-job completion time: the last of the job's 4 x ntiles
+          // quarter tiles to finish stamps the global timer
+          __syncwarp();
+          if (lane == 0 && atomicSub(ev.left, 1) == 1) *ev.done_ns = global_ns();
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(xempty);
@@ -548,11 +685,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     // load: in a short pass each SM sees one or two tiles on cold caches,
     // where every shell change would otherwise wait on a chain of L2 loads.
     const int t = threadIdx.x - 64;
-    prefetch_l1(Bs.f_pack, Bs.nbf * sizeof(int), t, 64);
-    prefetch_l1(Bs.sh_pack, Bs.nshells * sizeof(int4), t, 64);
-    prefetch_l1(Bs.sh_rad2_df, Bs.nshells * sizeof(float2), t, 64);
-    prefetch_l1(Bs.p_pack, Bs.nprim * sizeof(float4), t, 64);
-    prefetch_l1(Bs.atom_df, Bs.natoms * 3 * sizeof(float2), t, 64);
+    const DevBasis& PB = kMulti ? jobs[0].B : Bs;
+    prefetch_l1(PB.f_pack, PB.nbf * sizeof(int), t, 64);
+    prefetch_l1(PB.sh_pack, PB.nshells * sizeof(int4), t, 64);
+    prefetch_l1(PB.sh_rad2_df, PB.nshells * sizeof(float2), t, 64);
+    prefetch_l1(PB.p_pack, PB.nprim * sizeof(float4), t, 64);
+    prefetch_l1(PB.atom_df, PB.natoms * 3 * sizeof(float2), t, 64);
   }
   tc_fence_before();
   __syncthreads();
@@ -567,15 +705,15 @@ namespace {
 // the register check (the register split assumes the launch allocation;
 // with fewer registers per thread the epilogue's setmaxnreg.inc could never
 // be granted).  Stores the device's SM count.
-template <bool kDiv>
+template <bool kDiv, bool kMulti>
 cudaError_t tc_kernel_setup(int* nsm) {
   static PerDevice pd;
   return once_per_device(pd, nsm, [](int dev, int* sms) {
-    cudaError_t e =
-        cudaFuncSetAttribute(tc_fused_kernel<kDiv>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    cudaError_t e = cudaFuncSetAttribute(tc_fused_kernel<kDiv, kMulti>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kSmemBytes);
     if (e != cudaSuccess) return e;
     cudaFuncAttributes fa;
-    e = cudaFuncGetAttributes(&fa, tc_fused_kernel<kDiv>);
+    e = cudaFuncGetAttributes(&fa, tc_fused_kernel<kDiv, kMulti>);
     if (e != cudaSuccess) return e;
     if (fa.numRegs < kRegsLaunch) return cudaErrorInvalidConfiguration;
     return cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
@@ -587,19 +725,39 @@ cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st)
   if (a.npts <= 0) return cudaSuccess;
   const bool div = a.out.divt || a.out.divt32;
   int nsm = 0;
-  cudaError_t e = div ? tc_kernel_setup<true>(&nsm) : tc_kernel_setup<false>(&nsm);
+  cudaError_t e = div ? tc_kernel_setup<true, false>(&nsm) : tc_kernel_setup<false, false>(&nsm);
   if (e != cudaSuccess) return e;
   if (nsm <= 0) return cudaErrorInvalidDevice;
   const int64_t ntiles = (a.npts + kBlockM - 1) / kBlockM;
   const int csplit = std::max(1, a.csplit);
   if (csplit > 1 && (!a.part || !a.tile_done)) return cudaErrorInvalidValue;
   const unsigned grid = static_cast<unsigned>(std::min<int64_t>(ntiles * csplit, nsm));
-  auto kernel = div ? tc_fused_kernel<true> : tc_fused_kernel<false>;
+  auto kernel = div ? tc_fused_kernel<true, false> : tc_fused_kernel<false, false>;
   kernel<<<grid, kThreads, kSmemBytes, st>>>(
       *static_cast<const CUtensorMap*>(a.tmap_a_hi), *static_cast<const CUtensorMap*>(a.tmap_a_lo),
       *static_cast<const CUtensorMap*>(a.tmap_b_hi), *static_cast<const CUtensorMap*>(a.tmap_b_lo), B,
       a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err, a.tiles, a.tile_stride, a.perm,
-      a.tile_order, a.tile_counter, csplit, a.part, a.tile_done);
+      a.tile_order, a.tile_counter, csplit, a.part, a.tile_done, nullptr, 0, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_fused_multi(const TcJob* jobs, int njobs, int64_t nsteps, Flags flags, bool div, int* err,
+                                  int* tile_counter, cudaStream_t st) {
+  if (njobs <= 0 || nsteps <= 0) return cudaSuccess;
+  if (!jobs || !err || !tile_counter) return cudaErrorInvalidValue;
+  int nsm = 0;
+  cudaError_t e = div ? tc_kernel_setup<true, true>(&nsm) : tc_kernel_setup<false, true>(&nsm);
+  if (e != cudaSuccess) return e;
+  if (nsm <= 0) return cudaErrorInvalidDevice;
+  const unsigned grid = static_cast<unsigned>(std::min<int64_t>(nsteps, nsm));
+  CUtensorMap none;
+  std::memset(&none, 0, sizeof(none));
+  const DevBasis nob{};
+  const Outputs noout{nullptr, nullptr, nullptr};
+  auto kernel = div ? tc_fused_kernel<true, true> : tc_fused_kernel<false, true>;
+  kernel<<<grid, kThreads, kSmemBytes, st>>>(none, none, none, none, nob, nullptr, nullptr, nullptr, 0, flags,
+                                             noout, err, nullptr, 0, nullptr, nullptr, tile_counter, 1, nullptr,
+                                             nullptr, jobs, njobs, nsteps);
   return cudaGetLastError();
 }
 

@@ -188,6 +188,23 @@ int gg_plane_integrals(gg_ctx *ctx, const gg_grid *grids, int nplanes, double *o
 int gg_plane_integrals_enqueue(gg_ctx *ctx, const gg_grid *grids, int nplanes, void *stream);
 int gg_plane_integrals_collect(gg_ctx *ctx, double *out, double *ms);
 
+/* Plane passes of many molecules in one contraction launch: the batched
+ * form of the reference's per-molecule, per-slice job loop
+ * (jobscripts/src/current-profile-header:132-146, each slice a run of
+ * integral.f90:50-186).  Molecule m (context ctxs[m], all distinct, on one
+ * device, split-FP16 precision, the same GIAO/dia/para flags) integrates
+ * nplanes[m] planes grids[m]; the points, ordering, tile screening and basis
+ * evaluation of every molecule's whole pass come first, then one persistent
+ * contraction kernel takes the tiles of all molecules from one queue (job
+ * order: 0 as given, 1 the most expensive molecules, points x nbf^2, first),
+ * then each molecule's reduction.  out receives sum(nplanes) x 7 sums in
+ * molecule order, laid out as gg_plane_integrals; mol_ms (optional, nmol)
+ * the time from the contraction's start to the completion of each
+ * molecule's last tile.  From the second call with the same contexts and
+ * layouts on, the whole batch is replayed as one CUDA graph.  Blocking. */
+int gg_plane_integrals_batch(gg_ctx *const *ctxs, const gg_grid *const *grids, const int *nplanes, int nmol,
+                             int order, double *out, double *mol_ms, void *stream);
+
 /* Composite quadrature (gaussint.f90:267-319); type 0 Gauss-Legendre,
  * 1 Gauss-Lobatto.  Returns GG_EINVAL if npts is not a multiple of order or
  * the Newton iteration fails. */
