@@ -52,9 +52,10 @@ def parse():
     ap.add_argument("--config", default="cube", choices=("cube", "scan", "large", "proposal"),
                     help="cube: the C24H24 128^3 cube (default); scan: batched bond-current profile scans")
     ap.add_argument("--molecules", type=int, default=16, help="molecules of the scan batch")
-    ap.add_argument("--scan-mode", default="queued", choices=("queued", "sequential"),
-                    help="queued: every molecule's pass queued before any is collected; sequential: one blocking "
-                         "call per molecule")
+    ap.add_argument("--scan-mode", default="auto", choices=("auto", "batch", "queued", "sequential"),
+                    help="auto: the measured choice of gimic_gb300.autotune; batch: one persistent contraction "
+                         "launch over all molecules (a CUDA graph per step); queued: every molecule's pass queued "
+                         "before any is collected; sequential: one blocking call per molecule")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 65,536 cube points (a z-slab), two passes")
     ap.add_argument("--data", default=os.environ.get("GIMIC_GB300_DATA",
@@ -253,7 +254,7 @@ def run_scan(args):
     10), all strips of a molecule in one device pass."""
     import torch
 
-    from gimic_gb300 import api, build, scan, shard, synth
+    from gimic_gb300 import api, autotune, build, scan, shard, synth
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -289,18 +290,41 @@ def run_scan(args):
                                          order=10, quadrature="lobatto",
                                          fixcoord=tuple(scan.plane_fixcoord(mol.coords, bond)))
         g.set_magnet(bb)
-        specs.append(planes)
-    for _ in range(max(1, args.warmup)):  # warm-up: device tables, matrices, scratch at full size
-        for g, planes in zip(ctxs, specs):
-            g.plane_integrals(planes)
+        specs.append(api.PlaneSet(planes))  # records built once, reused every step
+    pairs = list(zip(ctxs, specs))
+    tuned = None
+    mode = args.scan_mode
+    choice_arg = None
+    if mode == "auto":
+        choice, tt = autotune.tune_scan(pairs, sync=torch.cuda.synchronize)
+        tuned = {"%s/%s" % c: s_ for c, s_ in tt.items()}
+        mode = choice[0]
+        choice_arg = choice[1]
+    elif mode == "batch":
+        choice_arg = "cost"
+    for _ in range(max(1, args.warmup)):  # warm-up: device tables, matrices, scratch, graph capture
+        if mode in ("batch", "queued") and choice_arg is not None:
+            autotune.run(pairs, (mode, choice_arg))
+        else:
+            for g, planes in pairs:
+                g.plane_integrals(planes)
     times, npl, npt = [], 0, 0
     torch.cuda.synchronize()
     t_all = time.perf_counter()
     for _ in range(args.steps):
-        if args.scan_mode == "queued":
+        if mode == "batch":
+            # one persistent contraction over all molecules (one CUDA graph
+            # launch per step); the per-molecule time is the completion of
+            # its last tile, from the contraction's start
+            _, ms = api.plane_integrals_batch(pairs, order=choice_arg, timings=True)
+            times += [t * 1e-3 for t in ms]
+        elif mode == "queued":
             # all molecules queued on one stream, one wait at the end; the
             # per-molecule time is each pass's own stream time
-            _, ms = api.plane_integrals_multi(list(zip(ctxs, specs)), timings=True)
+            if choice_arg is not None:
+                for g, _ in pairs:
+                    g.set_max_batch(choice_arg)
+            _, ms = api.plane_integrals_multi(pairs, timings=True)
             times += [t * 1e-3 for t in ms]
         else:
             for g, planes in zip(ctxs, specs):
@@ -326,11 +350,14 @@ def run_scan(args):
                        "parallelism": "molecules sharded over %d GPUs" % world if world > 1 else "1 GPU",
                        "planes_per_step": npl // args.steps, "points_per_step": npt // args.steps},
             "points_per_s": npt / wall,
-            "scan_mode": args.scan_mode,
+            "scan_mode": "%s%s" % (mode, "" if choice_arg is None else "/%s" % choice_arg),
+            "autotune_s_per_step": tuned,
             "per_molecule_ms": {"p50": float(np.percentile(times, 50) * 1e3),
                                 "p99": float(np.percentile(times, 99) * 1e3),
-                                "what": ("stream time of each molecule's queued pass" if args.scan_mode == "queued"
-                                         else "host wall time of each blocking call"),
+                                "what": {"batch": "completion of each molecule's last tile, from the start of the one "
+                                                  "contraction launch",
+                                         "queued": "stream time of each molecule's queued pass"}.get(
+                                             mode, "host wall time of each blocking call"),
                                 "ranks": "rank 0's molecules" if world > 1 else "all"}}
     print(json.dumps(line), flush=True)
 

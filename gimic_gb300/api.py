@@ -262,12 +262,35 @@ class Gimic:
     def plane_integrals(self, planes, stream=None):
         """Many planes (origin, basv, axes, radius) in one device pass, e.g. a
         bond-current profile scan; returns one dict per plane."""
-        specs, flat = _grid_records(planes)
+        specs, flat = _records(planes)
         n = len(planes)
         out = np.zeros((n, 7))
         check(self._L.gg_plane_integrals(self._h, specs.ctypes.data_as(C.POINTER(_lib.GridSpec)), n, _dptr(out),
                                          C.c_void_p(stream) if stream else None), self._h)
         return _plane_results(out)
+
+
+class PlaneSet:
+    """Planes whose gg_grid records are built once, for planes integrated
+    again and again (the strips of a profile scan at every step): building
+    the records of a few thousand planes costs tens of milliseconds of host
+    time, which a single launch over many molecules cannot hide.  Accepted
+    wherever a list of planes is."""
+
+    def __init__(self, planes):
+        self.planes = list(planes)
+        self.specs, self._keep = _grid_records(self.planes)
+
+    def __len__(self):
+        return len(self.planes)
+
+
+def _records(planes):
+    """(records, what keeps their axis buffers alive) of a list of planes or
+    a PlaneSet."""
+    if isinstance(planes, PlaneSet):
+        return planes.specs, planes
+    return _grid_records(planes)
 
 
 def _plane_results(out):
@@ -327,8 +350,10 @@ def plane_integrals_multi(jobs, stream=None, timings=False):
     st = C.c_void_p(stream) if stream else None
     queued = []
     try:
+        keep = []
         for g, planes in jobs:
-            specs, flat = _grid_records(planes)
+            specs, flat = _records(planes)
+            keep.append(flat)
             check(g._L.gg_plane_integrals_enqueue(g._h, specs.ctypes.data_as(C.POINTER(_lib.GridSpec)), len(planes),
                                                   st), g._h)
             queued.append((g, len(planes)))
@@ -360,7 +385,7 @@ def plane_integrals_batch(jobs, stream=None, order="cost", timings=False):
     if n == 0:
         return ([], []) if timings else []
     L = jobs[0][0]._L
-    recs = [_grid_records(planes) for _, planes in jobs]  # keep the axis buffers referenced
+    recs = [_records(planes) for _, planes in jobs]  # keep the axis buffers referenced
     counts = (C.c_int * n)(*[len(planes) for _, planes in jobs])
     hs = (C.c_void_p * n)(*[g._h.value for g, _ in jobs])
     gp = (C.POINTER(_lib.GridSpec) * n)(*[specs.ctypes.data_as(C.POINTER(_lib.GridSpec)) for specs, _ in recs])

@@ -69,3 +69,32 @@ def test_batch_rejects_bad_batches(synth_dir, c6h6, c6h6_uhf):
     g1.set_precision("split16")
     # still usable afterwards, and a one-molecule batch is a plain pass
     assert api.plane_integrals_batch([(g1, p1)])[0] == api.plane_integrals_batch([(g1, p1)])[0]
+
+
+def test_autotuner_picks_a_candidate_that_gives_the_same_sums(synth_dir, c6h6, c6h6_uhf):
+    """gimic_gb300.autotune times every launch layout on the batch and keeps
+    the fastest per nbf class; every layout gives the same plane sums."""
+    torch = pytest.importorskip("torch")
+    from gimic_gb300 import autotune
+    pairs = [(g, planes) for g, planes, *_ in _jobs(synth_dir, c6h6, c6h6_uhf)]
+    best, times = autotune.tune_scan(pairs, reps=1, sync=torch.cuda.synchronize)
+    assert best in autotune.CANDIDATES and set(times) == set(autotune.CANDIDATES)
+    assert all(t > 0 for t in times.values())
+    assert autotune.choice_for(pairs) == best
+    ref = autotune.run(pairs, ("batch", "cost"))
+    for cand in autotune.CANDIDATES:
+        got = autotune.run(pairs, cand)
+        for a, b in zip(got, ref):
+            for ra, rb in zip(a, b):
+                x, y = np.array(ra["current"]), np.array(rb["current"])
+                assert np.all(np.abs(x - y) <= 1e-7 * np.abs(y).max() + 1e-12), cand
+
+
+def test_plane_sets_give_the_same_sums(synth_dir, c6h6, c6h6_uhf):
+    """Records built once (api.PlaneSet) and plain plane lists give the same
+    sums through the single, queued and batched entry points."""
+    pairs = [(g, planes) for g, planes, *_ in _jobs(synth_dir, c6h6, c6h6_uhf)]
+    sets = [(g, api.PlaneSet(planes)) for g, planes in pairs]
+    assert [g.plane_integrals(p) for g, p in pairs] == [g.plane_integrals(p) for g, p in sets]
+    assert api.plane_integrals_multi(pairs) == api.plane_integrals_multi(sets)
+    assert api.plane_integrals_batch(pairs) == api.plane_integrals_batch(sets)
