@@ -56,8 +56,11 @@ def parse():
                     help="auto: the measured choice of gimic_gb300.autotune; batch: one persistent contraction "
                          "launch over all molecules (a CUDA graph per step); queued: every molecule's pass queued "
                          "before any is collected; sequential: one blocking call per molecule")
-    ap.add_argument("--profile-case", action="store_true",
-                    help="small case for ncu: 65,536 cube points (a z-slab), two passes")
+    ap.add_argument("--profile-case", nargs="?", const="cube", default=None,
+                    choices=("cube", "plane", "mlp", "fp64"),
+                    help="small cases for ncu: cube (65,536 C24H24 cube points, two passes), plane (30 C6H6 "
+                         "60x60 bond-plane passes), mlp (proposal features, one training epoch, inference on "
+                         "262,144 samples), fp64 (the plain FP64 path on 16,384 C24H24 points, twice)")
     ap.add_argument("--data", default=os.environ.get("GIMIC_GB300_DATA",
                                                      os.path.join(tempfile.gettempdir(), "gimic_gb300_data")))
     return ap.parse_args()
@@ -529,13 +532,52 @@ def run_proposal(args):
 
 
 def run_profile_case(args):
-    """65,536 cube points (every 32nd, so that they span the cube) through the
-    split path twice; the second pass is the one to capture."""
+    """Small cases for ncu captures (a few MB to a few hundred MB on the
+    device).  cube: 65,536 cube points (every 32nd, so that they span the
+    cube) through the split path twice; the second pass is the one to
+    capture."""
     import torch
 
     from gimic_gb300 import api, build, synth
 
     build.build()
+    if args.profile_case == "plane":
+        from gimic_gb300 import grid as ggrid
+        from gimic_gb300 import inp as ginp
+
+        mp, xp, mol = synth.make_workload("c6h6", args.data, seed=2024)
+        g = api.Gimic(mp, xp, screening=1e-8)
+        i = ginp.read(synth.ring_bond_plane_input(mol), is_text=True)
+        grd = ggrid.new_grid(i, mol.coords)
+        bb, _ = ggrid.get_magnet(grd, i)
+        g.set_magnet(bb)
+        for _ in range(30):
+            r = g.plane_integral(grd.origin, grd.basv, grd.axes(), grd.radius)
+        print("profile case: 30 passes of the C6H6 60x60 bond plane, current %.6f nA/T" % api.au2si(r["current"][0]))
+        return
+    if args.profile_case == "mlp":
+        from gimic_gb300 import proposal as Pr
+
+        mp, xp, mol = synth.make_workload("c24h24", args.data, seed=2024)
+        g = api.Gimic(mp, xp, screening=1e-8)
+        reg, bb = Pr.Region.bond_plane(mol.coords, (1, 2))
+        g.set_magnet(bb)
+        f, t = Pr.sample_plane(g, reg, 262144, np.random.default_rng(0))
+        net = Pr.ProposalNet(seed=1)
+        net.fit(f, t, epochs=1, batch=65536)
+        y = net.infer(f)
+        torch.cuda.synchronize()
+        print("profile case: proposal network on 262,144 samples, mean prediction %.4f" % float(y.mean()))
+        return
+    if args.profile_case == "fp64":
+        mp, xp, mol = synth.make_workload("c24h24", args.data, seed=2024)
+        g = api.Gimic(mp, xp, screening=1e-8, precision="fp64")
+        P = torch.as_tensor(np.random.default_rng(0).uniform(-16, 16, (16384, 3)), device="cuda")
+        for _ in range(2):
+            jt = g.jtensor_batch(P, rho=True, divj=True)[0]
+        torch.cuda.synchronize()
+        print("profile case: FP64 path on 16,384 C24H24 points, max |t| %.4e" % float(jt.abs().max()))
+        return
     mp, xp, mol = synth.make_workload("c24h24", args.data, seed=2024)
     g = api.Gimic(mp, xp, screening=1e-8, precision="split16")
     if args.batch:
