@@ -127,11 +127,13 @@ def peaks():
         return None
 
 
-def traffic_per_point():
-    """DRAM bytes per point of the tensor-core kernel from the committed ncu
-    summary (profiles/tc_fused_traffic.json), or None."""
+def traffic_model():
+    """(fixed bytes, bytes per point) of the tensor-core kernel's DRAM traffic
+    from the committed ncu summary of the 65,536-point profile case
+    (profiles/tc_fused_traffic.json), or None."""
     try:
-        return json.load(open(os.path.join(ROOT, "profiles", "tc_fused_traffic.json")))["dram_bytes_per_point"]
+        t = json.load(open(os.path.join(ROOT, "profiles", "tc_fused_traffic.json")))
+        return t["fixed_matrix_operand_MB"] * 1e6, t["dram_bytes_per_point"]
     except Exception:
         return None
 
@@ -687,7 +689,7 @@ def main():
         peak_tf, peak_src = pk["bf16_tflops_sustained"] / 3.0, "measured sustained bf16/3 (fp16 same rate, 3 products)"
     else:
         peak_tf, peak_src = 1700.0 / 3.0, "fallback sustained 1.7 PF/3"
-    tpp = traffic_per_point()
+    tmodel = traffic_model()
 
     # ---- end-to-end through the C ABI with pinned host buffers ------------
     hp = torch.empty((npts, 3), dtype=torch.float64, pin_memory=True)
@@ -814,7 +816,9 @@ def main():
                      "frac": exec_tflops / peak_tf, "peak_source": peak_src,
                      "accounting": "flops of the GEMM blocks issued after tile screening (one product of the "
                                    "three-term split) / tc_fused_kernel time",
-                     "traffic": (tpp * per_launch_pts) if tpp else None,
+                     "traffic": (tmodel[0] + tmodel[1] * per_launch_pts) if tmodel else None,
+                     "traffic_source": "ncu dram bytes of the 65,536-point profile case scaled to the launch: "
+                                       "fixed matrix operand + bytes per point x points",
                      "kernel": "tc_fused_kernel", "launch_ms": tc_avg, "points_per_launch": per_launch_pts,
                      "gemm_blocks_issued_fraction": issued / dense if dense else None,
                      "dense_equivalent_tflops": dense_tflops,
