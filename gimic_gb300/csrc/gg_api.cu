@@ -382,11 +382,18 @@ struct gg_ctx {
         p_cc.push_back(static_cast<float>(s.ncc[i]));
       }
     }
-    // per-shell records of the shell-blocked kernels
+    // per-shell records of the shell-blocked kernels; bit 24 marks a shell
+    // whose components are in the order of cart_case_id (then the
+    // contraction's epilogue evaluates them with compile-time forms)
     for (size_t si = 0; si < b.shells.size(); ++si) {
       const gg::Shell& sh = b.shells[si];
+      bool std_order = sh.l <= 3;
+      for (int c = 0; std_order && c < sh_ncomp[si]; ++c)
+        std_order = gg::cart_case_id(f_ijk[sh_f0[si] + c]) == gg::kCartBase[sh.l] + c;
       sh_pack.push_back(make_int4(sh.atom, sh_f0[si],
-                                  sh_ncomp[si] | (static_cast<int>(sh.xp.size()) << 8) | (sh.l << 16), sh_prim[si]));
+                                  sh_ncomp[si] | (static_cast<int>(sh.xp.size()) << 8) | (sh.l << 16) |
+                                      (std_order ? 1 << 24 : 0),
+                                  sh_prim[si]));
     }
     // per-atom envelope of the row-scale bound over bins of log2 d^2 (the
     // shell bound l log2 d + max_p (log2 |c_p| + log2 npf - a_p log2(e) d^2)

@@ -205,4 +205,82 @@ __device__ __forceinline__ void cart_case(int id, const CartPow& p, float f1, fl
   if (lap) *lap = fmaf(sec, f1, X * fmaf(4.f * (x2 + y2 + z2), f3, -lsum * f2));
 }
 
+// Straight-line forms for a component known at compile time, in the order
+// of cart_case_id (kCartStdCode[id] = i * 100 + j * 10 + k): used when a
+// shell's functions are stored in that order (the component is then a
+// compile-time function of its position in the shell).  Terms whose
+// coefficient is zero are left out at compile time instead of multiplied.
+constexpr int kCartStdCode[20] = {0, 100, 10, 1, 200, 110, 101, 20, 11, 2, 300, 210, 201, 120, 111, 102, 30, 21, 12, 3};
+constexpr int kCartBase[4] = {0, 1, 4, 10};  // case id of a shell's first component, by l
+
+template <int E>
+__device__ __forceinline__ float cart_pw(float v, float v2) {
+  static_assert(E >= 1 && E <= 3, "power");
+  if constexpr (E == 1) return v;
+  else if constexpr (E == 2) return v2;
+  else return v2 * v;
+}
+
+// K x^A y^B z^C f
+template <int K, int A, int B, int C>
+__device__ __forceinline__ float cart_term(const CartPow& p, float f) {
+  float m = f;
+  if constexpr (A > 0) m = cart_pw<A>(p.x, p.x2) * m;
+  if constexpr (B > 0) m = cart_pw<B>(p.y, p.y2) * m;
+  if constexpr (C > 0) m = cart_pw<C>(p.z, p.z2) * m;
+  if constexpr (K != 1) m = static_cast<float>(K) * m;
+  return m;
+}
+
+// x^A y^B z^C (A + B + C > 0)
+template <int A, int B, int C>
+__device__ __forceinline__ float cart_mono(const CartPow& p) {
+  static_assert(A + B + C > 0, "constant monomial");
+  if constexpr (A > 0) {
+    float m = cart_pw<A>(p.x, p.x2);
+    if constexpr (B > 0) m = m * cart_pw<B>(p.y, p.y2);
+    if constexpr (C > 0) m = m * cart_pw<C>(p.z, p.z2);
+    return m;
+  } else if constexpr (B > 0) {
+    float m = cart_pw<B>(p.y, p.y2);
+    if constexpr (C > 0) m = m * cart_pw<C>(p.z, p.z2);
+    return m;
+  } else {
+    return cart_pw<C>(p.z, p.z2);
+  }
+}
+
+// phi, grad phi and (kLap) the Laplacian of case ID from the shell's radial
+// sums: f1, m2f2 = -2 f2 and lq = 4 r^2 f3 - 2 (2l + 3) f2 (the Laplacian's
+// coefficient of the monomial).  Same quantities as cart_case.
+template <int ID, bool kLap>
+__device__ __forceinline__ void cart_std(const CartPow& p, float f1, float m2f2, float lq, float* phi, float* gx,
+                                         float* gy, float* gz, float* lap) {
+  constexpr int code = kCartStdCode[ID], A = code / 100, B = (code / 10) % 10, C = code % 10;
+  float tX, xl;  // -2 f2 X and the Laplacian's X term
+  if constexpr (A + B + C == 0) {
+    *phi = f1;
+    tX = m2f2;
+    xl = lq;
+  } else {
+    const float X = cart_mono<A, B, C>(p);
+    *phi = X * f1;
+    tX = X * m2f2;
+    xl = X * lq;
+  }
+  if constexpr (A > 0) *gx = fmaf(p.x, tX, cart_term<A, A - 1, B, C>(p, f1));
+  else *gx = p.x * tX;
+  if constexpr (B > 0) *gy = fmaf(p.y, tX, cart_term<B, A, B - 1, C>(p, f1));
+  else *gy = p.y * tX;
+  if constexpr (C > 0) *gz = fmaf(p.z, tX, cart_term<C, A, B, C - 1>(p, f1));
+  else *gz = p.z * tX;
+  if constexpr (kLap) {
+    // l <= 3: at most one exponent reaches 2, so the second derivatives are one term
+    if constexpr (A >= 2) *lap = cart_term<A * (A - 1), A - 2, B, C>(p, f1) + xl;
+    else if constexpr (B >= 2) *lap = cart_term<B * (B - 1), A, B - 2, C>(p, f1) + xl;
+    else if constexpr (C >= 2) *lap = cart_term<C * (C - 1), A, B, C - 2>(p, f1) + xl;
+    else *lap = xl;
+  }
+}
+
 }  // namespace gg

@@ -34,7 +34,7 @@ struct DevBasis {
   const float* p_cc;       // normalised contraction coefficients (fp32)
   const float4* p_pack;    // {p_xp, p_xplo, p_cc, 0} per primitive
   int nprim;
-  const int4* sh_pack;     // {atom, first function, ncomp | npf << 8 | l << 16, first primitive}
+  const int4* sh_pack;     // {atom, first function, ncomp | npf << 8 | l << 16 | standard order << 24, first primitive}
   const double* p_xpd;     // same in fp64
   const double* p_ccd;
   // Row-scale envelope: atom_env[a * env_bins + b] bounds log2 |phi| over all

@@ -14,22 +14,24 @@
 // operand pair per stage).  The two TMEM accumulators alternate between
 // chunks so that the epilogue of chunk c overlaps the MMAs of chunk c+1.
 //
-// Roles (384 threads, three warpgroups):
+// Roles (512 threads, four warpgroups):
 //   warp 0      TMA producer (A: phi pieces of the tile, B: matrix pieces)
 //   warp 1      TMEM owner and MMA issuer
 //   warps 2, 3  none (they complete the first warpgroup, which hands its
 //               registers to the epilogue)
-//   warps 4..11 epilogue, two warps per TMEM lane quarter, each taking half
-//               of a chunk's functions: for its point (one TMEM lane) it
-//               re-evaluates phi, grad phi and the Laplacian of the chunk's 32
+//   warps 4..15 epilogue, three warps per TMEM lane quarter, each taking a
+//               third of a chunk's functions: for its point (one TMEM lane)
+//               it re-evaluates phi, grad phi and the Laplacian of those
 //               functions in fp32 (src/libgimic/caos.f90:17-110 semantics)
-//               and accumulates the kNDots bilinear forms; fp32 within a
-//               chunk, double-float across chunks and in the final
-//               combination (gg_combine.cuh, src/libgimic/jtensor.F90:148-237).
+//               and accumulates the kNDots bilinear forms in fp32 over the
+//               tile; the three groups' sums are added as double-floats, and
+//               the final combination runs in double-float
+//               (gg_combine.cuh, src/libgimic/jtensor.F90:148-237).
 #include <cuda.h>
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 #include "gg_cart.cuh"
 #include "gg_combine.cuh"
@@ -46,26 +48,41 @@ constexpr int kStages = 4;
 constexpr int kTileA = kBlockM * kBlockK * 2;          // 16 KiB
 constexpr int kTileB = kBlockN * kBlockK * 2;          // 28 KiB
 constexpr int kStageBytes = kTileA + kTileB;           // 44 KiB
-constexpr int kEpiWarps = 8;                           // 2 per TMEM lane quarter
+// Epilogue warps per TMEM lane quarter: each takes one group of a chunk's
+// functions (11, 11 and 10 of the 32).  The epilogue is bound by the latency
+// of its per-function chains (shell changes, the primitive sums, the
+// polynomial), so three warps per quarter issue more of it than two.
+constexpr int kEpiGroups = 3;
+constexpr int kGroupF = (kChunkF + kEpiGroups - 1) / kEpiGroups;
+constexpr int kEpiWarps = 4 * kEpiGroups;
 constexpr int kCtlWarps = 4;                           // TMA producer, MMA issuer, two idle: one warpgroup
 constexpr int kThreads = 32 * (kCtlWarps + kEpiWarps);
 // Register split (setmaxnreg, per warpgroup): the control warpgroup gives
 // registers up so that the epilogue warpgroups can hold their accumulators,
-// the geometry and the TMEM values of two functions without spilling.  The
-// shares add up to the launch allocation of 168 per thread (65,536 / 384,
-// rounded down to a multiple of 8), which the launcher checks.
-constexpr int kRegsLaunch = 168;
+// the geometry and the TMEM values of a function without spilling.  The
+// shares add up to at most the launch allocation of 128 per thread
+// (65,536 / 512), which the launcher checks.
+constexpr int kRegsLaunch = 128;
 constexpr int kRegsCtl = 56;
-constexpr int kRegsEpi = 224;
+constexpr int kRegsEpi = 152;
 static_assert(kCtlWarps * kRegsCtl + kEpiWarps * kRegsEpi <= (kCtlWarps + kEpiWarps) * kRegsLaunch,
               "register split exceeds the launch allocation");
 constexpr uint32_t kTmemCols = 512;
 constexpr int kAccStride = 256;
-constexpr int kRedBytes = kBlockM * kNDots * 8;        // half-sums exchanged between the two epilogue halves
+constexpr int kRedBytes = (kEpiGroups - 1) * kBlockM * kNDots * 4;  // group sums handed to group 0 (fp32)
 constexpr int kRing = 4;  // tile steps in flight between the producer and the other roles
-constexpr int kSmemBytes = kStages * kStageBytes + kRedBytes + 1024 + 256;
+constexpr int kSmemBytes = kStages * kStageBytes + kRedBytes + 1024 + 512;  // + alignment, barriers and ring
 
 __device__ __forceinline__ void reg_dealloc_ctl() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kRegsCtl)); }
+
+// f(integral_constant<int, I>) for I = I0 .. N-1, unrolled at compile time
+template <int I0, int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  if constexpr (I0 < N) {
+    f(std::integral_constant<int, I0>{});
+    static_for<I0 + 1, N>(f);
+  }
+}
 
 __device__ __forceinline__ void tmem_ld1(uint32_t taddr, float& v) {
   uint32_t r;
@@ -82,9 +99,6 @@ __device__ __forceinline__ void tmem_wait7(float* v) {
                : "memory");
 }
 
-// compensated fp32 sum (Kahan): hi + lo tracks the running total; lo holds
-// what the last addition lost.  The chunk's partial sum y starts from lo
-// (instead of zero), which feeds the loss into the next addition.
 // the matrix of each of the kNDots sums: 0..12 D (rho, X, E), 13..24 C_d
 // (Y_dm at 13 + 3d + m, Laplacian terms at 22 + d), 25..36 P_d (Z_dm at
 // 25 + 3d + m, Laplacian terms at 34 + d)
@@ -94,9 +108,6 @@ __host__ __device__ constexpr int dot_matrix(int i) {
 static_assert(dot_matrix(12) == 0 && dot_matrix(13) == 1 && dot_matrix(21) == 3 && dot_matrix(24) == 3 &&
                   dot_matrix(25) == 4 && dot_matrix(33) == 6 && dot_matrix(36) == 6 && kNDots == 37,
               "sum layout");
-
-// the Laplacian sums, used only by div j
-__host__ __device__ constexpr bool is_div_sum(int i) { return (i >= 22 && i < 25) || i >= 34; }
 
 // What a step needs of its job (one pass over one molecule's points): the
 // operands' tensor maps and the tile lists for the producer and the MMA
@@ -126,12 +137,6 @@ struct EpiView {
   int* left;
   unsigned long long* done_ns;
 };
-
-__device__ __forceinline__ void kahan_add(float& hi, float& lo, float y) {
-  const float t = hi + y;
-  lo = y - (t - hi);
-  hi = t;
-}
 }  // namespace
 
 int tc_smem_bytes() { return kSmemBytes; }
@@ -170,9 +175,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* empty = full + kStages;
   uint64_t* accfull = empty + kStages;
   uint64_t* accempty = accfull + 2;
-  uint64_t* xfull = accempty + 2;   // half-1 sums of a tile are in `red`
-  uint64_t* xempty = xfull + 1;     // half-0 has read them
-  uint64_t* ring_full = xempty + 1;          // tile steps handed from the producer to the other roles
+  uint64_t* xfull = accempty + 2;   // [4] per lane quarter: groups 1.. have put a tile's sums in `red`
+  uint64_t* xempty = xfull + 4;     // [4] group 0 has read them
+  uint64_t* ring_full = xempty + 4;          // tile steps handed from the producer to the other roles
   uint64_t* ring_empty = ring_full + kRing;
   uint64_t* drain = ring_empty + kRing;      // the MMA issuer's last MMAs, after an error
   int* ring = reinterpret_cast<int*>(drain + 1);
@@ -304,8 +309,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&accfull[b], 1);
       mbar_init(&accempty[b], kEpiWarps);
     }
-    mbar_init(xfull, kEpiWarps / 2);
-    mbar_init(xempty, kEpiWarps / 2);
+    for (int k = 0; k < 4; ++k) {
+      mbar_init(&xfull[k], kEpiGroups - 1);
+      mbar_init(&xempty[k], 1);
+    }
     for (int k = 0; k < kRing; ++k) {
       mbar_init(&ring_full[k], 1);
       mbar_init(&ring_empty[k], 1 + kEpiWarps);
@@ -426,11 +433,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp >= kCtlWarps) {
     asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kRegsEpi));
-    // ---------------- epilogue: 8 warps ----------------
+    // ---------------- epilogue: kEpiWarps warps ----------------
     // warp w reads TMEM lanes 32*(w%4) .. +31 (its 32 points) and handles
-    // half (w-4)/4 of the 32 functions of every chunk.
+    // function group (w-4)/4 (kGroupF functions) of every chunk.
     const int q = warp & 3;
-    const int half = (warp - kCtlWarps) >> 2;
+    const int grp = (warp - kCtlWarps) >> 2;
     const int row = q * 32 + lane;
     const uint32_t lane_base = tmem_base + (static_cast<uint32_t>(q * 32) << 16);
     int acc = 0, tk = 0;
@@ -454,9 +461,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         r[2] = ev.pts[3 * p + 2];
       }
       const DFloat rdf[3] = {df_split(r[0]), df_split(r[1]), df_split(r[2])};
-      float thi[kNDots], tlo[kNDots];
+      // fp32 running sums over the tile's functions in this group (a
+      // compensated sum across chunks changed no digit of the error against
+      // the FP64 oracle: it is set by the fp16 products)
+      float sum[kNDots];
 #pragma unroll
-      for (int i = 0; i < kNDots; ++i) thi[i] = tlo[i] = 0.f;
+      for (int i = 0; i < kNDots; ++i) sum[i] = 0.f;
       int cur_shell = -1, cur_atom = -1;
       // the next shell's record and its screening radius, loaded when a
       // shell starts (shells are contiguous in function order), so that a
@@ -464,10 +474,55 @@ __global__ void __launch_bounds__(kThreads, 1)
       int sh_pre = -1;
       int4 pk_pre = make_int4(0, 0, 0, 0);
       float2 rad_pre = make_float2(0.f, 0.f);
-      float sx = 0.f, sy = 0.f, sz = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
+      // the current shell (first function, components, l, whether they are
+      // in the standard order) and its radial sums
+      int sh_first = 0, sh_ncomp = 0, sh_l = 0;
+      bool sh_std = false, warp_on = false;
+      float f1 = 0.f, f2 = 0.f, f3 = 0.f, m2f2 = 0.f, lq = 0.f;
+      // the current atom: r - R_A (the high parts) and its squared length
+      float sx = 0.f, sy = 0.f, sz = 0.f, r2x4 = 0.f;
       CartPow cp = cart_pow(0.f, 0.f, 0.f);
       DFloat d2a{0.f, 0.f};
-      bool on = false, warp_on = false;
+      // D's terms summed over the current atom's functions: w0 phi and w0
+      // grad phi.  The X and E sums carry r - R_A, which is constant per
+      // atom, so they take these sums times r - R_A when the atom changes
+      // (and at the end of the tile) instead of a product per function.
+      float aP = 0.f, aGx = 0.f, aGy = 0.f, aGz = 0.f;
+      auto fold_atom = [&]() {
+        sum[0] += aP;
+        sum[1] = fmaf(sx, aP, sum[1]);
+        sum[2] = fmaf(sy, aP, sum[2]);
+        sum[3] = fmaf(sz, aP, sum[3]);
+        sum[4 + 1] = fmaf(sy, aGx, sum[4 + 1]);  // E[x][y] = sum w0 s_y d/dx phi
+        sum[4 + 2] = fmaf(sz, aGx, sum[4 + 2]);  // E[x][z]
+        sum[4 + 3] = fmaf(sx, aGy, sum[4 + 3]);  // E[y][x]
+        sum[4 + 5] = fmaf(sz, aGy, sum[4 + 5]);  // E[y][z]
+        sum[4 + 6] = fmaf(sx, aGz, sum[4 + 6]);  // E[z][x]
+        sum[4 + 7] = fmaf(sy, aGz, sum[4 + 7]);  // E[z][y]
+        aP = aGx = aGy = aGz = 0.f;
+      };
+      // one function's terms from its seven TMEM values; the sums stay in
+      // the matrices' scaled units until the combination
+      auto add_function = [&](const float* v, float ph, float gx, float gy, float gz, float lp) {
+        const float w0 = v[0];
+        aP = fmaf(w0, ph, aP);
+        aGx = fmaf(w0, gx, aGx);
+        aGy = fmaf(w0, gy, aGy);
+        aGz = fmaf(w0, gz, aGz);
+        const float g[3] = {gx, gy, gz};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            sum[13 + 3 * d + m] = fmaf(v[1 + d], g[m], sum[13 + 3 * d + m]);
+            sum[25 + 3 * d + m] = fmaf(v[4 + d], g[m], sum[25 + 3 * d + m]);
+          }
+          if (kDiv) {
+            sum[22 + d] = fmaf(v[1 + d], lp, sum[22 + d]);
+            sum[34 + d] = fmaf(v[4 + d], lp, sum[34 + d]);
+          }
+        }
+      };
       const int nkb = n_kb(v, tile), nchunk = n_chunk(v, tile, nkb);
       int c0, c1;
       chunk_span(t, nchunk, &c0, &c1);
@@ -479,32 +534,47 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         tc_fence_after();
-        float part[kNDots];
-#pragma unroll
-        for (int i = 0; i < kNDots; ++i) part[i] = tlo[i];
         const int f0 = c * kChunkF;
-        const int mb = f0 + half * (kChunkF / 2);
-        const int me = min(mb + kChunkF / 2, ev.nbf);
+        const int mb = f0 + grp * kGroupF;
+        const int me = min(f0 + min((grp + 1) * kGroupF, kChunkF), ev.nbf);
         const uint32_t tcol = lane_base + b * kAccStride;
-        int fp_next = mb < me ? ev.fpack[mb] : 0;
+        // a function of the current shell at column u: its TMEM loads, then
+        // (while they are in flight) its value, gradient and Laplacian (all
+        // zero on lanes whose shell is screened: f1 = f2 = f3 = 0 there)
+        auto std_function = [&](auto idc, int u) {
+          constexpr int kId = decltype(idc)::value;
+          float w[kMats];
+#pragma unroll
+          for (int m = 0; m < kMats; ++m) tmem_ld1(tcol + m * kChunkF + u, w[m]);
+          float ph, gx, gy, gz, lp = 0.f;
+          cart_std<kId, kDiv>(cp, f1, m2f2, lq, &ph, &gx, &gy, &gz, &lp);
+          tmem_wait7(w);
+          add_function(w, ph, gx, gy, gz, lp);
+        };
+        int mu = mb;
 #pragma unroll 1
-        for (int mu = mb; mu < me; ++mu) {
-          const int u = mu - f0;
-          const int fp = fp_next;
-          if (mu + 1 < me) fp_next = ev.fpack[mu + 1];
-          const int sh = fp >> 12;
+        while (mu < me) {
+          // shells are contiguous in function order: after the range's first
+          // shell comes the next one
+          const int sh = mu == mb ? (ev.fpack[mb] >> 12) : cur_shell + 1;
           if (sh != cur_shell) {
             cur_shell = sh;
             const bool hit = sh == sh_pre;
-            const int4 pk = hit ? pk_pre : ev.shp[sh];  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
+            // atom, first function, ncomp | npf << 8 | l << 16 | standard order << 24, first primitive
+            const int4 pk = hit ? pk_pre : ev.shp[sh];
             const float2 rad = hit ? rad_pre : ev.shr[sh];
             if (sh + 1 < ev.nshells) {
               sh_pre = sh + 1;
               pk_pre = ev.shp[sh + 1];
               rad_pre = ev.shr[sh + 1];
             }
+            sh_first = pk.y;
+            sh_ncomp = pk.z & 0xff;
+            sh_l = (pk.z >> 16) & 0xff;
+            sh_std = ((pk.z >> 24) & 1) != 0;
             const int a = pk.x;
             if (a != cur_atom) {
+              fold_atom();
               cur_atom = a;
               float s3[3];
               d2a = atom_offset_t(rdf, ev.atm, a, s3);
@@ -512,98 +582,103 @@ __global__ void __launch_bounds__(kThreads, 1)
               sy = s3[1];
               sz = s3[2];
               cp = cart_pow(sx, sy, sz);
+              if (kDiv) r2x4 = 4.f * (cp.x2 + cp.y2 + cp.z2);
             }
-            on = df_le(d2a, rad);
+            const bool on = df_le(d2a, rad);
             // a shell screened for all 32 points of the warp contributes
-            // nothing: skip its remaining functions in this range
+            // nothing: its functions in this range are skipped
             warp_on = __any_sync(0xffffffffu, on);
-            if (!warp_on) {
-              const int last = min(me, pk.y + (pk.z & 0xff)) - 1;
-              if (last > mu) {
-                mu = last;
-                fp_next = mu + 1 < me ? ev.fpack[mu + 1] : 0;
+            if (warp_on) {
+              f1 = f2 = f3 = 0.f;
+              if (on) {
+                const int np = (pk.z >> 8) & 0xff;
+                for (int k = 0; k < np; ++k) {
+                  const float4 pr = ev.prm[pk.w + k];  // exponent hi, exponent lo, coefficient
+                  const float al = pr.x;
+                  const float e = pr.z * gauss_df(al, pr.y, d2a.h, d2a.l);
+                  f1 += e;
+                  f2 += al * e;
+                  if (kDiv) f3 += al * al * e;
+                }
               }
-              continue;
+              m2f2 = -2.f * f2;
+              if (kDiv) lq = fmaf(r2x4, f3, -static_cast<float>(2 * (2 * sh_l + 3)) * f2);
             }
-            f1 = f2 = f3 = 0.f;
-            if (on) {
-              const int np = (pk.z >> 8) & 0xff;
-              for (int k = 0; k < np; ++k) {
-                const float4 pr = ev.prm[pk.w + k];  // exponent hi, exponent lo, coefficient
-                const float al = pr.x;
-                const float e = pr.z * gauss_df(al, pr.y, d2a.h, d2a.l);
-                f1 += e;
-                f2 += al * e;
-                if (kDiv) f3 += al * al * e;
+          }
+          const int hi = min(me, sh_first + sh_ncomp);
+          if (warp_on) {
+            if (sh_std) {
+              // components cb .. ce-1 of the shell, component k at column u0 + k
+              const int cb = mu - sh_first, ce = hi - sh_first, u0 = sh_first - f0;
+              auto comps = [&](auto basec, auto ncc) {
+                static_for<0, decltype(ncc)::value>([&](auto kc) {
+                  constexpr int k = decltype(kc)::value;
+                  if (k >= cb && k < ce) std_function(std::integral_constant<int, decltype(basec)::value + k>{}, u0 + k);
+                });
+              };
+              switch (sh_l) {
+                case 0:
+                  comps(std::integral_constant<int, 0>{}, std::integral_constant<int, 1>{});
+                  break;
+                case 1:
+                  comps(std::integral_constant<int, 1>{}, std::integral_constant<int, 3>{});
+                  break;
+                case 2:
+                  comps(std::integral_constant<int, 4>{}, std::integral_constant<int, 6>{});
+                  break;
+                default:
+                  comps(std::integral_constant<int, 10>{}, std::integral_constant<int, 10>{});
+              }
+            } else {
+#pragma unroll 1
+              for (int f = mu; f < hi; ++f) {
+                const int u = f - f0;
+                float w[kMats];
+#pragma unroll
+                for (int m = 0; m < kMats; ++m) tmem_ld1(tcol + m * kChunkF + u, w[m]);
+                float ph, gx, gy, gz, lp = 0.f;
+                cart_case(ev.fpack[f] & 0xfff, cp, f1, f2, f3, &ph, &gx, &gy, &gz, kDiv ? &lp : nullptr);
+                tmem_wait7(w);
+                add_function(w, ph, gx, gy, gz, lp);
               }
             }
           }
-          if (!warp_on) continue;
-          float v[kMats];
-#pragma unroll
-          for (int m = 0; m < kMats; ++m) tmem_ld1(tcol + m * kChunkF + u, v[m]);
-          // while the loads are in flight: the function's value, gradient
-          // and Laplacian (all zero on lanes whose shell is screened, as
-          // f1 = f2 = f3 = 0 there).  The sums stay in the matrices' scaled
-          // units until the combination.
-          float ph, gx, gy, gz, lp = 0.f;
-          cart_case(fp & 0xfff, cp, f1, f2, f3, &ph, &gx, &gy, &gz, kDiv ? &lp : nullptr);
-          tmem_wait7(v);
-          {
-            const float w0 = v[0];
-            const float wc[3] = {v[1], v[2], v[3]};
-            const float qq[3] = {v[4], v[5], v[6]};
-            const float wp = w0 * ph;
-            part[0] = fmaf(w0, ph, part[0]);
-            part[1] = fmaf(wp, sx, part[1]);
-            part[2] = fmaf(wp, sy, part[2]);
-            part[3] = fmaf(wp, sz, part[3]);
-            const float wx = w0 * sx, wy = w0 * sy, wz = w0 * sz;
-            part[4 + 1] = fmaf(wy, gx, part[4 + 1]);  // E[x][y]
-            part[4 + 2] = fmaf(wz, gx, part[4 + 2]);  // E[x][z]
-            part[4 + 3] = fmaf(wx, gy, part[4 + 3]);  // E[y][x]
-            part[4 + 5] = fmaf(wz, gy, part[4 + 5]);  // E[y][z]
-            part[4 + 6] = fmaf(wx, gz, part[4 + 6]);  // E[z][x]
-            part[4 + 7] = fmaf(wy, gz, part[4 + 7]);  // E[z][y]
-            const float g[3] = {gx, gy, gz};
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-#pragma unroll
-              for (int m = 0; m < 3; ++m) {
-                part[13 + 3 * d + m] = fmaf(wc[d], g[m], part[13 + 3 * d + m]);
-                part[25 + 3 * d + m] = fmaf(qq[d], g[m], part[25 + 3 * d + m]);
-              }
-              if (kDiv) {
-                part[22 + d] = fmaf(wc[d], lp, part[22 + d]);
-                part[34 + d] = fmaf(qq[d], lp, part[34 + d]);
-              }
-            }
-          }
+          mu = hi;
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&accempty[b]);
-#pragma unroll
-        for (int i = 0; i < kNDots; ++i)
-          if (i != 4 && i != 8 && i != 12 && (kDiv || !is_div_sum(i))) kahan_add(thi[i], tlo[i], part[i]);
       }
       if (!ok) break;
-      // combine the two halves of every point through `red` (float pairs):
-      // half 1 writes once half 0 has read the previous tile's sums, half 0
-      // reads them
-      float2* redf = reinterpret_cast<float2*>(red);
-      if (half == 1) {
-        if (!mbar_wait(xempty, (tk & 1) ^ 1, err, 5)) break;
+      fold_atom();
+      // combine the groups' sums of every point through `red`: groups 1..
+      // write once group 0 of their lane quarter has read the previous
+      // tile's sums; group 0 adds them in group order as double-floats
+      float* redf = reinterpret_cast<float*>(red);  // [group - 1][sum][row]
+      if (grp > 0) {
+        if (!mbar_wait(&xempty[q], (tk & 1) ^ 1, err, 5)) break;
+        float* dst = redf + (grp - 1) * (kNDots * kBlockM) + row;
 #pragma unroll
-        for (int i = 0; i < kNDots; ++i) redf[row * kNDots + i] = make_float2(thi[i], tlo[i]);
+        for (int i = 0; i < kNDots; ++i) dst[i * kBlockM] = sum[i];
         __syncwarp();
-        if (lane == 0) mbar_arrive(xfull);
+        if (lane == 0) mbar_arrive(&xfull[q]);
       } else {
-        if (!mbar_wait(xfull, tk & 1, err, 6)) break;
-        const float2* h1 = redf + row * kNDots;
+        if (!mbar_wait(&xfull[q], tk & 1, err, 6)) break;
+        float thi[kNDots], tlo[kNDots];
+#pragma unroll
+        for (int i = 0; i < kNDots; ++i) {
+          DFloat a{sum[i], 0.f};
+#pragma unroll
+          for (int g = 1; g < kEpiGroups; ++g)
+            a = df_add(a, DFloat{redf[(g - 1) * (kNDots * kBlockM) + i * kBlockM + row], 0.f});
+          thi[i] = a.h;
+          tlo[i] = a.l;
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&xempty[q]);  // `red` is free for the next tile
         bool finish = true;  // this warp combines and stores its rows now
         if (csplit > 1) {
-          // Chunk split: the step's sums of these 32 rows (both halves) go to
+          // Chunk split: the step's sums of these 32 rows (all groups) go to
           // the tile's partial slot g; the warp that completes this quarter
           // of the tile (the last of the csplit steps to count) adds the
           // slots in chunk order into thi/tlo, so the result does not depend
@@ -613,10 +688,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (g < nchunk) {
             float2* dst = part + (tile * csplit + g) * static_cast<int64_t>(kNDots * kBlockM) + row;
 #pragma unroll
-            for (int i = 0; i < kNDots; ++i) {
-              const DFloat v = df_add(DFloat{thi[i], tlo[i]}, DFloat{h1[i].x, h1[i].y});
-              dst[i * kBlockM] = make_float2(v.h, v.l);
-            }
+            for (int i = 0; i < kNDots; ++i) dst[i * kBlockM] = make_float2(thi[i], tlo[i]);
           }
           __threadfence();
           __syncwarp();
@@ -647,12 +719,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           float msc[kMats];
 #pragma unroll
           for (int m = 0; m < kMats; ++m) msc[m] = sc * ev.icol[m];
-          const bool own = csplit == 1;  // the other half's sums still to add
           auto tot = [&](int i) -> DFloat {
-            const float2 o = own ? h1[i] : make_float2(0.f, 0.f);
-            const DFloat t = own ? df_add(DFloat{thi[i], tlo[i]}, DFloat{o.x, o.y}) : DFloat{thi[i], tlo[i]};
             const float f = msc[dot_matrix(i)];
-            return DFloat{t.h * f, t.l * f};
+            return DFloat{thi[i] * f, tlo[i] * f};
           };
           const int64_t o = ev.perm ? static_cast<int64_t>(ev.perm[p]) : p;  // caller's point order
           if (fl.giao && fl.dia && fl.para) {
@@ -675,8 +744,6 @@ __global__ void __launch_bounds__(kThreads, 1)
           __syncwarp();
           if (lane == 0 && atomicSub(ev.left, 1) == 1) *ev.done_ns = global_ns();
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(xempty);
       }
     }
   } else {
