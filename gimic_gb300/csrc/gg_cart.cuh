@@ -6,8 +6,18 @@
 // (src/libgimic/caos.f90:39-64 for the gradient).  cart_case_id() maps the
 // packed exponents i | j << 4 | k << 8 to the case number.
 #pragma once
+#include <type_traits>
 
 namespace gg {
+
+// f(integral_constant<int, I>) for I = I0 .. N-1, unrolled at compile time
+template <int I0, int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  if constexpr (I0 < N) {
+    f(std::integral_constant<int, I0>{});
+    static_for<I0 + 1, N>(f);
+  }
+}
 
 struct CartPow {
   float x, y, z, x2, y2, z2;

@@ -36,7 +36,9 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <type_traits>
 
+#include "gg_cart.cuh"
 #include "gg_device.cuh"
 #include "gg_kernels.h"
 #include "gg_once.h"
@@ -70,32 +72,133 @@ __device__ __forceinline__ uint32_t swz(int row, int col) {
   return static_cast<uint32_t>(row * 64 + ((((byte >> 4) ^ ((row >> 1) & 3)) << 4) | (byte & 15)));
 }
 
-struct Stager {
-  unsigned char* buf;  // current buffer: hi tile then lo tile
-  int row;
-  __half ph, pl;       // pending even column
-  __device__ __forceinline__ void put_pair(int col, __half h0, __half l0, __half h1, __half l1) {
-    const uint32_t o = swz(row, col);
-    *reinterpret_cast<__half2*>(buf + o) = __halves2half2(h0, h1);
-    *reinterpret_cast<__half2*>(buf + kStageBytes + o) = __halves2half2(l0, l1);
-  }
+// byte offset of column col of the row whose offset is rowoff = row * 64
+// and swizzle bits rxs = ((row >> 1) & 3) << 4 (the same as swz)
+__device__ __forceinline__ uint32_t swz_col(uint32_t rowoff, uint32_t rxs, int col) {
+  return rowoff + ((static_cast<uint32_t>(col) << 1) ^ rxs);
+}
+
+// the current atom of a point's shell walk: r - R_A (fp32 high parts, with
+// squares) and |r - R_A|^2 as a double-float
+struct AtomGeom {
+  int atom = -1;
+  CartPow cp = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  DFloat d2{0.f, 0.f};
 };
+
+// One point's values of the shells that overlap the columns [lo, hi) of a
+// half K block, every kStep-th shell from the first one there plus
+// `first`.  put(col, v) stages value v (or a zero) at column col - lo.
+// The shells in the standard Cartesian order (bit 24 of the shell record)
+// evaluate their components with compile-time monomials; the others select
+// the monomial from the packed exponents.  Both give x^i y^j z^k f1 with the
+// same operations in the same order.
+template <int kStep, typename Put>
+__device__ __forceinline__ void stage_shells(const DevBasis& B, const DFloat r[3], float scale, int lo, int hi,
+                                             int first, AtomGeom& g, Put&& put) {
+  for (int sh = __ldg(B.f_shell + lo) + first; sh < B.nshells; sh += kStep) {
+    const int4 pk = __ldg(B.sh_pack + sh);  // atom, first function, ncomp | npf << 8 | l << 16 | std << 24, first primitive
+    const int mu0 = pk.y, ncomp = pk.z & 0xff, np = (pk.z >> 8) & 0xff;
+    if (mu0 >= hi) break;  // shells are in function order
+    const int c0 = max(0, lo - mu0), c1 = min(ncomp, hi - mu0);
+    if (pk.x != g.atom) {
+      g.atom = pk.x;
+      float s3[3];
+      g.d2 = atom_offset(r, B.atom_df, pk.x, s3);
+      g.cp = cart_pow(s3[0], s3[1], s3[2]);
+    }
+    float f1 = 0.f;
+    const bool in_range = df_le(g.d2, __ldg(B.sh_rad2_df + sh));
+    if (in_range) {
+      for (int k = 0; k < np; ++k) {
+        const float4 pr = __ldg(B.p_pack + pk.w + k);  // exponent hi, exponent lo, coefficient
+        f1 += pr.z * gauss_df(pr.x, pr.y, g.d2.h, g.d2.l);
+      }
+      f1 *= scale;
+    }
+    const int col0 = mu0 - lo;
+    // a shell out of range for the whole warp only writes zeros
+    if (!__any_sync(0xffffffffu, in_range)) {
+      for (int c = c0; c < c1; ++c) put(col0 + c, 0.f, true);
+      continue;
+    }
+    if ((pk.z >> 24) & 1) {
+      const CartPow& cp = g.cp;
+      auto comps = [&](auto basec, auto ncc) {
+        static_for<0, decltype(ncc)::value>([&](auto kc) {
+          constexpr int c = decltype(kc)::value;
+          constexpr int code = kCartStdCode[decltype(basec)::value + c];
+          constexpr int A = code / 100, Bx = (code / 10) % 10, C = code % 10;
+          if (c >= c0 && c < c1) {
+            if constexpr (A + Bx + C == 0) put(col0 + c, f1, false);
+            else put(col0 + c, cart_mono<A, Bx, C>(cp) * f1, false);
+          }
+        });
+      };
+      switch ((pk.z >> 16) & 0xff) {
+        case 0:
+          comps(std::integral_constant<int, 0>{}, std::integral_constant<int, 1>{});
+          break;
+        case 1:
+          comps(std::integral_constant<int, 1>{}, std::integral_constant<int, 3>{});
+          break;
+        case 2:
+          comps(std::integral_constant<int, 4>{}, std::integral_constant<int, 6>{});
+          break;
+        default:
+          comps(std::integral_constant<int, 10>{}, std::integral_constant<int, 10>{});
+      }
+    } else {
+      const float px[4] = {1.f, g.cp.x, g.cp.x2, g.cp.x2 * g.cp.x};
+      const float py[4] = {1.f, g.cp.y, g.cp.y2, g.cp.y2 * g.cp.y};
+      const float pz[4] = {1.f, g.cp.z, g.cp.z2, g.cp.z2 * g.cp.z};
+      for (int c = c0; c < c1; ++c) {
+        const int ijk = __ldg(B.f_ijk + mu0 + c);
+        const int i = ijk & 15, j = (ijk >> 4) & 15, k = (ijk >> 8) & 15;  // each <= 3
+        const float xi = i == 0 ? 1.f : (i == 1 ? px[1] : (i == 2 ? px[2] : px[3]));
+        const float yj = j == 0 ? 1.f : (j == 1 ? py[1] : (j == 2 ? py[2] : py[3]));
+        const float zk = k == 0 ? 1.f : (k == 1 ? pz[1] : (k == 2 ? pz[2] : pz[3]));
+        // the same value as the compile-time forms: a factor 1 is exact
+        put(col0 + c, xi * yj * zk * f1, false);
+      }
+    }
+  }
+}
 
 }  // namespace
 
-__global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_constant__ CUtensorMap tm_hi,
-                                                                  const __grid_constant__ CUtensorMap tm_lo,
-                                                                  DevBasis B, const double* __restrict__ pts,
-                                                                  int64_t npts, const int* __restrict__ tiles,
-                                                                  int stride, float* __restrict__ inv_scale) {
+// kSubs threads per point (thread sub walks the shells sub, sub + kSubs,
+// ... of each half block: uniform in a warp, as sub = threadIdx.x / 128),
+// the tile's half K blocks split over gridDim.y CTAs.  basis_tile_kernel
+// is kSubs = 1 with one CTA per tile; basis_tile_short_kernel (passes with
+// fewer tiles than two per SM, where one CTA per SM cannot hide the shell
+// walk's latency chain) is kSubs = 4 over several CTAs per tile.  Every
+// column of a half block is written by exactly one thread, and the
+// arithmetic of a value does not depend on kSubs: both give the same
+// operand bit for bit.
+template <int kSubs>
+__device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const CUtensorMap& tm_lo, const DevBasis& B,
+                                                const double* __restrict__ pts, int64_t npts,
+                                                const int* __restrict__ tiles, int stride,
+                                                float* __restrict__ inv_scale, float* s_scale) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int row = threadIdx.x;
+  const int row = threadIdx.x & (kBlockM - 1), sub = threadIdx.x >> 7;
   const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBlockM;
   const int64_t p = min(m0 + row, npts - 1);  // rows past the end compute a copy; the TMA store clips them
-  const int nkb = B.kpad / kBlockK;
-  const int nhb = 2 * nkb;
+  const int nhb = 2 * (B.kpad / kBlockK);
+  const int hb0 = static_cast<int>(static_cast<int64_t>(blockIdx.y) * nhb / gridDim.y);
+  const int hb1 = static_cast<int>(static_cast<int64_t>(blockIdx.y + 1) * nhb / gridDim.y);
+  if (kSubs > 1) {
+    // one CTA per SM on cold caches: pull the tables into L1 first
+    prefetch_l1(B.sh_pack, B.nshells * sizeof(int4));
+    prefetch_l1(B.sh_rad2_df, B.nshells * sizeof(float2));
+    prefetch_l1(B.p_pack, B.nprim * sizeof(float4));
+    prefetch_l1(B.atom_df, B.natoms * 3 * sizeof(float2));
+    prefetch_l1(B.f_ijk, B.nbf * sizeof(int));
+    prefetch_l1(B.f_shell, B.nbf * sizeof(int));
+  }
 
   // active K blocks of this tile (all when no screening lists are given)
   uint64_t kb_on = ~0ull;
@@ -113,161 +216,9 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
   // ---- pass 1: log2 of an upper bound of |phi| over the row -------------
   // one table lookup per atom: the envelope of its shells' bounds at the
   // point's distance (shells of K blocks inactive for the tile are out of
-  // range of every point of it, so the envelope does not see them)
-  float lb = -INFINITY;
-  {
-    const float* __restrict__ env = B.atom_env;
-    const int nb = B.env_bins;
-    for (int a = 0; a < B.natoms; ++a) {
-      const float dx = r[0].h - __ldg(&B.atom_df[3 * a].x), dy = r[1].h - __ldg(&B.atom_df[3 * a + 1].x),
-                  dz = r[2].h - __ldg(&B.atom_df[3 * a + 2].x);
-      const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      const float t = (__log2f(fmaxf(d2, 1e-30f)) + kEnvOffset) * kEnvPerOctave;
-      const int bin = t <= 0.f ? 0 : static_cast<int>(t);
-      if (bin < nb) lb = fmaxf(lb, __ldg(env + static_cast<int64_t>(a) * nb + bin));
-    }
-  }
+  // range of every point of it, so the envelope does not see them); by the
+  // first thread of each point
   float scale = 1.f;
-  if (lb > -INFINITY) {
-    // bound < 2^e with e = floor(lb + margin) + 1; scale = 2^(14 - e)
-    const int e = static_cast<int>(floorf(lb + 0.05f)) + 1;
-    scale = ldexpf(1.f, max(-120, min(120, 14 - e)));
-  }
-  if (m0 + row < npts) inv_scale[m0 + row] = 1.f / scale;
-
-  // ---- pass 2: values, staged per K block and stored with TMA -------------
-  Stager st{base, row, __float2half_rn(0.f), __float2half_rn(0.f)};
-  int kb = 0;  // the half block being staged
-  bool active = (kb_on & 1ull) != 0;
-  auto flush = [&](int k) {  // all threads: the K block k is complete in the buffer
-    fence_proxy_async();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      tma_store_2d(&tm_hi, base, k * kHalfK, static_cast<int>(m0));
-      tma_store_2d(&tm_lo, base + kStageBytes, k * kHalfK, static_cast<int>(m0));
-      bulk_commit();
-      bulk_wait_read_0();  // the buffer may be written again
-    }
-    __syncthreads();
-  };
-  auto advance_to = [&](int k) {  // close K blocks before k (zeros never need staging: they are written in order)
-    while (kb < k) {
-      if (active) flush(kb);
-      ++kb;
-      active = kb < nhb && ((kb_on >> (kb >> 1)) & 1ull);
-    }
-  };
-  auto emit = [&](int mu, float v, bool zero) {
-    const int k = mu / kHalfK;
-    if (k != kb) advance_to(k);
-    if (!active) return;
-    const __half z = __float2half_rn(0.f);
-    const __half h = zero ? z : __float2half_rn(v);
-    const __half l = zero ? z : __float2half_rn(v - __half2float(h));
-    if ((mu & 1) == 0) {
-      st.ph = h;
-      st.pl = l;
-    } else {
-      st.put_pair((mu & (kHalfK - 1)) - 1, st.ph, st.pl, h, l);
-    }
-  };
-  {
-    int cur_atom = -1;
-    float px[4] = {1.f, 0.f, 0.f, 0.f}, py[4] = {1.f, 0.f, 0.f, 0.f}, pz[4] = {1.f, 0.f, 0.f, 0.f};
-    DFloat d2{0.f, 0.f};
-    for (int sh = 0; sh < B.nshells; ++sh) {
-      const int4 pk = __ldg(B.sh_pack + sh);  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
-      const int mu0 = pk.y, ncomp = pk.z & 0xff, np = (pk.z >> 8) & 0xff;
-      const int k_first = mu0 >> 6, k_last = (mu0 + ncomp - 1) >> 6;
-      // skip whole shells whose K blocks are inactive for the tile
-      if (!((kb_on >> k_first) & 1ull) && !((kb_on >> k_last) & 1ull)) continue;
-      if (pk.x != cur_atom) {
-        cur_atom = pk.x;
-        float s3[3];
-        d2 = atom_offset(r, B.atom_df, pk.x, s3);
-        px[1] = s3[0];
-        py[1] = s3[1];
-        pz[1] = s3[2];
-        px[2] = px[1] * px[1];
-        py[2] = py[1] * py[1];
-        pz[2] = pz[1] * pz[1];
-        px[3] = px[2] * px[1];
-        py[3] = py[2] * py[1];
-        pz[3] = pz[2] * pz[1];
-      }
-      float f1 = 0.f;
-      const bool in_range = df_le(d2, __ldg(B.sh_rad2_df + sh));
-      if (in_range) {
-        for (int k = 0; k < np; ++k) {
-          const float4 pr = __ldg(B.p_pack + pk.w + k);  // exponent hi, exponent lo, coefficient
-          f1 += pr.z * gauss_df(pr.x, pr.y, d2.h, d2.l);
-        }
-        f1 *= scale;
-      }
-      // a shell out of range for the whole warp only writes zeros
-      if (!__any_sync(0xffffffffu, in_range)) {
-        for (int c = 0; c < ncomp; ++c) emit(mu0 + c, 0.f, true);
-        continue;
-      }
-      for (int c = 0; c < ncomp; ++c) {
-        const int ijk = __ldg(B.f_ijk + mu0 + c);
-        const int i = ijk & 15, j = (ijk >> 4) & 15, k = (ijk >> 8) & 15;  // each <= 3
-        const float xi = i == 0 ? 1.f : (i == 1 ? px[1] : (i == 2 ? px[2] : px[3]));
-        const float yj = j == 0 ? 1.f : (j == 1 ? py[1] : (j == 2 ? py[2] : py[3]));
-        const float zk = k == 0 ? 1.f : (k == 1 ? pz[1] : (k == 2 ? pz[2] : pz[3]));
-        emit(mu0 + c, xi * yj * zk * f1, false);
-      }
-    }
-    // padding columns nbf .. kpad-1 of the last K block are zero
-    for (int mu = B.nbf; mu < B.kpad; ++mu) emit(mu, 0.f, true);
-    advance_to(nhb);
-  }
-  if (threadIdx.x == 0) bulk_wait_all();
-}
-
-// Short passes (fewer tiles than two per SM): the row-by-row shell walk of
-// basis_tile_kernel is a latency chain that one CTA per SM cannot hide.
-// Here a tile's half K blocks are split over gridDim.y CTAs, and within a
-// CTA four threads share a point (512 threads): thread sub of the point walks
-// the shells sub, sub + 4, ... of each half block and stages its components
-// one fp16 at a time; every column of the half block is written by exactly
-// one thread.  The arithmetic of every value is that of basis_tile_kernel,
-// so both kernels give the same operand bit for bit.
-constexpr int kSubs = 4;
-constexpr int kShortThreads = kBlockM * kSubs;
-
-__global__ void __launch_bounds__(kShortThreads) basis_tile_short_kernel(
-    const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo, DevBasis B,
-    const double* __restrict__ pts, int64_t npts, const int* __restrict__ tiles, int stride,
-    float* __restrict__ inv_scale) {
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* base =
-      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ float s_scale[kBlockM];
-  const int row = threadIdx.x & (kBlockM - 1), sub = threadIdx.x >> 7;  // sub is uniform in a warp
-  const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBlockM;
-  const int64_t p = min(m0 + row, npts - 1);  // rows past the end compute a copy; the TMA store clips them
-  const int nhb = 2 * (B.kpad / kBlockK);
-  const int hb0 = static_cast<int>(static_cast<int64_t>(blockIdx.y) * nhb / gridDim.y);
-  const int hb1 = static_cast<int>(static_cast<int64_t>(blockIdx.y + 1) * nhb / gridDim.y);
-  // one CTA per SM on cold caches: pull the tables into L1 first
-  prefetch_l1(B.sh_pack, B.nshells * sizeof(int4));
-  prefetch_l1(B.sh_rad2_df, B.nshells * sizeof(float2));
-  prefetch_l1(B.p_pack, B.nprim * sizeof(float4));
-  prefetch_l1(B.atom_df, B.natoms * 3 * sizeof(float2));
-  prefetch_l1(B.f_ijk, B.nbf * sizeof(int));
-  prefetch_l1(B.f_shell, B.nbf * sizeof(int));
-  uint64_t kb_on = ~0ull;
-  if (tiles) {
-    const int* tl = tiles + blockIdx.x * static_cast<int64_t>(stride);
-    const int nk = tl[1];
-    const int* kl = tl + 2 + B.nchunk;
-    kb_on = 0;
-    for (int i = 0; i < nk; ++i) kb_on |= 1ull << kl[i];
-  }
-  DFloat r[3];
-  for (int c = 0; c < 3; ++c) r[c] = df_split(pts[3 * p + c]);
-  // the row scale, as in basis_tile_kernel, by the first thread of each point
   if (sub == 0) {
     float lb = -INFINITY;
     const float* __restrict__ env = B.atom_env;
@@ -280,75 +231,37 @@ __global__ void __launch_bounds__(kShortThreads) basis_tile_short_kernel(
       const int bin = t <= 0.f ? 0 : static_cast<int>(t);
       if (bin < nb) lb = fmaxf(lb, __ldg(env + static_cast<int64_t>(a) * nb + bin));
     }
-    float scale = 1.f;
     if (lb > -INFINITY) {
+      // bound < 2^e with e = floor(lb + margin) + 1; scale = 2^(14 - e)
       const int e = static_cast<int>(floorf(lb + 0.05f)) + 1;
       scale = ldexpf(1.f, max(-120, min(120, 14 - e)));
     }
-    s_scale[row] = scale;
     if (blockIdx.y == 0 && m0 + row < npts) inv_scale[m0 + row] = 1.f / scale;
   }
-  __syncthreads();
-  const float scale = s_scale[row];
-  auto put = [&](int col, __half h, __half l) {
-    const uint32_t o = swz(row, col);
+  if (kSubs > 1) {
+    if (sub == 0) s_scale[row] = scale;
+    __syncthreads();
+    scale = s_scale[row];
+  }
+
+  // ---- pass 2: values, staged per half K block and stored with TMA --------
+  const uint32_t rowoff = static_cast<uint32_t>(row) * 64u, rxs = static_cast<uint32_t>((row >> 1) & 3) << 4;
+  auto put = [&](int col, float v, bool zero) {
+    const uint32_t o = swz_col(rowoff, rxs, col);
+    const __half z = __float2half_rn(0.f);
+    const __half h = zero ? z : __float2half_rn(v);
+    const __half l = zero ? z : __float2half_rn(v - __half2float(h));
     *reinterpret_cast<__half*>(base + o) = h;
     *reinterpret_cast<__half*>(base + kStageBytes + o) = l;
   };
-  const __half z = __float2half_rn(0.f);
-  int cur_atom = -1;
-  float px[4] = {1.f, 0.f, 0.f, 0.f}, py[4] = {1.f, 0.f, 0.f, 0.f}, pz[4] = {1.f, 0.f, 0.f, 0.f};
-  DFloat d2{0.f, 0.f};
+  AtomGeom g;
   for (int hb = hb0; hb < hb1; ++hb) {
     if (!((kb_on >> (hb >> 1)) & 1ull)) continue;  // inactive for the tile: never read
     const int lo = hb * kHalfK, hi = min(lo + kHalfK, B.nbf);
     if (sub == 0)
-      for (int mu = max(lo, B.nbf); mu < lo + kHalfK; ++mu) put(mu - lo, z, z);  // padding columns
-    if (lo < B.nbf) {
-      for (int sh = __ldg(B.f_shell + lo) + sub; sh < B.nshells; sh += kSubs) {
-        const int4 pk = __ldg(B.sh_pack + sh);  // atom, first function, ncomp | npf << 8 | l << 16, first primitive
-        const int mu0 = pk.y, ncomp = pk.z & 0xff, np = (pk.z >> 8) & 0xff;
-        if (mu0 >= hi) break;  // shells are in function order
-        const int c0 = max(0, lo - mu0), c1 = min(ncomp, hi - mu0);
-        if (pk.x != cur_atom) {
-          cur_atom = pk.x;
-          float s3[3];
-          d2 = atom_offset(r, B.atom_df, pk.x, s3);
-          px[1] = s3[0];
-          py[1] = s3[1];
-          pz[1] = s3[2];
-          px[2] = px[1] * px[1];
-          py[2] = py[1] * py[1];
-          pz[2] = pz[1] * pz[1];
-          px[3] = px[2] * px[1];
-          py[3] = py[2] * py[1];
-          pz[3] = pz[2] * pz[1];
-        }
-        float f1 = 0.f;
-        const bool in_range = df_le(d2, __ldg(B.sh_rad2_df + sh));
-        if (in_range) {
-          for (int k = 0; k < np; ++k) {
-            const float4 pr = __ldg(B.p_pack + pk.w + k);
-            f1 += pr.z * gauss_df(pr.x, pr.y, d2.h, d2.l);
-          }
-          f1 *= scale;
-        }
-        if (!__any_sync(0xffffffffu, in_range)) {
-          for (int c = c0; c < c1; ++c) put(mu0 + c - lo, z, z);
-          continue;
-        }
-        for (int c = c0; c < c1; ++c) {
-          const int ijk = __ldg(B.f_ijk + mu0 + c);
-          const int i = ijk & 15, j = (ijk >> 4) & 15, k = (ijk >> 8) & 15;
-          const float xi = i == 0 ? 1.f : (i == 1 ? px[1] : (i == 2 ? px[2] : px[3]));
-          const float yj = j == 0 ? 1.f : (j == 1 ? py[1] : (j == 2 ? py[2] : py[3]));
-          const float zk = k == 0 ? 1.f : (k == 1 ? pz[1] : (k == 2 ? pz[2] : pz[3]));
-          const float v = xi * yj * zk * f1;
-          const __half h = __float2half_rn(v);
-          put(mu0 + c - lo, h, __float2half_rn(v - __half2float(h)));
-        }
-      }
-    }
+      for (int mu = max(lo, B.nbf); mu < lo + kHalfK; ++mu) put(mu - lo, 0.f, true);  // padding columns
+    if (lo < B.nbf) stage_shells<kSubs>(B, r, scale, lo, hi, sub, g, put);
+    // the half block is complete: write it to HBM, then reuse the buffer
     fence_proxy_async();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -360,6 +273,25 @@ __global__ void __launch_bounds__(kShortThreads) basis_tile_short_kernel(
     __syncthreads();
   }
   if (threadIdx.x == 0) bulk_wait_all();
+}
+
+__global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_constant__ CUtensorMap tm_hi,
+                                                                  const __grid_constant__ CUtensorMap tm_lo,
+                                                                  DevBasis B, const double* __restrict__ pts,
+                                                                  int64_t npts, const int* __restrict__ tiles,
+                                                                  int stride, float* __restrict__ inv_scale) {
+  basis_tile_body<1>(tm_hi, tm_lo, B, pts, npts, tiles, stride, inv_scale, nullptr);
+}
+
+constexpr int kSubs = 4;
+constexpr int kShortThreads = kBlockM * kSubs;
+
+__global__ void __launch_bounds__(kShortThreads) basis_tile_short_kernel(
+    const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo, DevBasis B,
+    const double* __restrict__ pts, int64_t npts, const int* __restrict__ tiles, int stride,
+    float* __restrict__ inv_scale) {
+  __shared__ float s_scale[kBlockM];
+  basis_tile_body<kSubs>(tm_hi, tm_lo, B, pts, npts, tiles, stride, inv_scale, s_scale);
 }
 
 cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* tm_lo, const double* pts,

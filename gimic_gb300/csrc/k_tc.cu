@@ -75,15 +75,6 @@ constexpr int kSmemBytes = kStages * kStageBytes + kRedBytes + 1024 + 512;  // +
 
 __device__ __forceinline__ void reg_dealloc_ctl() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kRegsCtl)); }
 
-// f(integral_constant<int, I>) for I = I0 .. N-1, unrolled at compile time
-template <int I0, int N, typename F>
-__device__ __forceinline__ void static_for(F&& f) {
-  if constexpr (I0 < N) {
-    f(std::integral_constant<int, I0>{});
-    static_for<I0 + 1, N>(f);
-  }
-}
-
 __device__ __forceinline__ void tmem_ld1(uint32_t taddr, float& v) {
   uint32_t r;
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(r) : "r"(taddr) : "memory");
