@@ -302,7 +302,7 @@ def run_scan(args):
     choice_arg = None
     if mode == "auto":
         choice, tt = autotune.tune_scan(pairs, sync=torch.cuda.synchronize)
-        tuned = {"%s/%s" % c: s_ for c, s_ in tt.items()}
+        tuned = {autotune.label(c): s_ for c, s_ in tt.items()}
         mode = choice[0]
         choice_arg = choice[1]
     elif mode == "batch":

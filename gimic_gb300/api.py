@@ -119,6 +119,7 @@ class Gimic:
         return ("file", "locality")[mode.value], list(order[:nshells])
 
     def set_max_batch(self, n):
+        """Points per device pass (at least 128); 0 restores the default."""
         check(self._L.gg_set_max_batch(self._h, int(n)), self._h)
 
     def set_uhf(self, onoff):

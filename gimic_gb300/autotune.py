@@ -9,7 +9,9 @@ at run time is how a batch of molecules is laid out over launches:
   * "batch/given": the same launch with the molecules in the caller's order;
   * "queued/<n>":  one pass per molecule, all queued on one stream before any
     is collected, with at most n points per device pass
-    (gg_plane_integrals_enqueue / _collect, gg_set_max_batch).
+    (gg_plane_integrals_enqueue / _collect, gg_set_max_batch);
+  * "sequential":  one blocking call per molecule (gg_plane_integrals), which
+    replays each context's captured CUDA graph once its layout repeats.
 
 ``tune_scan`` times every candidate on the batch itself (after one warm-up
 call, which also builds the device tables and, for the batch forms, captures
@@ -23,7 +25,7 @@ from . import api
 
 # the queued forms first: their set_max_batch calls would otherwise make the
 # batch forms recapture their graph once more after tuning
-CANDIDATES = (("queued", 1 << 21), ("queued", 1 << 20), ("batch", "given"), ("batch", "cost"))
+CANDIDATES = (("queued", 1 << 21), ("queued", 1 << 20), ("sequential", None), ("batch", "given"), ("batch", "cost"))
 _CHOICE = {}
 
 
@@ -39,9 +41,20 @@ def run(jobs, choice, timings=False):
     mode, arg = choice
     if mode == "batch":
         return api.plane_integrals_batch(jobs, order=arg, timings=timings)
+    if mode == "sequential":
+        if timings:
+            raise ValueError("the sequential layout has no per-molecule stream timings")
+        for g, _ in jobs:
+            g.set_max_batch(0)  # the library's default pass size
+        return [g.plane_integrals(planes) for g, planes in jobs]
     for g, _ in jobs:
         g.set_max_batch(arg)
     return api.plane_integrals_multi(jobs, timings=timings)
+
+
+def label(choice):
+    """'queued/2097152', 'sequential', 'batch/cost', ..."""
+    return choice[0] if choice[1] is None else "%s/%s" % choice
 
 
 def tune_scan(jobs, reps=2, sync=None, candidates=CANDIDATES):

@@ -1153,7 +1153,7 @@ int gg_set_tile_screening(gg_ctx* ctx, int enable) {
 }
 
 int gg_set_max_batch(gg_ctx* ctx, int64_t npts) {
-  if (!ctx || npts < 128) return GG_EINVAL;
+  if (!ctx || (npts != 0 && npts < 128)) return GG_EINVAL;  // 0: the default
   std::lock_guard<std::mutex> g(ctx->mu);
   ctx->max_batch = npts;
   ++ctx->gen;

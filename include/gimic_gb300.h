@@ -93,10 +93,10 @@ int gg_get_magnet(const gg_ctx *ctx, double b[3]);
 int gg_set_screening(gg_ctx *ctx, double thrs);            /* takes effect on the next evaluation */
 int gg_set_flags(gg_ctx *ctx, int giao, int diamag, int paramag);  /* Advanced.GIAO/diamag/paramag */
 int gg_set_precision(gg_ctx *ctx, int mode);               /* GG_PREC_* */
-/* Points per device pass (scratch size), at least 128.  By default the split
- * path takes the largest power of two from 2^18 to 2^21 whose scratch (two
- * pipeline slots of 4 nbf + 128 bytes per point) fits 16 GiB; the FP64 path
- * at most 16,384. */
+/* Points per device pass (scratch size), at least 128; 0 restores the
+ * default.  By default the split path takes the largest power of two from
+ * 2^18 to 2^21 whose scratch (two pipeline slots of 4 nbf + 128 bytes per
+ * point) fits 16 GiB; the FP64 path at most 16,384. */
 int gg_set_max_batch(gg_ctx *ctx, int64_t npts);
 /* Split path: order the points into compact tiles and skip, per tile, the
  * shells that are screened for all of its points (on by default; results do

@@ -72,7 +72,8 @@ def test_batch_rejects_bad_batches(synth_dir, c6h6, c6h6_uhf):
 
 
 def test_autotuner_picks_a_candidate_that_gives_the_same_sums(synth_dir, c6h6, c6h6_uhf):
-    """gimic_gb300.autotune times every launch layout on the batch and keeps
+    """gimic_gb300.autotune times every launch layout on the batch (queued
+    passes, one blocking call per molecule, one batched launch) and keeps
     the fastest per nbf class; every layout gives the same plane sums."""
     torch = pytest.importorskip("torch")
     from gimic_gb300 import autotune
@@ -81,6 +82,11 @@ def test_autotuner_picks_a_candidate_that_gives_the_same_sums(synth_dir, c6h6, c
     assert best in autotune.CANDIDATES and set(times) == set(autotune.CANDIDATES)
     assert all(t > 0 for t in times.values())
     assert autotune.choice_for(pairs) == best
+    assert ("sequential", None) in autotune.CANDIDATES and autotune.label(("sequential", None)) == "sequential"
+    # 0 restores the default pass size; other sizes below 128 are rejected
+    pairs[0][0].set_max_batch(0)
+    with pytest.raises(_lib.GimicError):
+        pairs[0][0].set_max_batch(100)
     ref = autotune.run(pairs, ("batch", "cost"))
     for cand in autotune.CANDIDATES:
         got = autotune.run(pairs, cand)
