@@ -50,6 +50,7 @@ SIGNATURES = {
     "gg_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "gg_set_max_batch": (C.c_int, [C.c_void_p, C.c_int64]),
     "gg_set_tile_screening": (C.c_int, [C.c_void_p, C.c_int]),
+    "gg_set_cross_skip": (C.c_int, [C.c_void_p, C.c_int]),
     "gg_set_shell_order": (C.c_int, [C.c_void_p, C.c_int]),
     "gg_get_shell_order": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gg_basis_info": (C.c_int, [C.c_void_p, _ip, _ip, _ip, _ip]),

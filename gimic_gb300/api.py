@@ -103,6 +103,12 @@ class Gimic:
     def set_tile_screening(self, on=True):
         check(self._L.gg_set_tile_screening(self._h, int(bool(on))), self._h)
 
+    def set_cross_skip(self, on=True):
+        """Issue only the main product of the split for K blocks that are
+        small for a whole tile (on by default; gg_set_cross_skip).  Off:
+        results are bit-identical across batch splits."""
+        check(self._L.gg_set_cross_skip(self._h, int(bool(on))), self._h)
+
     def set_shell_order(self, mode="locality"):
         """'locality' (default): shells grouped by screening radius along a
         tour of the atoms, which lets tile screening skip more work; 'file':

@@ -124,6 +124,7 @@ struct gg_ctx {
   gg::Flags flags{1, 1, 1};
   int precision = GG_PREC_SPLIT16;
   bool tile_screening = true;
+  bool cross_skip = true;  // gg_set_cross_skip
   int device = 0;
   int64_t max_batch = 0;  // points per device pass; 0: batch_points() chooses
 
@@ -147,13 +148,14 @@ struct gg_ctx {
   // while the contraction of batch b runs on the caller's stream.
   struct SplitSlot {
     DevBuf a_hi, a_lo, inv_row, sort_keys, sort_keys2, sort_idx, sort_perm, sort_temp, pts_sorted, tile_lists,
-        tile_ord;
+        tile_ord, cross_mask;
     CUtensorMap tma_hi, tma_lo;  // the contraction's loads
     CUtensorMap tms_hi, tms_lo;  // the basis kernel's stores
     const double* tp = nullptr;
     const int* tiles = nullptr;
     const int* perm = nullptr;
     const int* tord = nullptr;
+    unsigned long long* xn = nullptr;  // per tile: half K blocks that need the cross products
     int stride = 0;
     int64_t n = 0;
     bool used = false;  // a contraction has been enqueued on this slot
@@ -254,7 +256,7 @@ struct gg_ctx {
                               &tc_part, &tc_done, &mjobs};
     for (SplitSlot& sl : slot)
       for (DevBuf* b : {&sl.a_hi, &sl.a_lo, &sl.inv_row, &sl.sort_keys, &sl.sort_keys2, &sl.sort_idx, &sl.sort_perm,
-                        &sl.sort_temp, &sl.pts_sorted, &sl.tile_lists, &sl.tile_ord})
+                        &sl.sort_temp, &sl.pts_sorted, &sl.tile_lists, &sl.tile_ord, &sl.cross_mask})
         v.push_back(b);
     return v;
   }
@@ -727,6 +729,7 @@ struct gg_ctx {
     sl.tiles = nullptr;
     sl.perm = nullptr;
     sl.tord = nullptr;
+    sl.xn = nullptr;
     if (screen) {
       const int64_t ntiles = (n + gg::kBlockM - 1) / gg::kBlockM;
       const size_t tb = std::max(gg::sort_temp_bytes(n), gg::tile_order_temp_bytes(ntiles));
@@ -738,6 +741,7 @@ struct gg_ctx {
       if (e == cudaSuccess) e = sl.pts_sorted.reserve(static_cast<size_t>(n) * 3 * sizeof(double));
       if (e == cudaSuccess) e = sl.tile_lists.reserve(static_cast<size_t>(ntiles) * stride * sizeof(int));
       if (e == cudaSuccess) e = sl.tile_ord.reserve(static_cast<size_t>(ntiles) * sizeof(int));
+      if (e == cudaSuccess) e = sl.cross_mask.reserve(static_cast<size_t>(ntiles) * 2 * sizeof(unsigned long long));
       if (e != cudaSuccess) return cuda_fail(e, "tile-screening scratch");
       // every tile gets an SM of its own at once: no tile ordering, and
       // points that come in coherent runs need no spatial sort either
@@ -772,6 +776,13 @@ struct gg_ctx {
       sl.tiles = sl.tile_lists.as<int>();
       sl.perm = sort ? sl.sort_perm.as<int>() : nullptr;
       sl.tord = order ? sl.tile_ord.as<int>() : nullptr;
+      // every half K block needs the cross products until the basis kernel
+      // finds it small for the whole tile
+      if (cross_skip) {
+        sl.xn = sl.cross_mask.as<unsigned long long>();
+        e = cudaMemsetAsync(sl.xn, 0xff, static_cast<size_t>(ntiles) * 2 * sizeof(unsigned long long), st);
+        if (e != cudaSuccess) return cuda_fail(e, "cross-product mask");
+      }
     }
     if (!encode_fp16_2d(&sl.tma_hi, sl.a_hi.p, n, dB.kpad, gg::kBlockM) ||
         !encode_fp16_2d(&sl.tma_lo, sl.a_lo.p, n, dB.kpad, gg::kBlockM) ||
@@ -779,7 +790,8 @@ struct gg_ctx {
         !encode_fp16_2d(&sl.tms_lo, sl.a_lo.p, n, dB.kpad, gg::kBlockM, true))
       return fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
     prof_begin(GG_PROF_BASIS, st, &ps);
-    e = gg::launch_basis_tile(dB, &sl.tms_hi, &sl.tms_lo, sl.tp, n, sl.tiles, stride, sl.inv_row.as<float>(), st);
+    e = gg::launch_basis_tile(dB, &sl.tms_hi, &sl.tms_lo, sl.tp, n, sl.tiles, stride, sl.inv_row.as<float>(), sl.xn,
+                              st);
     prof_end(st, ps);
     if (e != cudaSuccess) return cuda_fail(e, "basis kernel launch");
     launches += 1;
@@ -794,6 +806,7 @@ struct gg_ctx {
     ta.tile_stride = sl.stride;
     ta.perm = sl.perm;
     ta.tile_order = sl.tord;
+    ta.xneed = sl.xn;
     if (prof.on) {
       const unsigned long long blocks = static_cast<unsigned long long>((sl.n + gg::kBlockM - 1) / gg::kBlockM) *
                                         dB.nchunk * (dB.kpad / gg::kBlockK);
@@ -1148,6 +1161,14 @@ int gg_set_tile_screening(gg_ctx* ctx, int enable) {
   if (!ctx) return GG_EINVAL;
   std::lock_guard<std::mutex> g(ctx->mu);
   ctx->tile_screening = enable != 0;
+  ++ctx->gen;
+  return GG_OK;
+}
+
+int gg_set_cross_skip(gg_ctx* ctx, int enable) {
+  if (!ctx) return GG_EINVAL;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->cross_skip = enable != 0;
   ++ctx->gen;
   return GG_OK;
 }
@@ -1626,6 +1647,7 @@ int batch_enqueue(gg_ctx* lead, const std::vector<gg_ctx*>& c, BatchPlan& B, cud
     J.out = gg::Outputs{x->jt.as<double>(), nullptr, nullptr};
     J.tiles = sl.tiles;
     J.tstride = sl.stride;
+    J.xneed = sl.xn;
     J.perm = sl.perm;
     J.tile_order = sl.tord;
     J.step0 = step;
@@ -2176,7 +2198,7 @@ extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t 
     return ctx->fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
   size_t ps = 0;
   ctx->prof_begin(GG_PROF_BASIS, st, &ps);
-  e = gg::launch_basis_tile(ctx->dB, &tms_hi, &tms_lo, pts, n, nullptr, 0, inv_row, st);
+  e = gg::launch_basis_tile(ctx->dB, &tms_hi, &tms_lo, pts, n, nullptr, 0, inv_row, nullptr, st);
   ctx->prof_end(st, ps);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "basis kernel launch");
   gg::TcArgs ta{&tma_hi, &tma_lo, &ctx->tm_b_hi, &ctx->tm_b_lo, inv_row, ctx->inv_col.as<float>(),

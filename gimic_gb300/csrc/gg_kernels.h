@@ -20,8 +20,21 @@ constexpr int kNDots = 37;
 // bound, K blocks staged in shared memory and written with TMA tensor stores
 // through the point operand's own tensor maps; with tile lists, inactive K
 // blocks are skipped.
+//
+// Cross products: xneed (null: none) holds two 64-bit words per tile, one
+// bit per half K block (32 functions), all ones on entry.  The kernel
+// clears the bit of every half block whose scaled values are all below
+// kCrossSkipScaled in magnitude for every point of the tile: 2^-14 of the
+// row-scale bound (2^14), itself at least the row's largest value.  The
+// lo part of an fp16 split is at most 2^-11 of the value, so for such a
+// block the two cross products of the split (hi*lo, lo*hi) add at most
+// 2^-24 of the row's largest basis value times the matrix entry per term:
+// one fp32 rounding of the main product's largest terms.  The contraction
+// issues only the block's main product (hi*hi).
+constexpr float kCrossSkipScaled = 1.0f;
 cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* tm_lo, const double* pts,
-                              int64_t npts, const int* tiles, int stride, float* inv_scale, cudaStream_t st);
+                              int64_t npts, const int* tiles, int stride, float* inv_scale,
+                              unsigned long long* xneed, cudaStream_t st);
 // phi, grad phi and the Laplacian in fp64 for the plain FP64 path.
 void launch_basis_fp64(const DevBasis& B, const double* pts, int64_t npts, int64_t ld, double* phi, double* gx,
                        double* gy, double* gz, double* lap, cudaStream_t st);
@@ -61,6 +74,9 @@ struct TcArgs {
   int csplit = 1;
   float2* part = nullptr;
   unsigned* tile_done = nullptr;
+  // per tile, the half K blocks that need the cross products (as cleared by
+  // launch_basis_tile; null: all of them)
+  const unsigned long long* xneed = nullptr;
 };
 int tc_smem_bytes();
 
@@ -79,6 +95,7 @@ struct TcJob {
   Outputs out;
   const int* tiles;
   int tstride;
+  const unsigned long long* xneed;  // as TcArgs::xneed
   const int* perm;
   const int* tile_order;
   int64_t step0;

@@ -180,7 +180,8 @@ template <int kSubs>
 __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const CUtensorMap& tm_lo, const DevBasis& B,
                                                 const double* __restrict__ pts, int64_t npts,
                                                 const int* __restrict__ tiles, int stride,
-                                                float* __restrict__ inv_scale, float* s_scale) {
+                                                float* __restrict__ inv_scale, unsigned long long* xneed,
+                                                float* s_scale) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -246,7 +247,9 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
 
   // ---- pass 2: values, staged per half K block and stored with TMA --------
   const uint32_t rowoff = static_cast<uint32_t>(row) * 64u, rxs = static_cast<uint32_t>((row >> 1) & 3) << 4;
+  float vmax = 0.f;  // largest |value| this thread stages in the current half block
   auto put = [&](int col, float v, bool zero) {
+    if (!zero) vmax = fmaxf(vmax, fabsf(v));
     const uint32_t o = swz_col(rowoff, rxs, col);
     const __half z = __float2half_rn(0.f);
     const __half h = zero ? z : __float2half_rn(v);
@@ -261,9 +264,13 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
     if (sub == 0)
       for (int mu = max(lo, B.nbf); mu < lo + kHalfK; ++mu) put(mu - lo, 0.f, true);  // padding columns
     if (lo < B.nbf) stage_shells<kSubs>(B, r, scale, lo, hi, sub, g, put);
-    // the half block is complete: write it to HBM, then reuse the buffer
+    // the half block is complete: write it to HBM, then reuse the buffer;
+    // a half block small for every point of the tile needs no cross products
     fence_proxy_async();
-    __syncthreads();
+    const int small = __syncthreads_and(vmax < kCrossSkipScaled);
+    vmax = 0.f;
+    if (threadIdx.x == 0 && small && xneed)
+      atomicAnd(xneed + 2 * static_cast<int64_t>(blockIdx.x) + (hb >> 6), ~(1ull << (hb & 63)));
     if (threadIdx.x == 0) {
       tma_store_2d(&tm_hi, base, hb * kHalfK, static_cast<int>(m0));
       tma_store_2d(&tm_lo, base + kStageBytes, hb * kHalfK, static_cast<int>(m0));
@@ -279,8 +286,9 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
                                                                   const __grid_constant__ CUtensorMap tm_lo,
                                                                   DevBasis B, const double* __restrict__ pts,
                                                                   int64_t npts, const int* __restrict__ tiles,
-                                                                  int stride, float* __restrict__ inv_scale) {
-  basis_tile_body<1>(tm_hi, tm_lo, B, pts, npts, tiles, stride, inv_scale, nullptr);
+                                                                  int stride, float* __restrict__ inv_scale,
+                                                                  unsigned long long* __restrict__ xneed) {
+  basis_tile_body<1>(tm_hi, tm_lo, B, pts, npts, tiles, stride, inv_scale, xneed, nullptr);
 }
 
 constexpr int kSubs = 4;
@@ -289,13 +297,14 @@ constexpr int kShortThreads = kBlockM * kSubs;
 __global__ void __launch_bounds__(kShortThreads) basis_tile_short_kernel(
     const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo, DevBasis B,
     const double* __restrict__ pts, int64_t npts, const int* __restrict__ tiles, int stride,
-    float* __restrict__ inv_scale) {
+    float* __restrict__ inv_scale, unsigned long long* __restrict__ xneed) {
   __shared__ float s_scale[kBlockM];
-  basis_tile_body<kSubs>(tm_hi, tm_lo, B, pts, npts, tiles, stride, inv_scale, s_scale);
+  basis_tile_body<kSubs>(tm_hi, tm_lo, B, pts, npts, tiles, stride, inv_scale, xneed, s_scale);
 }
 
 cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* tm_lo, const double* pts,
-                              int64_t npts, const int* tiles, int stride, float* inv_scale, cudaStream_t st) {
+                              int64_t npts, const int* tiles, int stride, float* inv_scale,
+                              unsigned long long* xneed, cudaStream_t st) {
   if (npts <= 0) return cudaSuccess;
   if (B.kpad / kBlockK > 64) return cudaErrorInvalidValue;  // K-block mask is 64 bits
   // the shared-memory attribute (it applies to the current device) and the
@@ -321,11 +330,11 @@ cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* 
   if (kgroups > 1)
     basis_tile_short_kernel<<<grid, kShortThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
                                                                    *static_cast<const CUtensorMap*>(tm_lo), B, pts,
-                                                                   npts, tiles, stride, inv_scale);
+                                                                   npts, tiles, stride, inv_scale, xneed);
   else
     basis_tile_kernel<<<grid, kTileThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
                                                             *static_cast<const CUtensorMap*>(tm_lo), B, pts, npts,
-                                                            tiles, stride, inv_scale);
+                                                            tiles, stride, inv_scale, xneed);
   return cudaGetLastError();
 }
 

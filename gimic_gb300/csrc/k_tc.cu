@@ -108,6 +108,7 @@ static_assert(dot_matrix(12) == 0 && dot_matrix(13) == 1 && dot_matrix(21) == 3 
 struct JobView {
   const void *a_hi, *a_lo, *b_hi, *b_lo;  // CUtensorMap
   const int* tiles;
+  const unsigned long long* xneed;  // half K blocks that need the cross products (null: all)
   int tstride, nchunk, nkb;
   const int* tile_order;
   int64_t step0, npts;
@@ -156,8 +157,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const double* __restrict__ pts, int64_t npts, Flags fl, Outputs out, int* err,
                     const int* __restrict__ tiles, int tstride, const int* __restrict__ perm,
                     const int* __restrict__ tile_order, int* __restrict__ tile_counter, int csplit,
-                    float2* __restrict__ part, unsigned* __restrict__ tile_done, const TcJob* __restrict__ jobs,
-                    int njobs, int64_t multi_steps) {
+                    float2* __restrict__ part, unsigned* __restrict__ tile_done,
+                    const unsigned long long* __restrict__ xneed, const TcJob* __restrict__ jobs, int njobs,
+                    int64_t multi_steps) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                          ~static_cast<uintptr_t>(1023));
@@ -205,6 +207,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       v.nchunk = J.B.nchunk;
       v.nkb = J.B.kpad / kBlockK;
       v.tile_order = J.tile_order;
+      v.xneed = J.xneed;
       v.step0 = J.step0;
       v.npts = J.npts;
     } else {
@@ -217,6 +220,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       v.nchunk = Bs.nchunk;
       v.nkb = Bs.kpad / kBlockK;
       v.tile_order = tile_order;
+      v.xneed = xneed;
       v.step0 = 0;
       v.npts = npts;
     }
@@ -248,6 +252,16 @@ __global__ void __launch_bounds__(kThreads, 1)
   };
   auto kb_at = [&](const JobView& v, int64_t tile, int i) -> int {
     return v.tiles ? v.tiles[tile * v.tstride + 2 + v.nchunk + i] : i;
+  };
+  // whether K block kb of the tile needs the cross products (either of its
+  // two half blocks' bits); the tile's two mask words are read once per step
+  auto cross_words = [&](const JobView& v, int64_t tile, unsigned long long* w0, unsigned long long* w1) {
+    *w0 = v.xneed ? v.xneed[2 * tile] : ~0ull;
+    *w1 = v.xneed ? v.xneed[2 * tile + 1] : ~0ull;
+  };
+  auto needs_cross = [](unsigned long long w0, unsigned long long w1, int kb) -> bool {
+    const int h = 2 * kb;  // both half blocks in one word (h is even)
+    return (((h < 64 ? w0 : w1) >> (h & 63)) & 3ull) != 0;
   };
   auto failed = [&]() -> bool { return *reinterpret_cast<volatile int*>(err) != 0; };
   // epilogue tables: matrix scales, per-function records (shell << 12 |
@@ -349,21 +363,27 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int64_t tile = tile_of(v, t);
         const int m0 = static_cast<int>(tile * kBlockM);
         const int nkb = n_kb(v, tile), nchunk = n_chunk(v, tile, nkb);
+        unsigned long long xw0, xw1;
+        cross_words(v, tile, &xw0, &xw1);
         int c0, c1;
         chunk_span(t, nchunk, &c0, &c1);
         for (int ci = c0; ci < c1; ++ci) {
           const int c = chunk_at(v, tile, ci);
-          // cross pass: (A_hi, B_lo) then (A_lo, B_hi) of every K block;
-          // main pass: (A_hi, B_hi) of every K block; one pair per stage
-          for (int q = 0; q < 3 * nkb; ++q, ++it) {
-            const int kb = kb_at(v, tile, q < 2 * nkb ? q >> 1 : q - 2 * nkb);
-            const bool a_lo = q < 2 * nkb && (q & 1), b_lo = q < 2 * nkb && !(q & 1);
+          // cross pass: (A_hi, B_lo) then (A_lo, B_hi) of every K block that
+          // needs them; main pass: (A_hi, B_hi) of every K block; one pair
+          // per stage
+          for (int q = 0; q < 3 * nkb; ++q) {
+            const bool cross = q < 2 * nkb;
+            const int kb = kb_at(v, tile, cross ? q >> 1 : q - 2 * nkb);
+            if (cross && !needs_cross(xw0, xw1, kb)) continue;
+            const bool a_lo = cross && (q & 1), b_lo = cross && !(q & 1);
             const int s = it % kStages, round = it / kStages;
             if (!mbar_wait(&empty[s], (round & 1) ^ 1, err, 1)) goto producer_exit;
             unsigned char* st = base + s * kStageBytes;
             mbar_expect_tx(&full[s], kStageBytes);
             tma_load_2d(st, a_lo ? v.a_lo : v.a_hi, &full[s], kb * kBlockK, m0);
             tma_load_2d(st + kTileA, b_lo ? v.b_lo : v.b_hi, &full[s], kb * kBlockK, c * kBlockN);
+            ++it;
           }
         }
       }
@@ -391,6 +411,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         const JobView v = view(j);
         const int64_t tile = tile_of(v, t);
         const int nkb = n_kb(v, tile), nchunk = n_chunk(v, tile, nkb);
+        // the producer's stage count per chunk: two cross pieces for each K
+        // block that needs them, then one main piece for every K block
+        unsigned long long xw0, xw1;
+        cross_words(v, tile, &xw0, &xw1);
+        int nstage = nkb;
+        for (int i = 0; i < nkb; ++i)
+          if (needs_cross(xw0, xw1, kb_at(v, tile, i))) nstage += 2;
         int c0, c1;
         chunk_span(t, nchunk, &c0, &c1);
         for (int ci = c0; ci < c1; ++ci, ++acc) {
@@ -398,8 +425,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (!mbar_wait(&accempty[b], (rb & 1) ^ 1, err, 2)) goto mma_exit;
           tc_fence_after();
           const uint32_t d_tmem = tmem_base + b * kAccStride;
-          // the stage sequence of the producer: 2 nkb cross pieces, then nkb main
-          for (int q = 0; q < 3 * nkb; ++q, ++it) {
+          for (int q = 0; q < nstage; ++q, ++it) {
             const int s = it % kStages, round = it / kStages;
             if (!mbar_wait(&full[s], round & 1, err, 3)) goto mma_exit;
             tc_fence_after();
@@ -795,7 +821,7 @@ cudaError_t launch_tc_fused(const DevBasis& B, const TcArgs& a, cudaStream_t st)
       *static_cast<const CUtensorMap*>(a.tmap_a_hi), *static_cast<const CUtensorMap*>(a.tmap_a_lo),
       *static_cast<const CUtensorMap*>(a.tmap_b_hi), *static_cast<const CUtensorMap*>(a.tmap_b_lo), B,
       a.inv_row_scale, a.inv_col_scale, a.pts, a.npts, a.flags, a.out, a.err, a.tiles, a.tile_stride, a.perm,
-      a.tile_order, a.tile_counter, csplit, a.part, a.tile_done, nullptr, 0, 0);
+      a.tile_order, a.tile_counter, csplit, a.part, a.tile_done, a.xneed, nullptr, 0, 0);
   return cudaGetLastError();
 }
 
@@ -815,7 +841,7 @@ cudaError_t launch_tc_fused_multi(const TcJob* jobs, int njobs, int64_t nsteps, 
   auto kernel = div ? tc_fused_kernel<true, true> : tc_fused_kernel<false, true>;
   kernel<<<grid, kThreads, kSmemBytes, st>>>(none, none, none, none, nob, nullptr, nullptr, nullptr, 0, flags,
                                              noout, err, nullptr, 0, nullptr, nullptr, tile_counter, 1, nullptr,
-                                             nullptr, jobs, njobs, nsteps);
+                                             nullptr, nullptr, jobs, njobs, nsteps);
   return cudaGetLastError();
 }
 

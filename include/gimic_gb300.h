@@ -102,6 +102,15 @@ int gg_set_max_batch(gg_ctx *ctx, int64_t npts);
  * shells that are screened for all of its points (on by default; results do
  * not change, only the work skipped). */
 int gg_set_tile_screening(gg_ctx *ctx, int enable);
+/* Split path with tile screening: issue only the main (hi*hi) product of
+ * the split for K blocks whose basis values stay below 2^-14 of every
+ * point's row bound in the tile (on by default).  The two cross products of
+ * such a block add at most one fp32 rounding of the main product's largest
+ * terms; the error against the FP64 path is unchanged.  Which blocks qualify
+ * depends on a tile's points, so with it on a point's result can differ in
+ * the last bits between batch splits; off, every batch split and the tile
+ * screening itself give bit-identical results. */
+int gg_set_cross_skip(gg_ctx *ctx, int enable);
 /* Internal order of the shells (and so of the basis functions and density
  * rows/columns).  mode 1 (the default, set at creation): shells grouped by
  * screening radius, atoms along a nearest-neighbour tour, when that activates

@@ -147,20 +147,35 @@ def test_edge_cases(c6h6):
 
 
 def test_batching_is_invariant(c6h6):
-    """Tiles are independent: any batch split gives bit-identical results."""
+    """Tiles are independent: with the cross-product skip off, any batch
+    split gives bit-identical results.  With it on (the default) the blocks
+    whose cross products are skipped depend on a tile's points, so a point's
+    result may change in its last bits with the split (one fp32 rounding of
+    the main product per skipped block)."""
     mp, xp, _ = c6h6
     g = api.Gimic(mp, xp, screening=1e-8)
     pts = sample_points(g.atoms()[0], 3000, 100, 8.0, seed=9)
-    a = g.jtensor_batch(pts)
-    g.set_max_batch(256)
-    b = g.jtensor_batch(pts)
-    c = np.vstack([g.jtensor_batch(pts[s:s + 777]) for s in range(0, len(pts), 777)])
-    assert np.array_equal(a, b) and np.array_equal(a, c)
+
+    def splits():
+        g.set_max_batch(0)
+        a = g.jtensor_batch(pts)
+        g.set_max_batch(256)
+        b = g.jtensor_batch(pts)
+        c = np.vstack([g.jtensor_batch(pts[s:s + 777]) for s in range(0, len(pts), 777)])
+        return a, b, c
+
+    a, b, c = splits()  # skip on
+    assert rel_max_err(b, a) <= 1e-7 and rel_max_err(c, a) <= 1e-7
+    g.set_cross_skip(False)
+    a0, b0, c0 = splits()
+    assert np.array_equal(a0, b0) and np.array_equal(a0, c0)
+    assert rel_max_err(a, a0) <= 1e-7
 
 
 def test_tile_screening_is_exact(c6h6):
     """Tile screening only skips exact zeros: results are bit-identical with
-    and without it, for compact, scattered and far-away points."""
+    and without it, for compact, scattered and far-away points (with the
+    cross-product skip off; on, within one fp32 rounding)."""
     mp, xp, _ = c6h6
     g = api.Gimic(mp, xp, screening=1e-8)
     rng = np.random.default_rng(12)
@@ -169,11 +184,16 @@ def test_tile_screening_is_exact(c6h6):
     pts = np.vstack([cube, sample_points(g.atoms()[0], 2000, 300, 9.0, seed=13),
                      rng.uniform(-60.0, 60.0, (500, 3))])
     pts = pts[rng.permutation(len(pts))]
+    g.set_cross_skip(False)  # the skip needs the tile lists: compare like with like
     a = g.jtensor_batch(pts, rho=True, divj=True)
     g.set_tile_screening(False)
     b = g.jtensor_batch(pts, rho=True, divj=True)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+    g.set_tile_screening(True)
+    g.set_cross_skip(True)
+    for x, y in zip(g.jtensor_batch(pts, rho=True, divj=True), a):
+        assert rel_max_err(x, y) <= 1e-7
     o = oracle.Oracle(mp, xp, screening=1e-8)
     sel = rng.choice(len(pts), 800, replace=False)
     assert rel_max_err(a[0][sel], o.jtensor(pts[sel])) <= TOL_SPLIT
