@@ -677,12 +677,16 @@ def main():
     basis_ms, basis_n = prof["basis"]
     order_ms, order_n = prof["order"]
     issued, dense = prof["gemm_blocks"]
+    cross = prof["cross_blocks"]
     per_launch_pts = npts / (tc_n / args.steps)
     tc_avg = tc_ms / tc_n
     # one GEMM block = 128 points x 224 columns x 64-deep, one product of the
     # three-term split (the other two are the split's emulation overhead)
     block_flops = 2.0 * 128 * 224 * 64
     exec_tflops = issued * block_flops / (tc_ms * 1e-3) / 1e12
+    # all products the tensor pipe ran: the main product of every issued
+    # block and the two cross products of the blocks that keep them
+    pipe_tflops = (issued + 2 * cross) * block_flops / (tc_ms * 1e-3) / 1e12
     dense_tflops = flops_per_point(n) * per_launch_pts / (tc_avg * 1e-3) / 1e12
     pk = peaks()
     if pk:
@@ -815,12 +819,17 @@ def main():
         "roofline": {"bound": "tensor", "achieved": exec_tflops, "peak": peak_tf, "unit": "TFLOP/s",
                      "frac": exec_tflops / peak_tf, "peak_source": peak_src,
                      "accounting": "flops of the GEMM blocks issued after tile screening (one product of the "
-                                   "three-term split) / tc_fused_kernel time",
+                                   "three-term split: the main product every block issues; the cross products "
+                                   "are precision overhead, skipped for blocks small for a whole tile) / "
+                                   "tc_fused_kernel time",
                      "traffic": (tmodel[0] + tmodel[1] * per_launch_pts) if tmodel else None,
                      "traffic_source": "ncu dram bytes of the 65,536-point profile case scaled to the launch: "
                                        "fixed matrix operand + bytes per point x points",
                      "kernel": "tc_fused_kernel", "launch_ms": tc_avg, "points_per_launch": per_launch_pts,
                      "gemm_blocks_issued_fraction": issued / dense if dense else None,
+                     "cross_products_issued_fraction": cross / issued if issued else None,
+                     "tensor_pipe_tflops_all_products": pipe_tflops,
+                     "tensor_pipe_frac_of_sustained": pipe_tflops / (3.0 * peak_tf),
                      "dense_equivalent_tflops": dense_tflops,
                      "algorithmic_flops_per_point": flops_per_point(n),
                      "basis_kernel_ms": basis_ms / max(1, basis_n),

@@ -73,6 +73,7 @@ SIGNATURES = {
     "gg_jtensor_batch_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_void_p]),
     "gg_profile_read": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "gg_profile_cross": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "gg_jtensor_batch_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "gg_properties": (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, _dp, C.c_int, C.POINTER(C.c_int64), C.c_int, _dp,

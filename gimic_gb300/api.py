@@ -180,6 +180,9 @@ class Gimic:
         issued, dense = C.c_int64(), C.c_int64()
         check(self._L.gg_profile_blocks(self._h, C.byref(issued), C.byref(dense)), self._h)
         out["gemm_blocks"] = (int(issued.value), int(dense.value))
+        cross = C.c_int64()
+        check(self._L.gg_profile_cross(self._h, C.byref(cross)), self._h)
+        out["cross_blocks"] = int(cross.value)  # of the issued blocks, those with the cross products
         return out
 
     # ---- evaluation -----------------------------------------------------

@@ -212,7 +212,7 @@ struct gg_ctx {
     size_t used = 0;
     double ms[GG_NPROF] = {0};
     int64_t launches[GG_NPROF] = {0};
-    unsigned long long* d_blocks = nullptr;  // GEMM blocks issued (profiling only)
+    unsigned long long* d_blocks = nullptr;  // [2]: GEMM blocks issued, of them with the cross products (profiling only)
     unsigned long long dense_blocks = 0;     // blocks without screening
     unsigned long long host_blocks = 0;      // blocks of unscreened batches
   } prof;
@@ -233,7 +233,8 @@ struct gg_ctx {
     if (prof.on) cudaEventRecord(prof.pool[slot].second, st);
   }
   void prof_add_blocks(unsigned long long v, cudaStream_t st) {
-    // host-known count (no screening): fold into the device counter later
+    // host-known count (no screening, so no cross-product skip either): fold
+    // into both device counters later
     prof.host_blocks += v;
     (void)st;
   }
@@ -794,6 +795,11 @@ struct gg_ctx {
                               st);
     prof_end(st, ps);
     if (e != cudaSuccess) return cuda_fail(e, "basis kernel launch");
+    if (prof.on && prof.d_blocks && sl.tiles) {  // blocks that keep their cross products
+      const int64_t ntiles = (n + gg::kBlockM - 1) / gg::kBlockM;
+      if (sl.xn) gg::launch_cross_work(sl.tiles, sl.xn, ntiles, stride, dB.nchunk, prof.d_blocks + 1, st);
+      else gg::launch_tile_work(sl.tiles, ntiles, stride, prof.d_blocks + 1, st);
+    }
     launches += 1;
     return GG_OK;
   }
@@ -1851,11 +1857,11 @@ int gg_profile(gg_ctx* ctx, int enable) {
   ctx->prof.host_blocks = 0;
   if (ctx->prof.on) {
     cudaSetDevice(ctx->device);
-    if (!ctx->prof.d_blocks && cudaMalloc(&ctx->prof.d_blocks, sizeof(unsigned long long)) != cudaSuccess) {
+    if (!ctx->prof.d_blocks && cudaMalloc(&ctx->prof.d_blocks, 2 * sizeof(unsigned long long)) != cudaSuccess) {
       ctx->prof.d_blocks = nullptr;
       return ctx->fail(GG_ENOMEM, "profiling counter");
     }
-    cudaMemset(ctx->prof.d_blocks, 0, sizeof(unsigned long long));
+    cudaMemset(ctx->prof.d_blocks, 0, 2 * sizeof(unsigned long long));
   }
   ctx->launches = 0;
   return GG_OK;
@@ -1868,6 +1874,14 @@ int gg_profile_read(const gg_ctx* ctx, double ms[GG_NPROF], int64_t launches[GG_
     if (launches) launches[i] = ctx->prof.launches[i];
   }
   if (total_kernels) *total_kernels = ctx->launches;
+  return GG_OK;
+}
+
+int gg_profile_cross(const gg_ctx* ctx, int64_t* cross) {
+  if (!ctx || !cross) return GG_EINVAL;
+  unsigned long long dev = 0;
+  if (ctx->prof.d_blocks) cudaMemcpy(&dev, ctx->prof.d_blocks + 1, sizeof(dev), cudaMemcpyDeviceToHost);
+  *cross = static_cast<int64_t>(dev + ctx->prof.host_blocks);
   return GG_OK;
 }
 

@@ -111,6 +111,10 @@ cudaError_t launch_spatial_order(const double* pts, int64_t n, const double lo[3
                                  double* pts_sorted, cudaStream_t st);
 void launch_tile_screen(const DevBasis& B, const double* pts_sorted, int64_t n, int* tiles, cudaStream_t st);
 void launch_tile_work(const int* tiles, int64_t ntiles, int stride, unsigned long long* acc, cudaStream_t st);
+// acc += the blocks (chunks x K blocks) of the tiles whose K block needs the
+// cross products (xneed as TcArgs::xneed; profiling)
+void launch_cross_work(const int* tiles, const unsigned long long* xneed, int64_t ntiles, int stride, int nchunk,
+                       unsigned long long* acc, cudaStream_t st);
 // Tiles ordered by decreasing GEMM work (blocks = chunks x K blocks), so that
 // the heaviest tiles start first and the tail of the launch is short.
 size_t tile_order_temp_bytes(int64_t ntiles);

@@ -138,6 +138,30 @@ void launch_tile_work(const int* tiles, int64_t ntiles, int stride, unsigned lon
   tile_work_kernel<<<static_cast<unsigned>((ntiles + 255) / 256), 256, 0, st>>>(tiles, ntiles, stride, acc);
 }
 
+__global__ void cross_work_kernel(const int* __restrict__ tiles, const unsigned long long* __restrict__ xneed,
+                                  int64_t ntiles, int stride, int nchunk, unsigned long long* __restrict__ acc) {
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  unsigned long long v = 0;
+  if (t < ntiles) {
+    const int* tl = tiles + t * stride;
+    const int nk = tl[1];
+    int n = 0;
+    for (int i = 0; i < nk; ++i) {
+      const int h = 2 * tl[2 + nchunk + i];
+      n += ((xneed[2 * t + (h >> 6)] >> (h & 63)) & 3ull) != 0;
+    }
+    v = static_cast<unsigned long long>(tl[0]) * n;
+  }
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(acc, v);
+}
+
+void launch_cross_work(const int* tiles, const unsigned long long* xneed, int64_t ntiles, int stride, int nchunk,
+                       unsigned long long* acc, cudaStream_t st) {
+  cross_work_kernel<<<static_cast<unsigned>((ntiles + 255) / 256), 256, 0, st>>>(tiles, xneed, ntiles, stride,
+                                                                                  nchunk, acc);
+}
+
 int tile_stride(const DevBasis& B) { return 2 + B.nchunk + B.kpad / kBlockK; }
 
 __global__ void tile_work_keys_kernel(const int* __restrict__ tiles, int64_t ntiles, int stride,

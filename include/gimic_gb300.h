@@ -238,6 +238,10 @@ int gg_profile_read(const gg_ctx *ctx, double ms[GG_NPROF], int64_t launches[GG_
  * 64 (three fp16 products each): issued after tile screening, and the count
  * a dense contraction would have issued. */
 int gg_profile_blocks(const gg_ctx *ctx, int64_t *issued, int64_t *dense);
+/* Of the issued blocks since gg_profile(ctx, 1), those that also issued the
+ * two cross products of the split (the others, gg_set_cross_skip, issued
+ * only the main product). */
+int gg_profile_cross(const gg_ctx *ctx, int64_t *cross);
 
 /* Self-tests of the failure paths (no counterpart in the reference, whose
  * Fortran stops the process on an error).  Every device-side wait of the

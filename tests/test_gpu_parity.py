@@ -240,9 +240,18 @@ def test_profile_counts_screened_work(c6h6):
     cube = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
     g.profile(True)
     g.jtensor_batch(cube)
-    issued, dense = g.profile_read()["gemm_blocks"]
+    pr = g.profile_read()
+    issued, dense = pr["gemm_blocks"]
     g.profile(False)
     assert 0 < issued < dense
+    # blocks small for a whole tile issue only the main product
+    assert 0 < pr["cross_blocks"] < issued
+    g.set_cross_skip(False)
+    g.profile(True)
+    g.jtensor_batch(cube)
+    pr = g.profile_read()
+    g.profile(False)
+    assert pr["cross_blocks"] == pr["gemm_blocks"][0] == issued
 
 
 def test_device_and_host_buffers_agree(c6h6):
