@@ -687,15 +687,37 @@ struct gg_ctx {
       }
       e = w64.reserve(static_cast<size_t>(n) * 7 * ld * sizeof(double));
       if (e != cudaSuccess) return cuda_fail(e, "FP64 GEMM scratch");
-      size_t slot = 0;
-      prof_begin(GG_PROF_FP64, st, &slot);
-      gg::launch_basis_fp64(dB, d_pts, n, ld, phi.as<double>(), gx.as<double>(), gy.as<double>(), gz.as<double>(),
+      // the split path's tile screening (slot 0's scratch, once any
+      // contraction still reading it is done): Z order, per-tile active
+      // chunks and K blocks
+      SplitSlot& sl = slot[0];
+      if (sl.used && sl.consumed) {
+        e = cudaStreamWaitEvent(st, sl.consumed, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "FP64 path scratch");
+      }
+      int rc = order_screen(sl, d_pts, n, st, false, false);
+      if (rc) return rc;
+      sl.used = false;
+      if (prof.on) prof.dense_blocks += static_cast<unsigned long long>((n + gg::kBlockM - 1) / gg::kBlockM) *
+                                        dB.nchunk * (dB.kpad / gg::kBlockK);
+      if (prof.on && !sl.tiles)
+        prof_add_blocks(static_cast<unsigned long long>((n + gg::kBlockM - 1) / gg::kBlockM) * dB.nchunk *
+                            (dB.kpad / gg::kBlockK),
+                        st);
+      size_t ps = 0;
+      prof_begin(GG_PROF_FP64, st, &ps);
+      gg::launch_basis_fp64(dB, sl.tp, n, ld, phi.as<double>(), gx.as<double>(), gy.as<double>(), gz.as<double>(),
                             lap.as<double>(), st);
-      gg::launch_dgemm(phi.as<double>(), ld, b_fp64.as<double>(), 7 * ld, w64.as<double>(), 7 * ld, n, 7 * ld, ld,
-                       st);
-      gg::launch_assemble_fp64(dB, d_pts, n, w64.as<double>(), 7 * ld, phi.as<double>(), gx.as<double>(),
-                               gy.as<double>(), gz.as<double>(), lap.as<double>(), ld, flags, out, st);
-      prof_end(st, slot);
+      if (sl.tiles)
+        gg::launch_dgemm_tiles(phi.as<double>(), ld, b_fp64.as<double>(), 7 * ld, w64.as<double>(), 7 * ld, n, nb,
+                               sl.tiles, sl.stride, dB.nchunk, st);
+      else
+        gg::launch_dgemm(phi.as<double>(), ld, b_fp64.as<double>(), 7 * ld, w64.as<double>(), 7 * ld, n, 7 * ld, ld,
+                         st);
+      gg::launch_assemble_fp64(dB, sl.tp, n, w64.as<double>(), 7 * ld, phi.as<double>(), gx.as<double>(),
+                               gy.as<double>(), gz.as<double>(), lap.as<double>(), ld, flags, out, sl.tiles,
+                               sl.stride, sl.perm, st);
+      prof_end(st, ps);
       launches += 3;
       e = cudaGetLastError();
       if (e != cudaSuccess) return cuda_fail(e, "FP64 path launch");
@@ -711,17 +733,13 @@ struct gg_ctx {
     return rc;
   }
 
-  // Ordering, tile screening and basis evaluation of one batch into a slot.
-  int prep_split(SplitSlot& sl, const double* d_pts, int64_t n, cudaStream_t st, bool coherent = false) {
+  // Tile screening of one batch into a slot: order the points along a Z curve
+  // so that tiles are compact, then list the shells each tile can see
+  // (k_tiles.cu).  for_tc: also the heaviest-first tile order of the
+  // contraction's queue and the cross-product mask (split path only).
+  int order_screen(SplitSlot& sl, const double* d_pts, int64_t n, cudaStream_t st, bool coherent, bool for_tc) {
     cudaError_t e;
-    const size_t abytes = static_cast<size_t>(n) * dB.kpad * sizeof(__half);
-    e = sl.a_hi.reserve(abytes);
-    if (e == cudaSuccess) e = sl.a_lo.reserve(abytes);
-    if (e == cudaSuccess) e = sl.inv_row.reserve(static_cast<size_t>(n) * sizeof(float));
-    if (e != cudaSuccess) return cuda_fail(e, "split-path scratch");
     size_t ps = 0;
-    // Tile screening: order the points along a Z curve so that tiles are
-    // compact, then list the shells each tile can see (k_tiles.cu).
     const int stride = gg::tile_stride(dB);
     const bool screen = tile_screening && stride <= 512;
     sl.n = n;
@@ -763,7 +781,7 @@ struct gg_ctx {
       const double* tpts = sort ? sl.pts_sorted.as<double>() : d_pts;
       gg::launch_tile_screen(dB, tpts, n, sl.tile_lists.as<int>(), st);
       // heaviest tiles first (the key/index scratch of the point sort is reused)
-      const bool order = !few;
+      const bool order = for_tc && !few;
       if (order) {
         e = gg::launch_tile_order(sl.tile_lists.as<int>(), ntiles, stride, sl.sort_keys.as<uint32_t>(),
                                   sl.sort_keys2.as<uint32_t>(), sl.sort_idx.as<int>(), sl.tile_ord.as<int>(),
@@ -779,12 +797,27 @@ struct gg_ctx {
       sl.tord = order ? sl.tile_ord.as<int>() : nullptr;
       // every half K block needs the cross products until the basis kernel
       // finds it small for the whole tile
-      if (cross_skip) {
+      if (for_tc && cross_skip) {
         sl.xn = sl.cross_mask.as<unsigned long long>();
         e = cudaMemsetAsync(sl.xn, 0xff, static_cast<size_t>(ntiles) * 2 * sizeof(unsigned long long), st);
         if (e != cudaSuccess) return cuda_fail(e, "cross-product mask");
       }
     }
+    return GG_OK;
+  }
+
+  // Ordering, tile screening and basis evaluation of one batch into a slot.
+  int prep_split(SplitSlot& sl, const double* d_pts, int64_t n, cudaStream_t st, bool coherent = false) {
+    cudaError_t e;
+    const size_t abytes = static_cast<size_t>(n) * dB.kpad * sizeof(__half);
+    e = sl.a_hi.reserve(abytes);
+    if (e == cudaSuccess) e = sl.a_lo.reserve(abytes);
+    if (e == cudaSuccess) e = sl.inv_row.reserve(static_cast<size_t>(n) * sizeof(float));
+    if (e != cudaSuccess) return cuda_fail(e, "split-path scratch");
+    int rc = order_screen(sl, d_pts, n, st, coherent, true);
+    if (rc) return rc;
+    size_t ps = 0;
+    const int stride = sl.stride;
     if (!encode_fp16_2d(&sl.tma_hi, sl.a_hi.p, n, dB.kpad, gg::kBlockM) ||
         !encode_fp16_2d(&sl.tma_lo, sl.a_lo.p, n, dB.kpad, gg::kBlockM) ||
         !encode_fp16_2d(&sl.tms_hi, sl.a_hi.p, n, dB.kpad, gg::kBlockM, true) ||

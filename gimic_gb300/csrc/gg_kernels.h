@@ -42,12 +42,21 @@ void launch_basis_fp64(const DevBasis& B, const double* pts, int64_t npts, int64
 // C[M][N] = A[M][K] B[K][N], fp64, row-major with leading dimensions.
 void launch_dgemm(const double* A, int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc, int64_t M,
                   int64_t N, int64_t K, cudaStream_t st);
+// The same product restricted by tile lists (points in Z order, tiles of 128
+// rows): per tile, the columns of its active 32-function chunks of each of
+// the 7 matrices (M has ldm = 7 ld columns, block m at column m ld), summed
+// over its active 64-function K blocks.  Other columns are not written.
+void launch_dgemm_tiles(const double* phi, int64_t ld, const double* M, int64_t ldm, double* W, int64_t ldw,
+                        int64_t n, int nbf, const int* tiles, int stride, int nchunk, cudaStream_t st);
 
 // Plain FP64 assembly from W = phi^T [D | C_x C_y C_z | P_x P_y P_z]
-// (row stride ldw, block m at column m * nbf) and fp64 basis values.
+// (row stride ldw, block m at column m * nbf) and fp64 basis values.  With
+// tile lists only the active chunks of each point's tile are read, and the
+// outputs of sorted point p go to perm[p] (null: p).
 void launch_assemble_fp64(const DevBasis& B, const double* pts, int64_t npts, const double* W, int64_t ldw,
                           const double* phi, const double* gx, const double* gy, const double* gz, const double* lap,
-                          int64_t ld, Flags fl, Outputs out, cudaStream_t st);
+                          int64_t ld, Flags fl, Outputs out, const int* tiles, int stride, const int* perm,
+                          cudaStream_t st);
 
 // Split-FP16 tensor-core path: TMA maps are opaque 128-byte CUtensorMap blobs.
 struct TcArgs {

@@ -2,6 +2,10 @@
 // warp-per-point assembly of the bilinear forms and their FP64 combination.
 // This path is the accuracy baseline of the split-precision tensor-core path
 // and the "plain FP64 GPU path" the throughput target is measured against.
+// With tile screening it skips the same work as the split path: the points
+// are in the split path's Z order, dgemm_tiles_kernel forms W only for each
+// tile's active column chunks over its active K blocks, and the assembly
+// walks only the active chunks (the skipped basis values are exact zeros).
 #include "gg_combine.cuh"
 #include "gg_kernels.h"
 
@@ -62,8 +66,81 @@ void launch_dgemm(const double* A, int64_t lda, const double* B, int64_t ldb, do
   dgemm_kernel<<<grid, 256, 0, st>>>(A, lda, B, ldb, C, ldc, M, N, K);
 }
 
+namespace {
+constexpr int kQM = 64, kQN = 32;  // one output block: half a tile x the 32 functions of a chunk
+}
+
+// W[p, m ld + c 32 + j] = sum over the tile's active K blocks k of
+// phi[p, k] M[k, m ld + c 32 + j] for every active chunk c of the tile of
+// point p.  Grid (2 ntiles, nchunk, 7): block x is half a tile, y the
+// tile's y-th active chunk (none past its count), z the matrix m.  128
+// threads, 4 x 4 outputs each.  Columns of inactive chunks are not written.
+__global__ void __launch_bounds__(128) dgemm_tiles_kernel(const double* __restrict__ phi, int64_t ld,
+                                                          const double* __restrict__ M, int64_t ldm,
+                                                          double* __restrict__ W, int64_t ldw, int64_t n, int nbf,
+                                                          const int* __restrict__ tiles, int stride, int nchunk) {
+  __shared__ double As[kTK][kQM + 1];
+  __shared__ double Bs[kTK][kQN + 1];
+  const int64_t t = blockIdx.x >> 1;
+  const int* tl = tiles + t * stride;
+  if (static_cast<int>(blockIdx.y) >= tl[0]) return;
+  const int c = tl[2 + blockIdx.y], nk = tl[1];
+  const int* kl = tl + 2 + nchunk;
+  const int64_t r0 = t * 128 + (blockIdx.x & 1) * kQM;
+  const int64_t col0 = static_cast<int64_t>(blockIdx.z) * ld + c * 32;  // column of the block's first function
+  const int f0 = c * 32;
+  const int tx = threadIdx.x % 8, ty = threadIdx.x / 8;  // columns tx + 8 j, rows ty + 16 i
+  double acc[4][4] = {};
+  for (int i = 0; i < nk; ++i) {
+    for (int k0 = kl[i] * 64; k0 < kl[i] * 64 + 64; k0 += kTK) {
+      for (int e = threadIdx.x; e < kQM * kTK; e += 128) {
+        const int mm = e / kTK, kk = e % kTK;
+        const int64_t gr = r0 + mm, gk = k0 + kk;
+        As[kk][mm] = (gr < n && gk < nbf) ? phi[gr * ld + gk] : 0.0;
+      }
+      for (int e = threadIdx.x; e < kQN * kTK; e += 128) {
+        const int kk = e / kQN, nn = e % kQN;
+        const int64_t gk = k0 + kk;
+        Bs[kk][nn] = (gk < nbf && f0 + nn < nbf) ? M[gk * ldm + col0 + nn] : 0.0;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < kTK; ++kk) {
+        double a[4], b[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a[q] = As[kk][ty + 16 * q];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) b[q] = Bs[kk][tx + 8 * q];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q][u] = fma(a[q], b[u], acc[q][u]);
+      }
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t gr = r0 + ty + 16 * q;
+      const int fn = f0 + tx + 8 * u;
+      if (gr < n && fn < nbf) W[gr * ldw + col0 + tx + 8 * u] = acc[q][u];
+    }
+}
+
+void launch_dgemm_tiles(const double* phi, int64_t ld, const double* M, int64_t ldm, double* W, int64_t ldw,
+                        int64_t n, int nbf, const int* tiles, int stride, int nchunk, cudaStream_t st) {
+  if (n <= 0) return;
+  const int64_t ntiles = (n + 127) / 128;
+  dim3 grid(static_cast<unsigned>(2 * ntiles), static_cast<unsigned>(nchunk), 7u);
+  dgemm_tiles_kernel<<<grid, 128, 0, st>>>(phi, ld, M, ldm, W, ldw, n, nbf, tiles, stride, nchunk);
+}
+
 // One warp per point: lanes stride over basis functions and accumulate the
-// kNDots bilinear forms in fp64; lane 0 combines and stores.
+// kNDots bilinear forms in fp64; lane 0 combines and stores.  With tile
+// lists (points in Z order) the lanes walk only the active chunks of the
+// point's tile, and the outputs go to perm[p] (the caller's order).
 __global__ void __launch_bounds__(256) assemble_fp64_kernel(DevBasis Bs, const double* __restrict__ pts, int64_t npts,
                                                             const double* __restrict__ W, int64_t ldw,
                                                             const double* __restrict__ phi,
@@ -71,7 +148,8 @@ __global__ void __launch_bounds__(256) assemble_fp64_kernel(DevBasis Bs, const d
                                                             const double* __restrict__ gy,
                                                             const double* __restrict__ gz,
                                                             const double* __restrict__ lap, int64_t ld, Flags fl,
-                                                            Outputs out) {
+                                                            Outputs out, const int* __restrict__ tiles, int stride,
+                                                            const int* __restrict__ perm) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t p = static_cast<int64_t>(blockIdx.x) * 8 + warp;
   if (p >= npts) return;
@@ -81,7 +159,11 @@ __global__ void __launch_bounds__(256) assemble_fp64_kernel(DevBasis Bs, const d
 #pragma unroll
   for (int i = 0; i < kNDots; ++i) d[i] = 0.0;
   const double* w = W + p * ldw;
-  for (int mu = lane; mu < n; mu += 32) {
+  const int* tl = tiles ? tiles + (p / 128) * stride : nullptr;
+  const int nsteps = tl ? tl[0] : (n + 31) / 32;  // active chunks, or all functions 32 at a time
+  for (int step = 0; step < nsteps; ++step) {
+    const int mu = (tl ? tl[2 + step] * 32 : step * 32) + lane;
+    if (mu >= n) continue;
     const int64_t o = p * ld + mu;
     const double f = phi[o], g[3] = {gx[o], gy[o], gz[o]}, l = lap[o];
     const int a = __ldg(Bs.sh_atom + __ldg(Bs.f_shell + mu));
@@ -117,16 +199,17 @@ __global__ void __launch_bounds__(256) assemble_fp64_kernel(DevBasis Bs, const d
   if (lane == 0) {
     double ct[9], dv[3];
     combine_point(d, r, fl, ct, dv);
-    store_outputs(out, p, ct, d[0], dv);
+    store_outputs(out, perm ? static_cast<int64_t>(perm[p]) : p, ct, d[0], dv);
   }
 }
 
 void launch_assemble_fp64(const DevBasis& B, const double* pts, int64_t npts, const double* W, int64_t ldw,
                           const double* phi, const double* gx, const double* gy, const double* gz, const double* lap,
-                          int64_t ld, Flags fl, Outputs out, cudaStream_t st) {
+                          int64_t ld, Flags fl, Outputs out, const int* tiles, int stride, const int* perm,
+                          cudaStream_t st) {
   if (npts <= 0) return;
   assemble_fp64_kernel<<<static_cast<unsigned>((npts + 7) / 8), 256, 0, st>>>(B, pts, npts, W, ldw, phi, gx, gy, gz,
-                                                                              lap, ld, fl, out);
+                                                                              lap, ld, fl, out, tiles, stride, perm);
 }
 
 }  // namespace gg

@@ -395,3 +395,32 @@ def test_queued_plane_passes_match_blocking_calls(c6h6, c6h6_uhf):
     assert L.gg_plane_integrals_collect(g._h, out.ctypes.data_as(C.POINTER(C.c_double)), None) == 0
     assert np.allclose(out[:, 0], [r["current"][0] for r in want[0]], rtol=1e-12, atol=1e-15)
     assert L.gg_plane_integrals_collect(g._h, out.ctypes.data_as(C.POINTER(C.c_double)), None) != 0
+
+
+def test_fp64_path_screens_tiles_like_the_split_path(c6h6):
+    """The plain FP64 path runs the split path's tile screening (Z order,
+    per-tile active chunks and K blocks; the skipped basis values are exact
+    zeros): with and without it the results agree to FP64 rounding (the
+    GEMM sums in another order), for compact, scattered and far points, and
+    both match the oracle."""
+    mp, xp, _ = c6h6
+    g = api.Gimic(mp, xp, screening=1e-8, precision="fp64")
+    rng = np.random.default_rng(21)
+    ax = np.linspace(-12.0, 12.0, 20)
+    cube = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+    pts = np.vstack([cube, sample_points(g.atoms()[0], 1500, 300, 9.0, seed=22),
+                     rng.uniform(-60.0, 60.0, (300, 3))])
+    pts = pts[rng.permutation(len(pts))]
+    g.profile(True)
+    a = g.jtensor_batch(pts, rho=True, divj=True)
+    issued, dense = g.profile_read()["gemm_blocks"]
+    g.profile(False)
+    assert 0 < issued < dense
+    g.set_tile_screening(False)
+    b = g.jtensor_batch(pts, rho=True, divj=True)
+    for x, y in zip(a, b):
+        assert rel_max_err(x, y) <= 1e-13
+    o = oracle.Oracle(mp, xp, screening=1e-8)
+    sel = rng.choice(len(pts), 600, replace=False)
+    ref, rho_ref = o.jtensor(pts[sel], with_rho=True)
+    assert rel_max_err(a[0][sel], ref) <= TOL_FP64 and rel_max_err(a[1][sel], rho_ref) <= TOL_FP64
