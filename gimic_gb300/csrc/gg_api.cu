@@ -903,10 +903,15 @@ struct gg_ctx {
       if (!*ev && e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     if (e == cudaSuccess && sl.used) e = cudaStreamWaitEvent(aux_stream, sl.consumed, 0);
     if (e == cudaSuccess && input_ready) e = cudaStreamWaitEvent(aux_stream, input_ready, 0);
-    // the preparation may start only once work already queued on `st` that
-    // produced d_pts is done
-    if (e == cudaSuccess) e = cudaEventRecord(sl.prepared, st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux_stream, sl.prepared, 0);
+    // Points on the caller's device memory: the first batch's preparation
+    // starts once the work already queued on `st` (which produced them) is
+    // done; that covers the later batches too, whose preparation may then
+    // overlap the previous batch's contraction.  Points copied in on the
+    // copy stream come with input_ready instead.
+    if (e == cudaSuccess && !input_ready && b == 0) {
+      e = cudaEventRecord(sl.prepared, st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(aux_stream, sl.prepared, 0);
+    }
     if (e != cudaSuccess) return cuda_fail(e, "batch pipeline");
     int rc = prep_split(sl, d_pts, n, aux_stream, coherent);
     if (rc) return rc;
@@ -955,13 +960,28 @@ struct gg_ctx {
                          (!divo || is_device_ptr(divo));
     const int64_t batch = batch_points();
     if (!dev_in && !dev_out) {
-      // the input copy of the first batch and the output copy of the last
-      // overlap nothing: at least four batches (of no fewer than 2^18
-      // points) keep them short (2^21 points at batch 2^20: 1.39e8 -> 1.49e8
-      // points/s end to end)
-      const int64_t quarter = ((n + 3) / 4 + gg::kBlockM - 1) / gg::kBlockM * gg::kBlockM;
-      const int64_t ob = std::min(batch, std::max<int64_t>(int64_t{1} << 18, quarter));
-      if (n > ob) return jtensor_overlapped(p, n, ob, jto, rhoo, divo, st);
+      // The input copy of the first batch and the output copy of the last
+      // overlap nothing, and every batch has a fixed cost: a short first and
+      // last batch (2^18 points, at most a pass) around batches as large as
+      // the pass size.
+      // 2^21 points: four batches of 2^19 gave 2.90e8 points/s end to end
+      // (1.39e8 -> 1.49e8 earlier, against two batches of 2^20).
+      const int64_t edge = std::min<int64_t>(int64_t{1} << 18, batch);
+      if (n > batch || n >= 4 * edge) {
+        std::vector<int64_t> sizes;
+        int64_t rest = n;
+        if (n >= 4 * edge) {
+          sizes.push_back(edge);
+          rest -= 2 * edge;
+        }
+        while (rest > 0) {
+          const int64_t m = std::min(batch, rest);
+          sizes.push_back(m);
+          rest -= m;
+        }
+        if (n >= 4 * edge) sizes.push_back(edge);
+        return jtensor_overlapped(p, sizes, jto, rhoo, divo, st);
+      }
     }
     cudaError_t e;
     int b = 0;
@@ -1019,7 +1039,10 @@ struct gg_ctx {
   // waits for its input copy and for the output copy of batch b - 2, and the
   // output copy waits for the evaluation.
   template <typename T>
-  int jtensor_overlapped(const double* p, int64_t n, int64_t batch, T* jto, T* rhoo, T* divo, cudaStream_t st) {
+  int jtensor_overlapped(const double* p, const std::vector<int64_t>& sizes, T* jto, T* rhoo, T* divo,
+                         cudaStream_t st) {
+    int64_t batch = 0;
+    for (int64_t m : sizes) batch = std::max(batch, m);
     cudaError_t e = cudaSuccess;
     if (!copy_stream) e = cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess && !out_stream) e = cudaStreamCreateWithFlags(&out_stream, cudaStreamNonBlocking);
@@ -1037,9 +1060,9 @@ struct gg_ctx {
       if (e == cudaSuccess && divo) e = sd[i]->reserve(static_cast<size_t>(batch) * 3 * sizeof(T));
     }
     if (e != cudaSuccess) return cuda_fail(e, "overlapped staging");
-    int b = 0;
-    for (int64_t off = 0; off < n; off += batch, ++b) {
-      const int64_t m = std::min(batch, n - off);
+    int64_t off = 0;
+    for (int b = 0; b < static_cast<int>(sizes.size()); off += sizes[b], ++b) {
+      const int64_t m = sizes[b];
       const int s = b & 1;
       if (b >= 2) e = cudaStreamWaitEvent(copy_stream, ev_done[s], 0);  // batch b-2 has read its points
       if (e == cudaSuccess)
