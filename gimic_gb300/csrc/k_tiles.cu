@@ -58,45 +58,54 @@ __global__ void gather_kernel(const double* __restrict__ pts, const int* __restr
 // One block of 128 threads per tile.  tiles[t * stride] = {#chunks, #kblocks,
 // chunk ids..., kblock ids...}.  A shell is out of range for the tile when
 // |R_A - c| - rho > radius (c, rho: centre and radius of the tile's bounding
-// box), which by the triangle inequality excludes it for every point.
+// box), which by the triangle inequality excludes it for every point.  The
+// box is formed in fp32 from coordinates rounded outwards (warp shuffles,
+// then the four warps through shared memory), and rho is widened by far
+// more than the fp32 rounding of the centre, so the test stays conservative
+// without FP64 arithmetic (the FP64 pipe runs at 1/64 of the fp32 rate).
 __global__ void __launch_bounds__(128) tile_screen_kernel(DevBasis B, const double* __restrict__ pts, int64_t n,
                                                           int stride, int* __restrict__ tiles) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* shell_on = smem_raw;                    // nshells
   unsigned char* chunk_on = shell_on + B.nshells;        // nchunk
   unsigned char* kb_on = chunk_on + B.nchunk;            // kpad / 64
-  __shared__ double bmin[3][128], bmax[3][128];
+  __shared__ float wmin[4][3], wmax[4][3];
   const int64_t t = blockIdx.x;
   const int64_t p = t * kBlockM + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nkb = B.kpad / kBlockK;
+  float lo[3], hi[3];
   for (int d = 0; d < 3; ++d) {
     const double v = p < n ? pts[3 * p + d] : pts[3 * (t * kBlockM) + d];
-    bmin[d][threadIdx.x] = v;
-    bmax[d][threadIdx.x] = v;
+    lo[d] = __double2float_rd(v);
+    hi[d] = __double2float_ru(v);
   }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+    }
+  if (lane == 0)
+    for (int d = 0; d < 3; ++d) {
+      wmin[warp][d] = lo[d];
+      wmax[warp][d] = hi[d];
+    }
   for (int i = threadIdx.x; i < B.nchunk; i += 128) chunk_on[i] = 0;
   for (int i = threadIdx.x; i < nkb; i += 128) kb_on[i] = 0;
   __syncthreads();
-  for (int s = 64; s > 0; s >>= 1) {
-    if (threadIdx.x < s)
-      for (int d = 0; d < 3; ++d) {
-        bmin[d][threadIdx.x] = fmin(bmin[d][threadIdx.x], bmin[d][threadIdx.x + s]);
-        bmax[d][threadIdx.x] = fmax(bmax[d][threadIdx.x], bmax[d][threadIdx.x + s]);
-      }
-    __syncthreads();
-  }
-  double c[3], rho2 = 0.0;
+  float cf[3], rho2 = 0.f, cmax = 0.f;
   for (int d = 0; d < 3; ++d) {
-    c[d] = 0.5 * (bmin[d][0] + bmax[d][0]);
-    const double h = 0.5 * (bmax[d][0] - bmin[d][0]);
-    rho2 += h * h;
+    const float a = fminf(fminf(wmin[0][d], wmin[1][d]), fminf(wmin[2][d], wmin[3][d]));
+    const float b = fmaxf(fmaxf(wmax[0][d], wmax[1][d]), fmaxf(wmax[2][d], wmax[3][d]));
+    cf[d] = 0.5f * (a + b);
+    const float h = __fmul_ru(0.5f, __fsub_ru(b, a));
+    rho2 = __fmaf_ru(h, h, rho2);
+    cmax = fmaxf(cmax, fabsf(cf[d]));
   }
-  // fp32 without square roots (the FP64 pipe runs at 1/64 of the fp32
-  // rate): out of range when |R_A - c|^2 > (radius + rho)^2, the right side
-  // widened by 1e-5 relative and 1e-4 Bohr^2, far above the fp32 rounding of
-  // either side, so the test stays conservative
-  const float rhof = static_cast<float>(sqrt(rho2)) * (1.f + 1e-6f);
-  const float cf[3] = {static_cast<float>(c[0]), static_cast<float>(c[1]), static_cast<float>(c[2])};
+  // the centre's fp32 rounding is below 2^-23 |c| per axis; widen by 2^-16
+  const float rhof = __fmul_ru(sqrtf(rho2), 1.f + 1e-6f) + 1.6e-5f * (1.f + cmax);
+  // out of range when |R_A - c|^2 > (radius + rho)^2, the right side
+  // widened by 1e-5 relative and 1e-4 Bohr^2 against the rounding of both
   for (int sh = threadIdx.x; sh < B.nshells; sh += 128) {
     const float4 at = __ldg(B.atom_f4 + __ldg(B.sh_atom + sh));
     const float dx = at.x - cf[0], dy = at.y - cf[1], dz = at.z - cf[2];
@@ -111,15 +120,28 @@ __global__ void __launch_bounds__(128) tile_screen_kernel(DevBasis B, const doub
       kb_on[mu / kBlockK] = 1;
     }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  // the lists, compacted by warp 0 in index order
+  if (warp == 0) {
     int* out = tiles + t * stride;
     int nc = 0, nk = 0;
-    for (int i = 0; i < B.nchunk; ++i)
-      if (chunk_on[i]) out[2 + nc++] = i;
-    for (int i = 0; i < nkb; ++i)
-      if (kb_on[i]) out[2 + B.nchunk + nk++] = i;
-    out[0] = nc;
-    out[1] = nk;
+    for (int i0 = 0; i0 < B.nchunk; i0 += 32) {
+      const int i = i0 + lane;
+      const bool on = i < B.nchunk && chunk_on[i];
+      const unsigned m = __ballot_sync(0xffffffffu, on);
+      if (on) out[2 + nc + __popc(m & ((1u << lane) - 1u))] = i;
+      nc += __popc(m);
+    }
+    for (int i0 = 0; i0 < nkb; i0 += 32) {
+      const int i = i0 + lane;
+      const bool on = i < nkb && kb_on[i];
+      const unsigned m = __ballot_sync(0xffffffffu, on);
+      if (on) out[2 + B.nchunk + nk + __popc(m & ((1u << lane) - 1u))] = i;
+      nk += __popc(m);
+    }
+    if (lane == 0) {
+      out[0] = nc;
+      out[1] = nk;
+    }
   }
 }
 
