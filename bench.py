@@ -506,7 +506,9 @@ def run_proposal(args):
         torch.cuda.synchronize(dev)
         t_adapt += time.perf_counter() - t0
         res0 = P.integrate_adaptive(g, net0, reg, min_inside=0.0)
+        std = P.integrate_uniform(g, reg, 60)
         rows.append({"nbf": nbf, "judge_nAT": judge, "uniform_points": upts, "adaptive_points": res["points"],
+                     "standard_60x60_err_nAT": std - judge,
                      "adaptive_err_nAT": res["current"] - judge, "method": res["method"],
                      "untrained_points": res0["points"], "untrained_err_nAT": res0["current"] - judge})
     u = sum(r["uniform_points"] or 40000 for r in rows)
@@ -524,6 +526,12 @@ def run_proposal(args):
             # fallback (the value above compares with the smallest uniform
             # grid from which every finer one is converged, a stricter base)
             "vs_uniform_judge_grid": 40000.0 * len(rows) / a,
+            # against the standard 60 x 60 Gauss-Lobatto grid (order 10, the
+            # shape of the single-plane benchmark), when it is itself within
+            # 0.01 nA/T of the judge on every plane
+            "vs_standard_60x60_grid": (3600.0 * len(rows) / a
+                                       if max(abs(r["standard_60x60_err_nAT"]) for r in rows) <= 0.01 else None),
+            "standard_60x60_max_err_nAT": max(abs(r["standard_60x60_err_nAT"]) for r in rows),
             "adaptive_max_err_nAT": max(errs), "planes_within_0.01": int(sum(e <= 0.01 for e in errs)),
             "untrained_max_err_nAT": max(abs(r["untrained_err_nAT"]) for r in rows),
             "untrained_planes_within_0.01": int(sum(abs(r["untrained_err_nAT"]) <= 0.01 for r in rows)),
