@@ -265,6 +265,31 @@ def test_device_and_host_buffers_agree(c6h6):
         assert np.array_equal(h, d.cpu().numpy())
 
 
+def test_host_buffers_in_uneven_batches_agree_with_device_buffers(c6h6):
+    """Host buffers of 2^20 + 3,000 points go through the overlapped copy
+    pipeline in batches of 2^18, a full pass and 2^18 points, each prepared
+    while the previous one is contracted; device buffers take one pass.  With
+    the cross-product skip off the results are bit-identical (tiles are
+    independent); with it on they agree to the skip's rounding."""
+    torch = pytest.importorskip("torch")
+    mp, xp, _ = c6h6
+    g = api.Gimic(mp, xp, screening=1e-8)
+    rng = np.random.default_rng(31)
+    pts = np.vstack([rng.uniform(-10.0, 10.0, ((1 << 20) + 2000, 3)),
+                     sample_points(g.atoms()[0], 900, 100, 8.0, seed=32)])
+    dpts = torch.as_tensor(pts, device="cuda")
+    g.set_cross_skip(False)
+    host = g.jtensor_batch(pts, rho=True, divj=True)
+    dev = g.jtensor_batch(dpts, rho=True, divj=True)
+    for h, d in zip(host, dev):
+        assert np.array_equal(h, d.cpu().numpy())
+    g.set_cross_skip(True)
+    host = g.jtensor_batch(pts, rho=True, divj=True)
+    dev = g.jtensor_batch(dpts, rho=True, divj=True)
+    for h, d in zip(host, dev):
+        assert rel_max_err(h, d.cpu().numpy()) <= 1e-7
+
+
 def test_reference_compat_interface(golden_dir):
     """gimic_init / gimic_calc_jtensor / gimic_calc_jvector / mkgausspoints
     (src/libgimic/gimic_interface.h, gausspoints.h) through ctypes."""
