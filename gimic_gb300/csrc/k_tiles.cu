@@ -11,8 +11,9 @@
 //  1. morton_key_kernel + a radix sort order the points along a Z curve so
 //     that 128 consecutive points form a compact tile;
 //  2. gather_kernel copies the points into that order;
-//  3. tile_screen_kernel lists, per tile, the active 32-function column
-//     chunks and 64-function K blocks with a conservative bounding-sphere test.
+//  3. tile_screen_kernel lists, per tile (one warp each), the active
+//     32-function column chunks and 64-function K blocks with a conservative
+//     bounding-sphere test.
 #include <cub/device/device_radix_sort.cuh>
 
 #include "gg_kernels.h"
@@ -55,93 +56,88 @@ __global__ void gather_kernel(const double* __restrict__ pts, const int* __restr
   out[3 * p + 2] = pts[3 * s + 2];
 }
 
-// One block of 128 threads per tile.  tiles[t * stride] = {#chunks, #kblocks,
-// chunk ids..., kblock ids...}.  A shell is out of range for the tile when
-// |R_A - c| - rho > radius (c, rho: centre and radius of the tile's bounding
-// box), which by the triangle inequality excludes it for every point.  The
-// box is formed in fp32 from coordinates rounded outwards (warp shuffles,
-// then the four warps through shared memory), and rho is widened by far
-// more than the fp32 rounding of the centre, so the test stays conservative
-// without FP64 arithmetic (the FP64 pipe runs at 1/64 of the fp32 rate).
+// One warp per tile, four tiles per block of 128 threads.  tiles[t * stride]
+// = {#chunks, #kblocks, chunk ids..., kblock ids...}.  A shell is out of
+// range for the tile when |R_A - c| - rho > radius (c, rho: centre and radius
+// of the tile's bounding box), which by the triangle inequality excludes it
+// for every point.  The box is formed in fp32 from coordinates rounded
+// outwards (warp shuffles), and rho is widened by far more than the fp32
+// rounding of the centre, so the test stays conservative without FP64
+// arithmetic (the FP64 pipe runs at 1/64 of the fp32 rate).  A shell in range
+// marks the chunks and K blocks its functions fall in (the functions of a
+// shell are contiguous).
 __global__ void __launch_bounds__(128) tile_screen_kernel(DevBasis B, const double* __restrict__ pts, int64_t n,
-                                                          int stride, int* __restrict__ tiles) {
+                                                          int64_t ntiles, int stride, int* __restrict__ tiles) {
   extern __shared__ unsigned char smem_raw[];
-  unsigned char* shell_on = smem_raw;                    // nshells
-  unsigned char* chunk_on = shell_on + B.nshells;        // nchunk
-  unsigned char* kb_on = chunk_on + B.nchunk;            // kpad / 64
-  __shared__ float wmin[4][3], wmax[4][3];
-  const int64_t t = blockIdx.x;
-  const int64_t p = t * kBlockM + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nkb = B.kpad / kBlockK;
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * 4 + warp;
+  if (t >= ntiles) return;  // the whole warp
+  unsigned char* chunk_on = smem_raw + warp * (B.nchunk + nkb);  // nchunk
+  unsigned char* kb_on = chunk_on + B.nchunk;                      // kpad / 64
   float lo[3], hi[3];
-  for (int d = 0; d < 3; ++d) {
-    const double v = p < n ? pts[3 * p + d] : pts[3 * (t * kBlockM) + d];
-    lo[d] = __double2float_rd(v);
-    hi[d] = __double2float_ru(v);
+  for (int k = 0; k < kBlockM / 32; ++k) {
+    const int64_t p = t * kBlockM + k * 32 + lane;
+    const int64_t q = p < n ? p : t * kBlockM;  // the tile's first point stands in past the end
+    for (int d = 0; d < 3; ++d) {
+      const double v = pts[3 * q + d];
+      const float l = __double2float_rd(v), h = __double2float_ru(v);
+      lo[d] = k == 0 ? l : fminf(lo[d], l);
+      hi[d] = k == 0 ? h : fmaxf(hi[d], h);
+    }
   }
   for (int o = 16; o > 0; o >>= 1)
     for (int d = 0; d < 3; ++d) {
       lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
       hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
     }
-  if (lane == 0)
-    for (int d = 0; d < 3; ++d) {
-      wmin[warp][d] = lo[d];
-      wmax[warp][d] = hi[d];
-    }
-  for (int i = threadIdx.x; i < B.nchunk; i += 128) chunk_on[i] = 0;
-  for (int i = threadIdx.x; i < nkb; i += 128) kb_on[i] = 0;
-  __syncthreads();
+  for (int i = lane; i < B.nchunk; i += 32) chunk_on[i] = 0;
+  for (int i = lane; i < nkb; i += 32) kb_on[i] = 0;
   float cf[3], rho2 = 0.f, cmax = 0.f;
   for (int d = 0; d < 3; ++d) {
-    const float a = fminf(fminf(wmin[0][d], wmin[1][d]), fminf(wmin[2][d], wmin[3][d]));
-    const float b = fmaxf(fmaxf(wmax[0][d], wmax[1][d]), fmaxf(wmax[2][d], wmax[3][d]));
-    cf[d] = 0.5f * (a + b);
-    const float h = __fmul_ru(0.5f, __fsub_ru(b, a));
+    cf[d] = 0.5f * (lo[d] + hi[d]);
+    const float h = __fmul_ru(0.5f, __fsub_ru(hi[d], lo[d]));
     rho2 = __fmaf_ru(h, h, rho2);
     cmax = fmaxf(cmax, fabsf(cf[d]));
   }
   // the centre's fp32 rounding is below 2^-23 |c| per axis; widen by 2^-16
   const float rhof = __fmul_ru(sqrtf(rho2), 1.f + 1e-6f) + 1.6e-5f * (1.f + cmax);
+  __syncwarp();
   // out of range when |R_A - c|^2 > (radius + rho)^2, the right side
   // widened by 1e-5 relative and 1e-4 Bohr^2 against the rounding of both
-  for (int sh = threadIdx.x; sh < B.nshells; sh += 128) {
+  for (int sh = lane; sh < B.nshells; sh += 32) {
     const float4 at = __ldg(B.atom_f4 + __ldg(B.sh_atom + sh));
     const float dx = at.x - cf[0], dy = at.y - cf[1], dz = at.z - cf[2];
     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float reach = __ldg(B.sh_rad + sh) + rhof;
-    shell_on[sh] = !(d2 > fmaf(reach * reach, 1.00001f, 1e-4f));
+    const int nc = __ldg(B.sh_ncomp + sh);
+    if (nc > 0 && !(d2 > fmaf(reach * reach, 1.00001f, 1e-4f))) {
+      const int f0 = __ldg(B.sh_f0 + sh), f1 = f0 + nc - 1;
+      for (int c = f0 / kChunkF; c <= f1 / kChunkF; ++c) chunk_on[c] = 1;
+      for (int c = f0 / kBlockK; c <= f1 / kBlockK; ++c) kb_on[c] = 1;
+    }
   }
-  __syncthreads();
-  for (int mu = threadIdx.x; mu < B.nbf; mu += 128)
-    if (shell_on[B.f_shell[mu]]) {
-      chunk_on[mu / kChunkF] = 1;
-      kb_on[mu / kBlockK] = 1;
-    }
-  __syncthreads();
-  // the lists, compacted by warp 0 in index order
-  if (warp == 0) {
-    int* out = tiles + t * stride;
-    int nc = 0, nk = 0;
-    for (int i0 = 0; i0 < B.nchunk; i0 += 32) {
-      const int i = i0 + lane;
-      const bool on = i < B.nchunk && chunk_on[i];
-      const unsigned m = __ballot_sync(0xffffffffu, on);
-      if (on) out[2 + nc + __popc(m & ((1u << lane) - 1u))] = i;
-      nc += __popc(m);
-    }
-    for (int i0 = 0; i0 < nkb; i0 += 32) {
-      const int i = i0 + lane;
-      const bool on = i < nkb && kb_on[i];
-      const unsigned m = __ballot_sync(0xffffffffu, on);
-      if (on) out[2 + B.nchunk + nk + __popc(m & ((1u << lane) - 1u))] = i;
-      nk += __popc(m);
-    }
-    if (lane == 0) {
-      out[0] = nc;
-      out[1] = nk;
-    }
+  __syncwarp();
+  // the lists, compacted in index order
+  int* out = tiles + t * stride;
+  int nc = 0, nk = 0;
+  for (int i0 = 0; i0 < B.nchunk; i0 += 32) {
+    const int i = i0 + lane;
+    const bool on = i < B.nchunk && chunk_on[i];
+    const unsigned m = __ballot_sync(0xffffffffu, on);
+    if (on) out[2 + nc + __popc(m & ((1u << lane) - 1u))] = i;
+    nc += __popc(m);
+  }
+  for (int i0 = 0; i0 < nkb; i0 += 32) {
+    const int i = i0 + lane;
+    const bool on = i < nkb && kb_on[i];
+    const unsigned m = __ballot_sync(0xffffffffu, on);
+    if (on) out[2 + B.nchunk + nk + __popc(m & ((1u << lane) - 1u))] = i;
+    nk += __popc(m);
+  }
+  if (lane == 0) {
+    out[0] = nc;
+    out[1] = nk;
   }
 }
 
@@ -231,8 +227,10 @@ cudaError_t launch_spatial_order(const double* pts, int64_t n, const double lo[3
 
 void launch_tile_screen(const DevBasis& B, const double* pts_sorted, int64_t n, int* tiles, cudaStream_t st) {
   const int64_t ntiles = (n + kBlockM - 1) / kBlockM;
-  const size_t smem = static_cast<size_t>(B.nshells) + B.nchunk + B.kpad / kBlockK;
-  tile_screen_kernel<<<static_cast<unsigned>(ntiles), 128, smem, st>>>(B, pts_sorted, n, tile_stride(B), tiles);
+  if (ntiles <= 0) return;
+  const size_t smem = 4 * static_cast<size_t>(B.nchunk + B.kpad / kBlockK);
+  const unsigned blocks = static_cast<unsigned>((ntiles + 3) / 4);
+  tile_screen_kernel<<<blocks, 128, smem, st>>>(B, pts_sorted, n, ntiles, tile_stride(B), tiles);
 }
 
 }  // namespace gg
