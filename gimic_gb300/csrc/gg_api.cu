@@ -354,6 +354,12 @@ struct gg_ctx {
       return make_float2(h, static_cast<float>(x - static_cast<double>(h)));
     };
     for (double v : axyz) atom_df.push_back(split(v));
+    // the same on the 2^-12 grid (grid_split in gg_device.cuh)
+    std::vector<float2> atom_g;
+    for (double v : axyz) {
+      const float g = static_cast<float>(std::nearbyint(v * 4096.0) / 4096.0);
+      atom_g.push_back(make_float2(g, static_cast<float>(v - static_cast<double>(g))));
+    }
     for (int mu = 0; mu < b.nbf; ++mu) {
       int e[3];
       gg::component_exponents(b.shells[f_shell[mu]].l, b.func_comp[mu], b.turbomole, e);
@@ -461,6 +467,7 @@ struct gg_ctx {
     if (e == cudaSuccess) e = upload(sh_rad2, &d.sh_rad2);
     if (e == cudaSuccess) e = upload(sh_rad2_df, &d.sh_rad2_df);
     if (e == cudaSuccess) e = upload(atom_df, &d.atom_df);
+    if (e == cudaSuccess) e = upload(atom_g, &d.atom_g);
     if (e == cudaSuccess) e = upload(p_xp, &d.p_xp);
     if (e == cudaSuccess) e = upload(p_xplo, &d.p_xplo);
     if (e == cudaSuccess) e = upload(p_cc, &d.p_cc);

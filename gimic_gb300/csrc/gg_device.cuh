@@ -29,6 +29,7 @@ struct DevBasis {
   const double* sh_rad2;   // squared screening radius
   const float2* sh_rad2_df;  // the same as a double-float (hi, lo)
   const float2* atom_df;     // natoms x 3 coordinates as double-floats (hi, lo)
+  const float2* atom_g;      // natoms x 3 coordinates split on the 2^-12 grid (grid_split)
   const float* p_xp;       // primitive exponents (fp32, rounded)
   const float* p_xplo;     // exponent residuals: p_xpd - p_xp (fp32)
   const float* p_cc;       // normalised contraction coefficients (fp32)
@@ -177,30 +178,37 @@ __device__ __forceinline__ double df_to_double(DFloat a) {
 // a <= b for normalised double-floats
 __device__ __forceinline__ bool df_le(DFloat a, float2 b) { return a.h < b.x || (a.h == b.x && a.l <= b.y); }
 
-// The same with the atom table read through a generic pointer (shared or
-// global memory).
-__device__ __forceinline__ DFloat atom_offset_t(const DFloat r[3], const float2* atom_df, int a, float s[3]) {
-  DFloat d2{0.f, 0.f};
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const DFloat dc = df_sub(r[c], atom_df[3 * a + c]);
-    s[c] = dc.h;
-    d2 = df_add(d2, df_sqr(dc));
-  }
-  return d2;
+// Grid split of a coordinate: x = g + l with g a multiple of 2^-12 and
+// |l| <= 2^-13 (for |x| < 2^12 Bohr; beyond, g is x rounded to fp32).  Two
+// grid-split coordinates below 2^12 in magnitude differ by an exact fp32
+// difference of the g parts plus a small one of the l parts, which makes
+// r - R_A cheap to form without losing digits.
+constexpr float kGridScale = 4096.f;
+__device__ __forceinline__ float2 grid_split(DFloat x) {
+  const float g = __fmul_rn(rintf(__fmul_rn(x.h, kGridScale)), 1.f / kGridScale);  // exact scalings
+  return make_float2(g, __fadd_rn(__fsub_rn(x.h, g), x.l));                       // x.h - g is exact
 }
 
-// Position of a point relative to atom a and its squared distance, from the
-// point as double-floats and the atom table.
-__device__ __forceinline__ DFloat atom_offset(const DFloat r[3], const float2* __restrict__ atom_df, int a, float s[3]) {
-  DFloat d2{0.f, 0.f};
+// Position of a point relative to atom a (fp32, rounded once) and its
+// squared distance as a double-float, from the grid splits of the point
+// (rg) and of the atom table.  d = dh + dl with dh = g_r - g_A exact and
+// |dl| <= 2^-12; d^2 = dh^2 (exact as p + e) + dl (2 dh + dl).  The relative
+// error of the result is about 2^-24 |dl| / |d| (2^-36 once |dh| >= 1).
+__device__ __forceinline__ DFloat atom_offset_g(const float2 rg[3], const float2* atom_g, int a, float s[3]) {
+  float dh[3], p[3], lo = 0.f;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const DFloat dc = df_sub(r[c], __ldg(atom_df + 3 * a + c));
-    s[c] = dc.h;
-    d2 = df_add(d2, df_sqr(dc));
+    const float2 A = atom_g[3 * a + c];
+    dh[c] = __fsub_rn(rg[c].x, A.x);
+    const float dl = __fsub_rn(rg[c].y, A.y);
+    s[c] = __fadd_rn(dh[c], dl);
+    p[c] = __fmul_rn(dh[c], dh[c]);
+    lo = __fadd_rn(lo, fmaf(dh[c], dh[c], -p[c]));
+    lo = fmaf(dl, fmaf(2.f, dh[c], dl), lo);
   }
-  return d2;
+  const DFloat a1 = two_sum(p[0], p[1]);
+  const DFloat a2 = two_sum(a1.h, p[2]);
+  return two_sum(a2.h, __fadd_rn(__fadd_rn(a1.l, a2.l), lo));
 }
 
 __device__ __forceinline__ int ipow_exp(int packed, int axis) { return (packed >> (4 * axis)) & 15; }

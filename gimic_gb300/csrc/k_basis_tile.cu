@@ -94,7 +94,7 @@ struct AtomGeom {
 // the monomial from the packed exponents.  Both give x^i y^j z^k f1 with the
 // same operations in the same order.
 template <int kStep, typename Put>
-__device__ __forceinline__ void stage_shells(const DevBasis& B, const DFloat r[3], float scale, int lo, int hi,
+__device__ __forceinline__ void stage_shells(const DevBasis& B, const float2 rg[3], float scale, int lo, int hi,
                                              int first, AtomGeom& g, Put&& put) {
   for (int sh = __ldg(B.f_shell + lo) + first; sh < B.nshells; sh += kStep) {
     const int4 pk = __ldg(B.sh_pack + sh);  // atom, first function, ncomp | npf << 8 | l << 16 | std << 24, first primitive
@@ -104,7 +104,7 @@ __device__ __forceinline__ void stage_shells(const DevBasis& B, const DFloat r[3
     if (pk.x != g.atom) {
       g.atom = pk.x;
       float s3[3];
-      g.d2 = atom_offset(r, B.atom_df, pk.x, s3);
+      g.d2 = atom_offset_g(rg, B.atom_g, pk.x, s3);
       g.cp = cart_pow(s3[0], s3[1], s3[2]);
     }
     float f1 = 0.f;
@@ -197,6 +197,7 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
     prefetch_l1(B.sh_rad2_df, B.nshells * sizeof(float2));
     prefetch_l1(B.p_pack, B.nprim * sizeof(float4));
     prefetch_l1(B.atom_df, B.natoms * 3 * sizeof(float2));
+    prefetch_l1(B.atom_g, B.natoms * 3 * sizeof(float2));
     prefetch_l1(B.f_ijk, B.nbf * sizeof(int));
     prefetch_l1(B.f_shell, B.nbf * sizeof(int));
   }
@@ -258,12 +259,13 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
     *reinterpret_cast<__half*>(base + kStageBytes + o) = l;
   };
   AtomGeom g;
+  const float2 rg[3] = {grid_split(r[0]), grid_split(r[1]), grid_split(r[2])};
   for (int hb = hb0; hb < hb1; ++hb) {
     if (!((kb_on >> (hb >> 1)) & 1ull)) continue;  // inactive for the tile: never read
     const int lo = hb * kHalfK, hi = min(lo + kHalfK, B.nbf);
     if (sub == 0)
       for (int mu = max(lo, B.nbf); mu < lo + kHalfK; ++mu) put(mu - lo, 0.f, true);  // padding columns
-    if (lo < B.nbf) stage_shells<kSubs>(B, r, scale, lo, hi, sub, g, put);
+    if (lo < B.nbf) stage_shells<kSubs>(B, rg, scale, lo, hi, sub, g, put);
     // the half block is complete: write it to HBM, then reuse the buffer;
     // a half block small for every point of the tile needs no cross products
     fence_proxy_async();

@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       e.shp = J.B.sh_pack;
       e.shr = J.B.sh_rad2_df;
       e.prm = J.B.p_pack;
-      e.atm = J.B.atom_df;
+      e.atm = J.B.atom_g;
       e.icol = J.inv_col;
       e.inv_row = J.inv_row;
       e.pts = J.pts;
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       e.shp = Bs.sh_pack;
       e.shr = Bs.sh_rad2_df;
       e.prm = Bs.p_pack;
-      e.atm = Bs.atom_df;
+      e.atm = Bs.atom_g;
       e.icol = inv_col;
       e.inv_row = inv_row;
       e.pts = pts;
@@ -478,6 +478,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         r[2] = ev.pts[3 * p + 2];
       }
       const DFloat rdf[3] = {df_split(r[0]), df_split(r[1]), df_split(r[2])};
+      const float2 rg[3] = {grid_split(rdf[0]), grid_split(rdf[1]), grid_split(rdf[2])};
       // fp32 running sums over the tile's functions in this group (a
       // compensated sum across chunks changed no digit of the error against
       // the FP64 oracle: it is set by the fp16 products)
@@ -594,7 +595,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               fold_atom();
               cur_atom = a;
               float s3[3];
-              d2a = atom_offset_t(rdf, ev.atm, a, s3);
+              d2a = atom_offset_g(rg, ev.atm, a, s3);
               sx = s3[0];
               sy = s3[1];
               sz = s3[2];
@@ -774,7 +775,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     prefetch_l1(PB.sh_pack, PB.nshells * sizeof(int4), t, 64);
     prefetch_l1(PB.sh_rad2_df, PB.nshells * sizeof(float2), t, 64);
     prefetch_l1(PB.p_pack, PB.nprim * sizeof(float4), t, 64);
-    prefetch_l1(PB.atom_df, PB.natoms * 3 * sizeof(float2), t, 64);
+    prefetch_l1(PB.atom_g, PB.natoms * 3 * sizeof(float2), t, 64);
   }
   tc_fence_before();
   __syncthreads();
