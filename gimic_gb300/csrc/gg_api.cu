@@ -142,7 +142,7 @@ struct gg_ctx {
   // scratch
   DevBuf pts, jt, rho, divt, jv;
   DevBuf tile_ctr;  // tile queue counter of the contraction kernel
-  DevBuf tc_part, tc_done;  // partial sums and counters of the chunk split
+  DevBuf tc_part;  // partial sums of the chunk split
   // Per-batch scratch of the split path.  Two slots let the ordering,
   // screening and basis evaluation of batch b+1 (on the auxiliary stream) run
   // while the contraction of batch b runs on the caller's stream.
@@ -254,7 +254,7 @@ struct gg_ctx {
   std::vector<DevBuf*> buffers() {
     std::vector<DevBuf*> v = {&b_fp64, &b_hi, &b_lo, &inv_col, &pts, &jt, &rho, &divt, &jv, &phi, &gx, &gy, &gz,
                               &lap, &w64, &plane_rows, &plane_out, &pts2, &jt2, &rho2, &divt2, &tile_ctr, &diag,
-                              &tc_part, &tc_done, &mjobs};
+                              &tc_part, &mjobs};
     for (SplitSlot& sl : slot)
       for (DevBuf* b : {&sl.a_hi, &sl.a_lo, &sl.inv_row, &sl.sort_keys, &sl.sort_keys2, &sl.sort_idx, &sl.sort_perm,
                         &sl.sort_temp, &sl.pts_sorted, &sl.tile_lists, &sl.tile_ord, &sl.cross_mask})
@@ -786,7 +786,10 @@ struct gg_ctx {
         launches += 3;
       }
       const double* tpts = sort ? sl.pts_sorted.as<double>() : d_pts;
-      gg::launch_tile_screen(dB, tpts, n, sl.tile_lists.as<int>(), st);
+      // every half K block needs the cross products until the basis kernel
+      // finds it small for the whole tile (the screen sets the mask)
+      sl.xn = for_tc && cross_skip ? sl.cross_mask.as<unsigned long long>() : nullptr;
+      gg::launch_tile_screen(dB, tpts, n, sl.tile_lists.as<int>(), sl.xn, st);
       // heaviest tiles first (the key/index scratch of the point sort is reused)
       const bool order = for_tc && !few;
       if (order) {
@@ -802,13 +805,6 @@ struct gg_ctx {
       sl.tiles = sl.tile_lists.as<int>();
       sl.perm = sort ? sl.sort_perm.as<int>() : nullptr;
       sl.tord = order ? sl.tile_ord.as<int>() : nullptr;
-      // every half K block needs the cross products until the basis kernel
-      // finds it small for the whole tile
-      if (for_tc && cross_skip) {
-        sl.xn = sl.cross_mask.as<unsigned long long>();
-        e = cudaMemsetAsync(sl.xn, 0xff, static_cast<size_t>(ntiles) * 2 * sizeof(unsigned long long), st);
-        if (e != cudaSuccess) return cuda_fail(e, "cross-product mask");
-      }
     }
     return GG_OK;
   }
@@ -859,8 +855,13 @@ struct gg_ctx {
       prof.dense_blocks += blocks;
       if (!sl.tiles && prof.d_blocks) prof_add_blocks(blocks, st);
     }
-    cudaError_t e = tile_ctr.reserve(sizeof(int));
-    if (e == cudaSuccess) e = cudaMemsetAsync(tile_ctr.p, 0, sizeof(int), st);
+    const int64_t ntiles = (sl.n + gg::kBlockM - 1) / gg::kBlockM;
+    const bool split = nsm > 0 && ntiles <= nsm && dB.nchunk > 1 && ntiles * dB.nchunk <= 8192;
+    // the tile queue's counter and, for a chunk split, the step count of
+    // every quarter tile after it: one buffer, one memset
+    const size_t cbytes = sizeof(unsigned) * static_cast<size_t>(1 + (split ? ntiles * 4 : 0));
+    cudaError_t e = tile_ctr.reserve(cbytes);
+    if (e == cudaSuccess) e = cudaMemsetAsync(tile_ctr.p, 0, cbytes, st);
     if (e != cudaSuccess) return cuda_fail(e, "tile queue");
     ta.tile_counter = tile_ctr.as<int>();
     // A short pass (no more tiles than SMs) would leave most SMs idle while
@@ -868,15 +869,12 @@ struct gg_ctx {
     // tile's chunks over steps of their own, whose partial sums the last
     // step of each quarter tile adds in chunk order.  All short passes thus
     // give the same results point by point, whatever their size.
-    const int64_t ntiles = (sl.n + gg::kBlockM - 1) / gg::kBlockM;
-    if (nsm > 0 && ntiles <= nsm && dB.nchunk > 1 && ntiles * dB.nchunk <= 8192) {
+    if (split) {
       ta.csplit = dB.nchunk;
       e = tc_part.reserve(static_cast<size_t>(ntiles) * dB.nchunk * gg::kNDots * gg::kBlockM * sizeof(float2));
-      if (e == cudaSuccess) e = tc_done.reserve(static_cast<size_t>(ntiles) * 4 * sizeof(unsigned));
-      if (e == cudaSuccess) e = cudaMemsetAsync(tc_done.p, 0, static_cast<size_t>(ntiles) * 4 * sizeof(unsigned), st);
       if (e != cudaSuccess) return cuda_fail(e, "chunk-split scratch");
       ta.part = tc_part.as<float2>();
-      ta.tile_done = tc_done.as<unsigned>();
+      ta.tile_done = tile_ctr.as<unsigned>() + 1;
     }
     size_t ps = 0;
     prof_begin(GG_PROF_TC, st, &ps);
@@ -1471,9 +1469,8 @@ static int plane_points_launch(gg_ctx* ctx, const PlanePass& P, cudaStream_t st)
   const int* drp = reinterpret_cast<const int*>(ab + P.o_rp);
   unsigned* ddone = reinterpret_cast<unsigned*>(ab + P.o_done);
   cudaError_t e = cudaMemcpyAsync(ab, hb, P.upload, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ddone, 0, static_cast<size_t>(P.nplanes) * sizeof(unsigned), st);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "copying plane axes");
-  gg::launch_plane_points(dx, ddesc, drp, P.nrows, ctx->pts.as<double>(), st);
+  gg::launch_plane_points(dx, ddesc, drp, P.nrows, ctx->pts.as<double>(), ddone, P.nplanes, st);
   ctx->launches += 1;
   return GG_OK;
 }

@@ -118,7 +118,10 @@ size_t sort_temp_bytes(int64_t n);
 cudaError_t launch_spatial_order(const double* pts, int64_t n, const double lo[3], double cell, uint32_t* keys,
                                  uint32_t* keys_sorted, int* idx, int* perm, void* temp, size_t temp_bytes,
                                  double* pts_sorted, cudaStream_t st);
-void launch_tile_screen(const DevBasis& B, const double* pts_sorted, int64_t n, int* tiles, cudaStream_t st);
+// xneed (may be null): the cross-product mask of the tiles (TcArgs::xneed),
+// set to all ones here for the basis kernel to clear.
+void launch_tile_screen(const DevBasis& B, const double* pts_sorted, int64_t n, int* tiles, unsigned long long* xneed,
+                        cudaStream_t st);
 void launch_tile_work(const int* tiles, int64_t ntiles, int stride, unsigned long long* acc, cudaStream_t st);
 // acc += the blocks (chunks x K blocks) of the tiles whose K block needs the
 // cross products (xneed as TcArgs::xneed; profiling)
@@ -151,9 +154,10 @@ struct PlaneDesc {
 };
 // Points of every plane, r(i,j,k) = origin + x1_i basv1 + x2_j basv2 +
 // x3_k basv3 in the host's operation order (no fused multiply-adds), one
-// block per plane row.
+// block per plane row.  Block 0 also zeroes the nplanes counters `done` of
+// the plane reduction that follows on the same stream.
 void launch_plane_points(const double* xs, const PlaneDesc* planes, const int* row_plane, int64_t nrows, double* pts,
-                         cudaStream_t st);
+                         unsigned* done, int nplanes, cudaStream_t st);
 // field: the magnetic field vector (3 doubles) in device memory; done:
 // nplanes counters, zero at launch (and zero again when it ends).
 void launch_plane_batch(const double* jt, const double* pts, const double* w, const PlaneDesc* planes, int nplanes,

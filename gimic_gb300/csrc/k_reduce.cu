@@ -123,8 +123,11 @@ __global__ void __launch_bounds__(kRowThreads) plane_batch_kernel(const double* 
 __global__ void __launch_bounds__(kRowThreads) plane_points_kernel(const double* __restrict__ xs,
                                                                    const PlaneDesc* __restrict__ planes,
                                                                    const int* __restrict__ row_plane,
-                                                                   double* __restrict__ pts) {
+                                                                   double* __restrict__ pts, unsigned* done,
+                                                                   int nplanes) {
   const int64_t row = blockIdx.x;
+  if (row == 0)
+    for (int q = threadIdx.x; q < nplanes; q += kRowThreads) done[q] = 0;
   const PlaneDesc& pl = planes[row_plane[row]];
   const int64_t r = row - pl.row_off;
   const int j = static_cast<int>(r % pl.p2), k = static_cast<int>(r / pl.p2);
@@ -140,9 +143,10 @@ __global__ void __launch_bounds__(kRowThreads) plane_points_kernel(const double*
 }
 
 void launch_plane_points(const double* xs, const PlaneDesc* planes, const int* row_plane, int64_t nrows, double* pts,
-                         cudaStream_t st) {
+                         unsigned* done, int nplanes, cudaStream_t st) {
   if (nrows <= 0) return;
-  plane_points_kernel<<<static_cast<unsigned>(nrows), kRowThreads, 0, st>>>(xs, planes, row_plane, pts);
+  plane_points_kernel<<<static_cast<unsigned>(nrows), kRowThreads, 0, st>>>(xs, planes, row_plane, pts, done,
+                                                                             nplanes);
 }
 
 void launch_plane_batch(const double* jt, const double* pts, const double* w, const PlaneDesc* planes, int nplanes,

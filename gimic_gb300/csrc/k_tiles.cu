@@ -67,12 +67,14 @@ __global__ void gather_kernel(const double* __restrict__ pts, const int* __restr
 // marks the chunks and K blocks its functions fall in (the functions of a
 // shell are contiguous).
 __global__ void __launch_bounds__(128) tile_screen_kernel(DevBasis B, const double* __restrict__ pts, int64_t n,
-                                                          int64_t ntiles, int stride, int* __restrict__ tiles) {
+                                                          int64_t ntiles, int stride, int* __restrict__ tiles,
+                                                          unsigned long long* __restrict__ xneed) {
   extern __shared__ unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nkb = B.kpad / kBlockK;
   const int64_t t = static_cast<int64_t>(blockIdx.x) * 4 + warp;
   if (t >= ntiles) return;  // the whole warp
+  if (xneed && lane < 2) xneed[2 * t + lane] = ~0ull;  // every half K block needs cross products until shown small
   unsigned char* chunk_on = smem_raw + warp * (B.nchunk + nkb);  // nchunk
   unsigned char* kb_on = chunk_on + B.nchunk;                      // kpad / 64
   float lo[3], hi[3];
@@ -225,12 +227,13 @@ cudaError_t launch_spatial_order(const double* pts, int64_t n, const double lo[3
   return cudaGetLastError();
 }
 
-void launch_tile_screen(const DevBasis& B, const double* pts_sorted, int64_t n, int* tiles, cudaStream_t st) {
+void launch_tile_screen(const DevBasis& B, const double* pts_sorted, int64_t n, int* tiles, unsigned long long* xneed,
+                        cudaStream_t st) {
   const int64_t ntiles = (n + kBlockM - 1) / kBlockM;
   if (ntiles <= 0) return;
   const size_t smem = 4 * static_cast<size_t>(B.nchunk + B.kpad / kBlockK);
   const unsigned blocks = static_cast<unsigned>((ntiles + 3) / 4);
-  tile_screen_kernel<<<blocks, 128, smem, st>>>(B, pts_sorted, n, ntiles, tile_stride(B), tiles);
+  tile_screen_kernel<<<blocks, 128, smem, st>>>(B, pts_sorted, n, ntiles, tile_stride(B), tiles, xneed);
 }
 
 }  // namespace gg
