@@ -3,8 +3,8 @@
 // (integrate_modulus) and :414-511 (integrate_acid) with the ACID density of
 // src/libgimic/acid.f90:11-43, for a batch of planes at once (bond-current
 // profile scans).  Row partial sums (over i) are formed by one block per row
-// with a fixed reduction tree and then summed over rows in order, all in
-// fp64, so the result is deterministic.
+// with a fixed reduction tree and then summed over the rows with a fixed
+// split and tree, all in fp64, so the result is deterministic.
 #include "gg_kernels.h"
 
 namespace gg {
@@ -21,8 +21,16 @@ __device__ __forceinline__ void point_terms(const double* t, const double* rr, c
   double jv[3];
   for (int m = 0; m < 3; ++m) jv[m] = t[m] * bb[0] + t[m + 3] * bb[1] + t[m + 6] * bb[2];
   const double dx = rr[0] - center[0], dy = rr[1] - center[1], dz = rr[2] - center[2];
-  const double dist = sqrt(dx * dx + dy * dy + dz * dz);
-  const bool inside = !(dist > radius);
+  const double d2 = dx * dx + dy * dy + dz * dz;
+  // !(|d| > radius) as the reference tests it; the square root only near
+  // the boundary (and for a negative or NaN radius or distance)
+  bool inside;
+  if (radius >= 0.0 && d2 < radius * radius * (1.0 - 1e-12))
+    inside = true;
+  else if (radius >= 0.0 && d2 > radius * radius * (1.0 + 1e-12))
+    inside = false;
+  else
+    inside = !(sqrt(d2) > radius);
   const double w = inside ? wi : 0.0;
   const double jn = normal[0] * jv[0] + normal[1] * jv[1] + normal[2] * jv[2];
   // current: jp = (n . j) w
@@ -62,8 +70,9 @@ __device__ __forceinline__ void block_reduce_store(double acc[kQ], double wj, do
 
 // One block per row of one plane of a batch: the row's sums over i (fixed
 // tree), times w_j, to row_out.  The block that finishes a plane's last row
-// (counted in done[plane], zero at launch) then sums the plane's rows in
-// order, s2 over j and s3 += w_k s2 over k (integral.f90:107-165), so the
+// (counted in done[plane], zero at launch) then sums the plane's rows, each
+// times w_k (the reference's s3 += w_k s2 over k of s2 over j,
+// integral.f90:107-165, as one sum), with a fixed split and tree, so the
 // plane's result does not depend on which block came last.
 __global__ void __launch_bounds__(kRowThreads) plane_batch_kernel(const double* __restrict__ jt,
                                                                   const double* __restrict__ pts,
@@ -92,31 +101,18 @@ __global__ void __launch_bounds__(kRowThreads) plane_batch_kernel(const double* 
   __syncthreads();
   if (!last) return;
   __threadfence();
-  // rows of the plane in order, staged through shared memory in chunks
-  __shared__ double chunk[kRowThreads][kQ];
-  double s2 = 0.0, s3 = 0.0;
-  int jj = 0, kk = 0;  // row j within the rows of k
+  // the plane's sums: sum over k of w_k times the sum over j of its rows,
+  // taken as one sum over the rows, each times the w_k of its k; thread t
+  // adds rows t, t + 128, ... in order, then the fixed block tree
   const double* wk = w + pl.w_off + pl.p1 + pl.p2;
-  for (int64_t base = 0; base < nr; base += kRowThreads) {
-    const int64_t rr = base + threadIdx.x;
-    if (rr < nr)
-      for (int c = 0; c < kQ; ++c) chunk[threadIdx.x][c] = __ldcg(row_out + (pl.row_off + rr) * kQ + c);
-    __syncthreads();
-    if (threadIdx.x < kQ) {
-      const int n = static_cast<int>(nr - base < kRowThreads ? nr - base : kRowThreads);
-      for (int t = 0; t < n; ++t) {
-        s2 += chunk[t][threadIdx.x];
-        if (++jj == pl.p2) {  // the rows of k are done
-          s3 = s3 + wk[kk] * s2;
-          s2 = 0.0;
-          jj = 0;
-          ++kk;
-        }
-      }
-    }
-    __syncthreads();
+  double s[kQ] = {0, 0, 0, 0, 0, 0, 0};
+  for (int64_t rr = threadIdx.x; rr < nr; rr += kRowThreads) {
+    const double f = wk[rr / pl.p2];
+    const double* src = row_out + (pl.row_off + rr) * kQ;
+#pragma unroll
+    for (int c = 0; c < kQ; ++c) s[c] += f * __ldcg(src + c);
   }
-  if (threadIdx.x < kQ) out[q * kQ + threadIdx.x] = s3;
+  block_reduce_store(s, 1.0, out + q * kQ);
   if (threadIdx.x == 0) done[q] = 0;
 }
 
