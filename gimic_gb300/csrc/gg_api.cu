@@ -156,6 +156,7 @@ struct gg_ctx {
     const int* perm = nullptr;
     const int* tord = nullptr;
     unsigned long long* xn = nullptr;  // per tile: half K blocks that need the cross products
+    bool screen_in_basis = false;       // the lists are written by the short basis kernel
     int stride = 0;
     int64_t n = 0;
     bool used = false;  // a contraction has been enqueued on this slot
@@ -756,6 +757,7 @@ struct gg_ctx {
     sl.perm = nullptr;
     sl.tord = nullptr;
     sl.xn = nullptr;
+    sl.screen_in_basis = false;
     if (screen) {
       const int64_t ntiles = (n + gg::kBlockM - 1) / gg::kBlockM;
       const size_t tb = std::max(gg::sort_temp_bytes(n), gg::tile_order_temp_bytes(ntiles));
@@ -789,7 +791,10 @@ struct gg_ctx {
       // every half K block needs the cross products until the basis kernel
       // finds it small for the whole tile (the screen sets the mask)
       sl.xn = for_tc && cross_skip ? sl.cross_mask.as<unsigned long long>() : nullptr;
-      gg::launch_tile_screen(dB, tpts, n, sl.tile_lists.as<int>(), sl.xn, st);
+      // a short split pass (every tile an SM of its own) screens its tiles
+      // in the basis kernel, one launch fewer on its latency chain
+      sl.screen_in_basis = for_tc && few && dB.nchunk <= 4096 / gg::kChunkF;
+      if (!sl.screen_in_basis) gg::launch_tile_screen(dB, tpts, n, sl.tile_lists.as<int>(), sl.xn, st);
       // heaviest tiles first (the key/index scratch of the point sort is reused)
       const bool order = for_tc && !few;
       if (order) {
@@ -799,8 +804,9 @@ struct gg_ctx {
         if (e != cudaSuccess) return cuda_fail(e, "tile ordering");
       }
       prof_end(st, ps);
-      if (prof.on && prof.d_blocks) gg::launch_tile_work(sl.tile_lists.as<int>(), ntiles, stride, prof.d_blocks, st);
-      launches += order ? 3 : 1;
+      if (prof.on && prof.d_blocks && !sl.screen_in_basis)
+        gg::launch_tile_work(sl.tile_lists.as<int>(), ntiles, stride, prof.d_blocks, st);
+      launches += (order ? 3 : 1) - (sl.screen_in_basis ? 1 : 0);
       sl.tp = tpts;
       sl.tiles = sl.tile_lists.as<int>();
       sl.perm = sort ? sl.sort_perm.as<int>() : nullptr;
@@ -828,11 +834,12 @@ struct gg_ctx {
       return fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
     prof_begin(GG_PROF_BASIS, st, &ps);
     e = gg::launch_basis_tile(dB, &sl.tms_hi, &sl.tms_lo, sl.tp, n, sl.tiles, stride, sl.inv_row.as<float>(), sl.xn,
-                              st);
+                              sl.screen_in_basis ? sl.tile_lists.as<int>() : nullptr, st);
     prof_end(st, ps);
     if (e != cudaSuccess) return cuda_fail(e, "basis kernel launch");
     if (prof.on && prof.d_blocks && sl.tiles) {  // blocks that keep their cross products
       const int64_t ntiles = (n + gg::kBlockM - 1) / gg::kBlockM;
+      if (sl.screen_in_basis) gg::launch_tile_work(sl.tiles, ntiles, stride, prof.d_blocks, st);
       if (sl.xn) gg::launch_cross_work(sl.tiles, sl.xn, ntiles, stride, dB.nchunk, prof.d_blocks + 1, st);
       else gg::launch_tile_work(sl.tiles, ntiles, stride, prof.d_blocks + 1, st);
     }
@@ -2272,7 +2279,7 @@ extern "C" int gg_jtensor_batch_noalloc(gg_ctx* ctx, const double* pts, int64_t 
     return ctx->fail(GG_ECUDA, "cuTensorMapEncodeTiled failed for the point operand");
   size_t ps = 0;
   ctx->prof_begin(GG_PROF_BASIS, st, &ps);
-  e = gg::launch_basis_tile(ctx->dB, &tms_hi, &tms_lo, pts, n, nullptr, 0, inv_row, nullptr, st);
+  e = gg::launch_basis_tile(ctx->dB, &tms_hi, &tms_lo, pts, n, nullptr, 0, inv_row, nullptr, nullptr, st);
   ctx->prof_end(st, ps);
   if (e != cudaSuccess) return ctx->cuda_fail(e, "basis kernel launch");
   gg::TcArgs ta{&tma_hi, &tma_lo, &ctx->tm_b_hi, &ctx->tm_b_lo, inv_row, ctx->inv_col.as<float>(),

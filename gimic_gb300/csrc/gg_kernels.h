@@ -31,10 +31,16 @@ constexpr int kNDots = 37;
 // 2^-24 of the row's largest basis value times the matrix entry per term:
 // one fp32 rounding of the main product's largest terms.  The contraction
 // issues only the block's main product (hi*hi).
+//
+// screen_out (short passes, no more tiles than SMs, only): no tile screen
+// ran before; the kernel screens every tile itself, writes the lists to
+// screen_out (as launch_tile_screen would, tiles is then ignored) and sets
+// the xneed bits it owns before clearing them (xneed need not be set on
+// entry).
 constexpr float kCrossSkipScaled = 1.0f;
 cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* tm_lo, const double* pts,
                               int64_t npts, const int* tiles, int stride, float* inv_scale,
-                              unsigned long long* xneed, cudaStream_t st);
+                              unsigned long long* xneed, int* screen_out, cudaStream_t st);
 // phi, grad phi and the Laplacian in fp64 for the plain FP64 path.
 void launch_basis_fp64(const DevBasis& B, const double* pts, int64_t npts, int64_t ld, double* phi, double* gx,
                        double* gy, double* gz, double* lap, cudaStream_t st);

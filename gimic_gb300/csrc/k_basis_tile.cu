@@ -42,6 +42,7 @@
 #include "gg_device.cuh"
 #include "gg_kernels.h"
 #include "gg_once.h"
+#include "gg_tiles.cuh"
 
 namespace gg {
 
@@ -52,6 +53,12 @@ constexpr int kHalfK = kBlockK / 2;                     // columns staged and st
 constexpr int kStageBytes = kBlockM * kHalfK * 2;       // one 128 x 32 fp16 tile: 8 KiB
 constexpr int kBufBytes = 2 * kStageBytes;              // hi + lo
 constexpr int kTileSmem = kBufBytes + 1024;             // one buffer + alignment slack
+constexpr int kMaxScreenChunks = 4096 / kChunkF;        // chunks a short pass screens in the kernel
+// the short kernel's screening marks and the tile's sphere (centre, radius)
+struct ScreenSmem {
+  float sph[4];
+  unsigned char chunk[kMaxScreenChunks], kb[64];
+};
 
 __device__ __forceinline__ void tma_store_2d(const void* tmap, const void* src, int c0, int c1) {
   asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
@@ -181,7 +188,7 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
                                                 const double* __restrict__ pts, int64_t npts,
                                                 const int* __restrict__ tiles, int stride,
                                                 float* __restrict__ inv_scale, unsigned long long* xneed,
-                                                float* s_scale) {
+                                                float* s_scale, ScreenSmem* ss, int* screen_out) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -204,7 +211,29 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
 
   // active K blocks of this tile (all when no screening lists are given)
   uint64_t kb_on = ~0ull;
-  if (tiles) {
+  // Short pass without an earlier tile screen (screen_out): every CTA of the
+  // tile screens it (the same lists as tile_screen_kernel, gg_tiles.cuh) and
+  // the first writes the lists for the contraction.  The marks are cleared
+  // here and the tile's sphere formed by the first warp of the second thread
+  // group while the first group computes the row scales; the shells are
+  // marked after the row-scale barrier.
+  if constexpr (kSubs > 1) {
+    if (screen_out) {
+      for (int i = threadIdx.x; i < B.nchunk; i += blockDim.x) ss->chunk[i] = 0;
+      for (int i = threadIdx.x; i < B.kpad / kBlockK; i += blockDim.x) ss->kb[i] = 0;
+      if (threadIdx.x >= kBlockM && threadIdx.x < kBlockM + 32) {
+        float cf[3], rf;
+        warp_tile_sphere(pts, npts, blockIdx.x, threadIdx.x & 31, cf, &rf);
+        if (threadIdx.x == kBlockM) {
+          ss->sph[0] = cf[0];
+          ss->sph[1] = cf[1];
+          ss->sph[2] = cf[2];
+          ss->sph[3] = rf;
+        }
+      }
+    }
+  }
+  if (tiles && !screen_out) {
     const int* tl = tiles + blockIdx.x * static_cast<int64_t>(stride);
     const int nk = tl[1];
     const int* kl = tl + 2 + B.nchunk;
@@ -244,6 +273,31 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
     if (sub == 0) s_scale[row] = scale;
     __syncthreads();
     scale = s_scale[row];
+  }
+  if constexpr (kSubs > 1) {
+    if (screen_out) {
+      const int nkb = B.kpad / kBlockK;
+      const float cf[3] = {ss->sph[0], ss->sph[1], ss->sph[2]};
+      for (int sh = threadIdx.x; sh < B.nshells; sh += blockDim.x) mark_shell(B, sh, cf, ss->sph[3], ss->chunk, ss->kb);
+      __syncthreads();
+      if (blockIdx.y == 0 && threadIdx.x < 32)
+        warp_write_lists(B, ss->chunk, ss->kb, screen_out + blockIdx.x * static_cast<int64_t>(stride), threadIdx.x);
+      kb_on = 0;
+      for (int i = 0; i < nkb; ++i)
+        if (ss->kb[i]) kb_on |= 1ull << i;
+      // this CTA's half blocks need the cross products until shown small
+      // below (no earlier kernel set the mask; the other CTAs of the tile
+      // own the other bits)
+      if (xneed && threadIdx.x == 0) {
+        unsigned long long w0 = 0ull, w1 = 0ull;
+        for (int hb = hb0; hb < hb1; ++hb) {
+          if (hb < 64) w0 |= 1ull << hb;
+          else w1 |= 1ull << (hb - 64);
+        }
+        if (w0) atomicOr(xneed + 2 * static_cast<int64_t>(blockIdx.x), w0);
+        if (w1) atomicOr(xneed + 2 * static_cast<int64_t>(blockIdx.x) + 1, w1);
+      }
+    }
   }
 
   // ---- pass 2: values, staged per half K block and stored with TMA --------
@@ -290,7 +344,7 @@ __global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_c
                                                                   int64_t npts, const int* __restrict__ tiles,
                                                                   int stride, float* __restrict__ inv_scale,
                                                                   unsigned long long* __restrict__ xneed) {
-  basis_tile_body<1>(tm_hi, tm_lo, B, pts, npts, tiles, stride, inv_scale, xneed, nullptr);
+  basis_tile_body<1>(tm_hi, tm_lo, B, pts, npts, tiles, stride, inv_scale, xneed, nullptr, nullptr, nullptr);
 }
 
 constexpr int kSubs = 4;
@@ -299,16 +353,18 @@ constexpr int kShortThreads = kBlockM * kSubs;
 __global__ void __launch_bounds__(kShortThreads) basis_tile_short_kernel(
     const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo, DevBasis B,
     const double* __restrict__ pts, int64_t npts, const int* __restrict__ tiles, int stride,
-    float* __restrict__ inv_scale, unsigned long long* __restrict__ xneed) {
+    float* __restrict__ inv_scale, unsigned long long* __restrict__ xneed, int* screen_out) {
   __shared__ float s_scale[kBlockM];
-  basis_tile_body<kSubs>(tm_hi, tm_lo, B, pts, npts, tiles, stride, inv_scale, xneed, s_scale);
+  __shared__ ScreenSmem ss;
+  basis_tile_body<kSubs>(tm_hi, tm_lo, B, pts, npts, tiles, stride, inv_scale, xneed, s_scale, &ss, screen_out);
 }
 
 cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* tm_lo, const double* pts,
                               int64_t npts, const int* tiles, int stride, float* inv_scale,
-                              unsigned long long* xneed, cudaStream_t st) {
+                              unsigned long long* xneed, int* screen_out, cudaStream_t st) {
   if (npts <= 0) return cudaSuccess;
   if (B.kpad / kBlockK > 64) return cudaErrorInvalidValue;  // K-block mask is 64 bits
+  if (screen_out && B.nchunk > kMaxScreenChunks) return cudaErrorInvalidValue;
   // the shared-memory attribute (it applies to the current device) and the
   // SM count, once per device
   static PerDevice pd;
@@ -329,10 +385,12 @@ cudaError_t launch_basis_tile(const DevBasis& B, const void* tm_hi, const void* 
   int kgroups = 1;
   if (nsm > 0 && ntiles < 2 * nsm) kgroups = static_cast<int>(std::min<int64_t>(nhb, (2 * nsm + ntiles - 1) / ntiles));
   const dim3 grid(static_cast<unsigned>(ntiles), static_cast<unsigned>(kgroups));
+  if (screen_out && kgroups == 1) return cudaErrorInvalidValue;  // only the short kernel screens its tiles
   if (kgroups > 1)
     basis_tile_short_kernel<<<grid, kShortThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
                                                                    *static_cast<const CUtensorMap*>(tm_lo), B, pts,
-                                                                   npts, tiles, stride, inv_scale, xneed);
+                                                                   npts, tiles, stride, inv_scale, xneed,
+                                                                   screen_out);
   else
     basis_tile_kernel<<<grid, kTileThreads, kTileSmem, st>>>(*static_cast<const CUtensorMap*>(tm_hi),
                                                             *static_cast<const CUtensorMap*>(tm_lo), B, pts, npts,

@@ -17,6 +17,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include "gg_kernels.h"
+#include "gg_tiles.cuh"
 
 namespace gg {
 
@@ -56,16 +57,9 @@ __global__ void gather_kernel(const double* __restrict__ pts, const int* __restr
   out[3 * p + 2] = pts[3 * s + 2];
 }
 
-// One warp per tile, four tiles per block of 128 threads.  tiles[t * stride]
-// = {#chunks, #kblocks, chunk ids..., kblock ids...}.  A shell is out of
-// range for the tile when |R_A - c| - rho > radius (c, rho: centre and radius
-// of the tile's bounding box), which by the triangle inequality excludes it
-// for every point.  The box is formed in fp32 from coordinates rounded
-// outwards (warp shuffles), and rho is widened by far more than the fp32
-// rounding of the centre, so the test stays conservative without FP64
-// arithmetic (the FP64 pipe runs at 1/64 of the fp32 rate).  A shell in range
-// marks the chunks and K blocks its functions fall in (the functions of a
-// shell are contiguous).
+// One warp per tile, four tiles per block of 128 threads: the tile's
+// bounding sphere, every shell against it, and the lists tiles[t * stride]
+// = {#chunks, #kblocks, chunk ids..., kblock ids...} (gg_tiles.cuh).
 __global__ void __launch_bounds__(128) tile_screen_kernel(DevBasis B, const double* __restrict__ pts, int64_t n,
                                                           int64_t ntiles, int stride, int* __restrict__ tiles,
                                                           unsigned long long* __restrict__ xneed) {
@@ -77,70 +71,14 @@ __global__ void __launch_bounds__(128) tile_screen_kernel(DevBasis B, const doub
   if (xneed && lane < 2) xneed[2 * t + lane] = ~0ull;  // every half K block needs cross products until shown small
   unsigned char* chunk_on = smem_raw + warp * (B.nchunk + nkb);  // nchunk
   unsigned char* kb_on = chunk_on + B.nchunk;                      // kpad / 64
-  float lo[3], hi[3];
-  for (int k = 0; k < kBlockM / 32; ++k) {
-    const int64_t p = t * kBlockM + k * 32 + lane;
-    const int64_t q = p < n ? p : t * kBlockM;  // the tile's first point stands in past the end
-    for (int d = 0; d < 3; ++d) {
-      const double v = pts[3 * q + d];
-      const float l = __double2float_rd(v), h = __double2float_ru(v);
-      lo[d] = k == 0 ? l : fminf(lo[d], l);
-      hi[d] = k == 0 ? h : fmaxf(hi[d], h);
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1)
-    for (int d = 0; d < 3; ++d) {
-      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
-      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
-    }
+  float cf[3], rhof;
+  warp_tile_sphere(pts, n, t, lane, cf, &rhof);
   for (int i = lane; i < B.nchunk; i += 32) chunk_on[i] = 0;
   for (int i = lane; i < nkb; i += 32) kb_on[i] = 0;
-  float cf[3], rho2 = 0.f, cmax = 0.f;
-  for (int d = 0; d < 3; ++d) {
-    cf[d] = 0.5f * (lo[d] + hi[d]);
-    const float h = __fmul_ru(0.5f, __fsub_ru(hi[d], lo[d]));
-    rho2 = __fmaf_ru(h, h, rho2);
-    cmax = fmaxf(cmax, fabsf(cf[d]));
-  }
-  // the centre's fp32 rounding is below 2^-23 |c| per axis; widen by 2^-16
-  const float rhof = __fmul_ru(sqrtf(rho2), 1.f + 1e-6f) + 1.6e-5f * (1.f + cmax);
   __syncwarp();
-  // out of range when |R_A - c|^2 > (radius + rho)^2, the right side
-  // widened by 1e-5 relative and 1e-4 Bohr^2 against the rounding of both
-  for (int sh = lane; sh < B.nshells; sh += 32) {
-    const float4 at = __ldg(B.atom_f4 + __ldg(B.sh_atom + sh));
-    const float dx = at.x - cf[0], dy = at.y - cf[1], dz = at.z - cf[2];
-    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float reach = __ldg(B.sh_rad + sh) + rhof;
-    const int nc = __ldg(B.sh_ncomp + sh);
-    if (nc > 0 && !(d2 > fmaf(reach * reach, 1.00001f, 1e-4f))) {
-      const int f0 = __ldg(B.sh_f0 + sh), f1 = f0 + nc - 1;
-      for (int c = f0 / kChunkF; c <= f1 / kChunkF; ++c) chunk_on[c] = 1;
-      for (int c = f0 / kBlockK; c <= f1 / kBlockK; ++c) kb_on[c] = 1;
-    }
-  }
+  for (int sh = lane; sh < B.nshells; sh += 32) mark_shell(B, sh, cf, rhof, chunk_on, kb_on);
   __syncwarp();
-  // the lists, compacted in index order
-  int* out = tiles + t * stride;
-  int nc = 0, nk = 0;
-  for (int i0 = 0; i0 < B.nchunk; i0 += 32) {
-    const int i = i0 + lane;
-    const bool on = i < B.nchunk && chunk_on[i];
-    const unsigned m = __ballot_sync(0xffffffffu, on);
-    if (on) out[2 + nc + __popc(m & ((1u << lane) - 1u))] = i;
-    nc += __popc(m);
-  }
-  for (int i0 = 0; i0 < nkb; i0 += 32) {
-    const int i = i0 + lane;
-    const bool on = i < nkb && kb_on[i];
-    const unsigned m = __ballot_sync(0xffffffffu, on);
-    if (on) out[2 + B.nchunk + nk + __popc(m & ((1u << lane) - 1u))] = i;
-    nk += __popc(m);
-  }
-  if (lane == 0) {
-    out[0] = nc;
-    out[1] = nk;
-  }
+  warp_write_lists(B, chunk_on, kb_on, tiles + t * stride, lane);
 }
 
 // Sum over tiles of (active chunks x active K blocks): the number of
