@@ -183,16 +183,21 @@ __global__ void __launch_bounds__(256) mlp_infer_kernel(const float* __restrict_
 //   f4 = log10(1e-6 + sum_s sqrt(a_s) exp(-a_s d_s^2)) / 3, the local
 //        shell-exponent density: a_s is the smallest exponent of shell s and
 //        d_s the distance to its centre.
+// All in fp32: the offsets r - R_A from grid splits (exact differences of
+// the high parts), |r - R_A|^2 as a double-float and the exponential with a
+// double-float argument (gauss_df), so the features agree with the FP64
+// formulas to a few fp32 roundings; the FP64 pipe stays idle.
 __global__ void __launch_bounds__(256) mlp_features_kernel(DevBasis B, const double* __restrict__ pts,
                                                            const double* __restrict__ uv, int64_t n,
                                                            float* __restrict__ f) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double r0 = pts[3 * i], r1 = pts[3 * i + 1], r2 = pts[3 * i + 2];
-  double n1 = 1e300, n2 = 1e300;
+  const float2 rg[3] = {grid_split(df_split(pts[3 * i])), grid_split(df_split(pts[3 * i + 1])),
+                        grid_split(df_split(pts[3 * i + 2]))};
+  float n1 = INFINITY, n2 = INFINITY;
+  float s3[3];
   for (int a = 0; a < B.natoms; ++a) {
-    const double dx = r0 - B.atom_xyz[3 * a], dy = r1 - B.atom_xyz[3 * a + 1], dz = r2 - B.atom_xyz[3 * a + 2];
-    const double d2 = dx * dx + dy * dy + dz * dz;
+    const float d2 = atom_offset_g(rg, B.atom_g, a, s3).h;
     if (d2 < n1) {
       n2 = n1;
       n1 = d2;
@@ -201,20 +206,29 @@ __global__ void __launch_bounds__(256) mlp_features_kernel(DevBasis B, const dou
     }
   }
   if (B.natoms < 2) n2 = n1;
-  double dens = 0.0;
+  DFloat dens{0.f, 0.f};  // a compensated sum over the shells
+  int cur = -1;
+  DFloat d2a{0.f, 0.f};
   for (int s = 0; s < B.nshells; ++s) {
-    const int a = B.sh_atom[s], p0 = B.sh_prim[s], np = B.sh_npf[s];
-    double amin = B.p_xpd[p0];
-    for (int q = 1; q < np; ++q) amin = fmin(amin, B.p_xpd[p0 + q]);
-    const double dx = r0 - B.atom_xyz[3 * a], dy = r1 - B.atom_xyz[3 * a + 1], dz = r2 - B.atom_xyz[3 * a + 2];
-    dens += sqrt(amin) * exp(-amin * (dx * dx + dy * dy + dz * dz));
+    const int a = __ldg(B.sh_atom + s), p0 = __ldg(B.sh_prim + s), np = __ldg(B.sh_npf + s);
+    if (a != cur) {
+      cur = a;
+      d2a = atom_offset_g(rg, B.atom_g, a, s3);
+    }
+    // the smallest exponent of the shell, as its (hi, lo) pair
+    float4 pm = __ldg(B.p_pack + p0);
+    for (int q = 1; q < np; ++q) {
+      const float4 pq = __ldg(B.p_pack + p0 + q);
+      if (pq.x + pq.y < pm.x + pm.y) pm = pq;
+    }
+    dens = df_add(dens, DFloat{sqrtf(pm.x) * gauss_df(pm.x, pm.y, d2a.h, d2a.l), 0.f});
   }
   float* o = f + kMlpIn * i;
-  o[0] = static_cast<float>(uv[2 * i] * 0.125);
-  o[1] = static_cast<float>(uv[2 * i + 1] * 0.125);
-  o[2] = static_cast<float>(log(fmax(sqrt(n1), 0.05)));
-  o[3] = static_cast<float>(log(fmax(sqrt(n2), 0.05)));
-  o[4] = static_cast<float>(log10(1e-6 + dens) / 3.0);
+  o[0] = static_cast<float>(uv[2 * i]) * 0.125f;
+  o[1] = static_cast<float>(uv[2 * i + 1]) * 0.125f;
+  o[2] = logf(fmaxf(sqrtf(n1), 0.05f));
+  o[3] = logf(fmaxf(sqrtf(n2), 0.05f));
+  o[4] = log10f(1e-6f + (dens.h + dens.l)) / 3.f;
 }
 
 void launch_mlp_features(const DevBasis& B, const double* pts, const double* uv, int64_t n, float* feats,
