@@ -91,6 +91,26 @@ def test_quadrature_known_answers():
     assert api.gauss_data(0.0, 5.0, 9, 1)[0].tolist() == [0.0]
 
 
+def test_plane_records_packed_like_the_structured_path():
+    """The gg_grid records of one to four planes (packed field by field)
+    hold the same fields as the concatenated path of five or more, and
+    point into the caller's axis arrays."""
+    ax = [(np.linspace(0, 8, 60), np.full(60, 0.5)), (np.linspace(-8, 8, 61), np.full(61, 0.25)),
+          (np.zeros(1), np.ones(1))]
+    pl = (np.array([1.0, -2.0, 3.5]), np.arange(9.0).reshape(3, 3), ax, 7.5)
+    few, keep = api._grid_records([pl, pl])
+    many, flat = api._grid_records([pl] * 5)
+    for f in ("origin", "basv", "npts", "radius"):
+        assert np.array_equal(few[f][:2], many[f][:2]), f
+    assert few["basv"][0].tolist() == np.arange(9.0).reshape(3, 3).T.reshape(9).tolist()
+    rec = _lib.GridSpec.from_buffer_copy(few[1].tobytes())
+    assert rec.npts[:] == [60, 61, 1] and rec.radius == 7.5
+    assert rec.pts[1] is not None
+    arrs = keep[1]
+    assert C.cast(rec.pts[1], C.c_void_p).value == arrs[2].__array_interface__["data"][0]
+    assert C.cast(rec.wgt[0], C.c_void_p).value == arrs[1].__array_interface__["data"][0]
+
+
 def test_au2si():
     assert abs(api.au2si(1.0) - 28.179409) < 5e-7
     assert api.au2si(-0.708546) == pytest.approx(oracle.au2si(-0.708546), rel=1e-15)
