@@ -151,25 +151,38 @@ __global__ void mlp_adam_kernel(float* __restrict__ params, const float* __restr
 // bf16 inference: weights and activations rounded to bf16, fp32 arithmetic.
 __global__ void __launch_bounds__(256) mlp_infer_kernel(const float* __restrict__ params, const float* __restrict__ x,
                                                         int n, float* __restrict__ y) {
-  __shared__ float w[kMlpParams];
+  __shared__ __align__(16) float w[kMlpParams];
   for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) w[i] = bf(params[i]);
   __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float xin[kIn];
   for (int k = 0; k < kIn; ++k) xin[k] = bf(x[static_cast<int64_t>(i) * kIn + k]);
+  // the hidden activations stay in registers (the layer loops are unrolled,
+  // so every index is a constant), and the second layer reads its weights
+  // four per shared-memory load; the same FMAs in the same order as a plain
+  // loop
   float h1[kH];
-#pragma unroll 8
+#pragma unroll
   for (int o = 0; o < kH; ++o) {
     float a = w[oB1 + o];
+#pragma unroll
     for (int k = 0; k < kIn; ++k) a = fmaf(w[oW1 + o * kIn + k], xin[k], a);
     h1[o] = bf(silu_fast(a));
   }
   float out = w[oB3];
+  static_assert(oW2 % 4 == 0 && kH % 4 == 0, "16-byte aligned weight rows");
   for (int o = 0; o < kH; ++o) {
     float a = w[oB2 + o];
-#pragma unroll 8
-    for (int k = 0; k < kH; ++k) a = fmaf(w[oW2 + o * kH + k], h1[k], a);
+    const float4* wr = reinterpret_cast<const float4*>(w + oW2 + o * kH);
+#pragma unroll
+    for (int k4 = 0; k4 < kH / 4; ++k4) {
+      const float4 q = wr[k4];
+      a = fmaf(q.x, h1[4 * k4], a);
+      a = fmaf(q.y, h1[4 * k4 + 1], a);
+      a = fmaf(q.z, h1[4 * k4 + 2], a);
+      a = fmaf(q.w, h1[4 * k4 + 3], a);
+    }
     out = fmaf(w[oW3 + o], bf(silu_fast(a)), out);
   }
   y[i] = out;
