@@ -61,6 +61,8 @@ def parse():
                     help="small cases for ncu: cube (65,536 C24H24 cube points, two passes), plane (30 C6H6 "
                          "60x60 bond-plane passes), mlp (proposal features, one training epoch, inference on "
                          "262,144 samples), fp64 (the plain FP64 path on 16,384 C24H24 points, twice)")
+    ap.add_argument("--profile-stride", type=int, default=32,
+                    help="cube profile case: every n-th cube point (32: 65,536 points; 4: 524,288)")
     ap.add_argument("--data", default=os.environ.get("GIMIC_GB300_DATA",
                                                      os.path.join(tempfile.gettempdir(), "gimic_gb300_data")))
     return ap.parse_args()
@@ -129,7 +131,7 @@ def peaks():
 
 def traffic_model():
     """(fixed bytes, bytes per point) of the tensor-core kernel's DRAM traffic
-    from the committed ncu summary of the 65,536-point profile case
+    from the committed ncu summary of the 524,288-point profile case
     (profiles/tc_fused_traffic.json), or None."""
     try:
         t = json.load(open(os.path.join(ROOT, "profiles", "tc_fused_traffic.json")))
@@ -543,8 +545,9 @@ def run_proposal(args):
 
 def run_profile_case(args):
     """Small cases for ncu captures (a few MB to a few hundred MB on the
-    device).  cube: 65,536 cube points (every 32nd, so that they span the
-    cube) through the split path twice; the second pass is the one to
+    device).  cube: every 32nd cube point (65,536, so that they span the
+    cube; --profile-stride 4 gives 524,288, about 3.5 waves of the basis
+    kernel) through the split path twice; the second pass is the one to
     capture."""
     import torch
 
@@ -595,7 +598,7 @@ def run_profile_case(args):
     g = api.Gimic(mp, xp, screening=1e-8, precision="split16")
     if args.batch:
         g.set_max_batch(args.batch)
-    P = torch.as_tensor(cube_points_np()[::32].copy(), device="cuda")
+    P = torch.as_tensor(cube_points_np()[::max(1, args.profile_stride)].copy(), device="cuda")
     for _ in range(2):
         g.jtensor_batch(P, rho=True, divj=True)
     torch.cuda.synchronize()
@@ -844,7 +847,7 @@ def main():
                                    "are precision overhead, skipped for blocks small for a whole tile) / "
                                    "tc_fused_kernel time",
                      "traffic": (tmodel[0] + tmodel[1] * per_launch_pts) if tmodel else None,
-                     "traffic_source": "ncu dram bytes of the 65,536-point profile case scaled to the launch: "
+                     "traffic_source": "ncu dram bytes of the 524,288-point profile case scaled to the launch: "
                                        "fixed matrix operand + bytes per point x points",
                      "kernel": "tc_fused_kernel", "launch_ms": tc_avg, "points_per_launch": per_launch_pts,
                      "gemm_blocks_issued_fraction": issued / dense if dense else None,
