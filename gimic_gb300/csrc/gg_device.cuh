@@ -179,7 +179,8 @@ __device__ __forceinline__ double df_to_double(DFloat a) {
 __device__ __forceinline__ bool df_le(DFloat a, float2 b) { return a.h < b.x || (a.h == b.x && a.l <= b.y); }
 
 // Grid split of a coordinate: x = g + l with g a multiple of 2^-12 and
-// |l| <= 2^-13 (for |x| < 2^12 Bohr; beyond, g is x rounded to fp32).  Two
+// |l| <= 2^-13 + ulp(x) / 2 (for |x| < 2^12 Bohr; beyond, g is x rounded to
+// fp32).  Two
 // grid-split coordinates below 2^12 in magnitude differ by an exact fp32
 // difference of the g parts plus a small one of the l parts, which makes
 // r - R_A cheap to form without losing digits.
@@ -192,8 +193,11 @@ __device__ __forceinline__ float2 grid_split(DFloat x) {
 // Position of a point relative to atom a (fp32, rounded once) and its
 // squared distance as a double-float, from the grid splits of the point
 // (rg) and of the atom table.  d = dh + dl with dh = g_r - g_A exact and
-// |dl| <= 2^-12; d^2 = dh^2 (exact as p + e) + dl (2 dh + dl).  The relative
-// error of the result is about 2^-24 |dl| / |d| (2^-36 once |dh| >= 1).
+// |dl| about 2^-12 at most; d^2 = dh^2 (exact as p + e) + dl (2 dh + dl).
+// The low parts carry about 2^-36 Bohr of rounding, so on random points
+// (restated in fp32 on the CPU, tests/test_numerics.py) the error of d^2
+// stays below 2^-33 |d| + 2^-45 Bohr^2: a relative 2^-33 once |d| >= 1
+// Bohr, far below what the fp32 exponential of alpha d^2 resolves.
 __device__ __forceinline__ DFloat atom_offset_g(const float2 rg[3], const float2* atom_g, int a, float s[3]) {
   float dh[3], p[3], lo = 0.f;
 #pragma unroll
