@@ -200,19 +200,24 @@ class ProposalNet:
         steps = epochs * ((n + batch - 1) // batch)
         k = 0
         hist = []
+        nb = (n + batch - 1) // batch
+        losses = torch.zeros(nb, dtype=torch.float32, device=self.device)  # one slot per step of an epoch
+        x = x.contiguous()
         for _ in range(epochs):
             perm = torch.randperm(n, device=self.device, generator=gen)
-            acc = torch.zeros(1, dtype=torch.float32, device=self.device)
-            nb = 0
-            for s in range(0, n, batch):
-                idx = perm[s:s + batch]
-                lo, _ = self.loss_grad(x[idx], t[idx])
-                acc += lo
-                nb += 1
+            # the epoch's samples in shuffled order, gathered once: every
+            # minibatch is then a contiguous slice (the same samples as
+            # indexing each batch), and each step writes its loss to its own
+            # slot, so a step launches only the library's kernels
+            xs, ts = x[perm], t[perm]
+            for b, s in enumerate(range(0, n, batch)):
+                _check(self._L.gg_mlp_grad(_ptr(self.params), _ptr(xs[s:s + batch]), _ptr(ts[s:s + batch]),
+                                           min(batch, n - s), _ptr(self.grad), _ptr(losses[b:b + 1]), _stream()),
+                       "gg_mlp_grad")
                 frac = k / max(steps - 1, 1)
                 self.adam(lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * frac)))
                 k += 1
-            hist.append(float(acc) / nb)
+            hist.append(float(losses.sum()) / nb)
         return hist
 
     def predict(self, x):
