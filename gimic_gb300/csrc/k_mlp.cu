@@ -119,18 +119,37 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_kernel(const float* _
     }
   }
   __syncthreads();
-  // dW2[o][k] = sum over the block's samples of dz2[o] h1[k]; db2[o] = sum dz2[o]
-  for (int e = threadIdx.x; e < kH * kH + kH; e += blockDim.x) {
-    float a = 0.f;
-    if (e < kH * kH) {
-      const int o = e / kH, k = e % kH;
-      for (int s = 0; s < kTrainThreads; ++s) a = fmaf(d2s[s][o], h1s[s][k], a);
-      atomicAdd(&grad[oW2 + e], a);
-    } else {
-      const int o = e - kH * kH;
-      for (int s = 0; s < kTrainThreads; ++s) a += d2s[s][o];
-      atomicAdd(&grad[oB2 + o], a);
+  // dW2[o][k] = sum over the block's samples of dz2[o] h1[k], a 4 x 8 tile
+  // of it per thread (twelve shared-memory loads feed 32 FMAs per sample;
+  // each entry still adds the samples in order); db2[o] = sum dz2[o]
+  static_assert(kTrainThreads == 128 && kH == 64, "dW2 tiles: 16 x 8 threads of 4 x 8 entries");
+  {
+    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
+    float acc[4][8];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+    for (int s = 0; s < kTrainThreads; ++s) {
+      float dv[4], hv[8];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) dv[a] = d2s[s][4 * ty + a];
+#pragma unroll
+      for (int b = 0; b < 8; ++b) hv[b] = h1s[s][8 * tx + b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(dv[a], hv[b], acc[a][b]);
     }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) atomicAdd(&grad[oW2 + (4 * ty + a) * kH + 8 * tx + b], acc[a][b]);
+  }
+  if (threadIdx.x < kH) {
+    float a = 0.f;
+    for (int s = 0; s < kTrainThreads; ++s) a += d2s[s][threadIdx.x];
+    atomicAdd(&grad[oB2 + threadIdx.x], a);
   }
 }
 
