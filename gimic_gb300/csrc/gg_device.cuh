@@ -143,21 +143,9 @@ __device__ __forceinline__ DFloat fast_two_sum(float a, float b) {
   return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 
-__device__ __forceinline__ DFloat df_sub(DFloat a, float2 b) {
-  const DFloat s = two_sum(a.h, -b.x);
-  return fast_two_sum(s.h, __fadd_rn(s.l, __fsub_rn(a.l, b.y)));
-}
-
 __device__ __forceinline__ DFloat df_add(DFloat a, DFloat b) {
   const DFloat s = two_sum(a.h, b.h);
   return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
-}
-
-// (h + l)^2 with the product error recovered by an fma
-__device__ __forceinline__ DFloat df_sqr(DFloat a) {
-  const float p = __fmul_rn(a.h, a.h);
-  const float e = fmaf(a.h, a.h, -p);
-  return fast_two_sum(p, fmaf(2.0f * a.h, a.l, e));
 }
 
 // (a.h + a.l) * (b.h + b.l), the product error recovered by fmas
