@@ -125,10 +125,7 @@ __device__ __forceinline__ void stage_shells(const DevBasis& B, const float2 rg[
     }
     const int col0 = mu0 - lo;
     // a shell out of range for the whole warp only writes zeros
-    if (!__any_sync(0xffffffffu, in_range)) {
-      for (int c = c0; c < c1; ++c) put(col0 + c, 0.f, true);
-      continue;
-    }
+    if (!__any_sync(0xffffffffu, in_range)) continue;  // its columns stay as zeroed
     if ((pk.z >> 24) & 1) {
       const CartPow& cp = g.cp;
       auto comps = [&](auto basec, auto ncc) {
@@ -317,8 +314,19 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
   for (int hb = hb0; hb < hb1; ++hb) {
     if (!((kb_on >> (hb >> 1)) & 1ull)) continue;  // inactive for the tile: never read
     const int lo = hb * kHalfK, hi = min(lo + kHalfK, B.nbf);
-    if (sub == 0)
-      for (int mu = max(lo, B.nbf); mu < lo + kHalfK; ++mu) put(mu - lo, 0.f, true);  // padding columns
+    // the row's 64 bytes of each half start as zeros (16-byte stores; each
+    // thread of the point clears its share): the padding columns and the
+    // shells out of range for the whole warp are left as they are
+    {
+      constexpr int kPart = 64 / kSubs;
+      const uint32_t o = rowoff + static_cast<uint32_t>(sub * kPart);
+#pragma unroll
+      for (int b = 0; b < kPart; b += 16) {
+        *reinterpret_cast<uint4*>(base + o + b) = make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(base + kStageBytes + o + b) = make_uint4(0u, 0u, 0u, 0u);
+      }
+      if (kSubs > 1) __syncthreads();  // the other threads of the point write into this share
+    }
     if (lo < B.nbf) stage_shells<kSubs>(B, rg, scale, lo, hi, sub, g, put);
     // the half block is complete: write it to HBM, then reuse the buffer;
     // a half block small for every point of the tile needs no cross products
@@ -338,7 +346,7 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
   if (threadIdx.x == 0) bulk_wait_all();
 }
 
-__global__ void __launch_bounds__(kTileThreads) basis_tile_kernel(const __grid_constant__ CUtensorMap tm_hi,
+__global__ void __launch_bounds__(kTileThreads, 10) basis_tile_kernel(const __grid_constant__ CUtensorMap tm_hi,
                                                                   const __grid_constant__ CUtensorMap tm_lo,
                                                                   DevBasis B, const double* __restrict__ pts,
                                                                   int64_t npts, const int* __restrict__ tiles,
