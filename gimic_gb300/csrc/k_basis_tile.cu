@@ -95,7 +95,8 @@ struct AtomGeom {
 
 // One point's values of the shells that overlap the columns [lo, hi) of a
 // half K block, every kStep-th shell from the first one there plus
-// `first`.  put(col, v) stages value v (or a zero) at column col - lo.
+// `first`.  put(col, v) stages value v at column col - lo; the columns of
+// shells out of range for the whole warp keep the zeros the row starts with.
 // The shells in the standard Cartesian order (bit 24 of the shell record)
 // evaluate their components with compile-time monomials; the others select
 // the monomial from the packed exponents.  Both give x^i y^j z^k f1 with the
@@ -124,7 +125,6 @@ __device__ __forceinline__ void stage_shells(const DevBasis& B, const float2 rg[
       f1 *= scale;
     }
     const int col0 = mu0 - lo;
-    // a shell out of range for the whole warp only writes zeros
     if (!__any_sync(0xffffffffu, in_range)) continue;  // its columns stay as zeroed
     if ((pk.z >> 24) & 1) {
       const CartPow& cp = g.cp;
@@ -134,8 +134,8 @@ __device__ __forceinline__ void stage_shells(const DevBasis& B, const float2 rg[
           constexpr int code = kCartStdCode[decltype(basec)::value + c];
           constexpr int A = code / 100, Bx = (code / 10) % 10, C = code % 10;
           if (c >= c0 && c < c1) {
-            if constexpr (A + Bx + C == 0) put(col0 + c, f1, false);
-            else put(col0 + c, cart_mono<A, Bx, C>(cp) * f1, false);
+            if constexpr (A + Bx + C == 0) put(col0 + c, f1);
+            else put(col0 + c, cart_mono<A, Bx, C>(cp) * f1);
           }
         });
       };
@@ -163,7 +163,7 @@ __device__ __forceinline__ void stage_shells(const DevBasis& B, const float2 rg[
         const float yj = j == 0 ? 1.f : (j == 1 ? py[1] : (j == 2 ? py[2] : py[3]));
         const float zk = k == 0 ? 1.f : (k == 1 ? pz[1] : (k == 2 ? pz[2] : pz[3]));
         // the same value as the compile-time forms: a factor 1 is exact
-        put(col0 + c, xi * yj * zk * f1, false);
+        put(col0 + c, xi * yj * zk * f1);
       }
     }
   }
@@ -300,12 +300,11 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
   // ---- pass 2: values, staged per half K block and stored with TMA --------
   const uint32_t rowoff = static_cast<uint32_t>(row) * 64u, rxs = static_cast<uint32_t>((row >> 1) & 3) << 4;
   float vmax = 0.f;  // largest |value| this thread stages in the current half block
-  auto put = [&](int col, float v, bool zero) {
-    if (!zero) vmax = fmaxf(vmax, fabsf(v));
+  auto put = [&](int col, float v) {
+    vmax = fmaxf(vmax, fabsf(v));
     const uint32_t o = swz_col(rowoff, rxs, col);
-    const __half z = __float2half_rn(0.f);
-    const __half h = zero ? z : __float2half_rn(v);
-    const __half l = zero ? z : __float2half_rn(v - __half2float(h));
+    const __half h = __float2half_rn(v);
+    const __half l = __float2half_rn(v - __half2float(h));
     *reinterpret_cast<__half*>(base + o) = h;
     *reinterpret_cast<__half*>(base + kStageBytes + o) = l;
   };
