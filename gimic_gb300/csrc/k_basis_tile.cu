@@ -200,7 +200,7 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
     prefetch_l1(B.sh_pack, B.nshells * sizeof(int4));
     prefetch_l1(B.sh_rad2_df, B.nshells * sizeof(float2));
     prefetch_l1(B.p_pack, B.nprim * sizeof(float4));
-    prefetch_l1(B.atom_df, B.natoms * 3 * sizeof(float2));
+    prefetch_l1(B.atom_f4, B.natoms * sizeof(float4));
     prefetch_l1(B.atom_g, B.natoms * 3 * sizeof(float2));
     prefetch_l1(B.f_ijk, B.nbf * sizeof(int));
     prefetch_l1(B.f_shell, B.nbf * sizeof(int));
@@ -252,8 +252,8 @@ __device__ __forceinline__ void basis_tile_body(const CUtensorMap& tm_hi, const 
     const float* __restrict__ env = B.atom_env;
     const int nb = B.env_bins;
     for (int a = 0; a < B.natoms; ++a) {
-      const float dx = r[0].h - __ldg(&B.atom_df[3 * a].x), dy = r[1].h - __ldg(&B.atom_df[3 * a + 1].x),
-                  dz = r[2].h - __ldg(&B.atom_df[3 * a + 2].x);
+      const float4 A = __ldg(B.atom_f4 + a);  // the coordinates rounded to fp32, one 16-byte load
+      const float dx = r[0].h - A.x, dy = r[1].h - A.y, dz = r[2].h - A.z;
       const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
       const float t = (__log2f(fmaxf(d2, 1e-30f)) + kEnvOffset) * kEnvPerOctave;
       const int bin = t <= 0.f ? 0 : static_cast<int>(t);
