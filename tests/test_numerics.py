@@ -1,6 +1,8 @@
 """CPU checks of the fp32 geometry the kernels use for r - R_A and
-|r - R_A|^2, restated with numpy float32 operations in the kernels' order
-(gimic_gb300/csrc/gg_device.cuh: grid_split, atom_offset_g, two_sum).
+|r - R_A|^2, and of the fp32 tile screen, restated with numpy float32
+operations (and the directed roundings) in the kernels' order
+(gimic_gb300/csrc/gg_device.cuh: grid_split, atom_offset_g, two_sum;
+gimic_gb300/csrc/gg_tiles.cuh: warp_tile_sphere, mark_shell).
 The kernels' results are checked against the FP64 oracle by the GPU tests;
 these tests pin the error bounds the device code states, over many random
 points, without a GPU.  A fused multiply-add is restated as the float64
@@ -76,3 +78,80 @@ def test_atom_offsets_within_stated_bounds():
         assert abs(float(h) + float(l) - exact) <= 2.0 ** -33 * np.sqrt(exact) + 2.0 ** -45
         for c in range(3):
             assert abs(float(s[c]) - d[c]) <= 2.0 ** -24 * abs(d[c]) + 2.0 ** -35
+
+
+# ---- tile screening (gimic_gb300/csrc/gg_tiles.cuh) -------------------------
+
+def _rd(x):
+    f = f32(x)
+    return np.nextafter(f, f32(-np.inf)) if float(f) > x else f
+
+
+def _ru(x):
+    f = f32(x)
+    return np.nextafter(f, f32(np.inf)) if float(f) < x else f
+
+
+def _tile_sphere(pts):
+    """warp_tile_sphere: the box from outward-rounded fp32 coordinates, its
+    centre and the radius widened against the centre's rounding."""
+    lo = [min(_rd(v) for v in pts[:, d]) for d in range(3)]
+    hi = [max(_ru(v) for v in pts[:, d]) for d in range(3)]
+    cf, rho2, cmax = [], f32(0.0), f32(0.0)
+    for d in range(3):
+        cf.append(f32(f32(0.5) * f32(lo[d] + hi[d])))
+        h = _ru(0.5 * float(_ru(float(hi[d]) - float(lo[d]))))
+        rho2 = _ru(float(h) * float(h) + float(rho2))
+        cmax = max(cmax, abs(cf[d]))
+    s = f32(np.sqrt(rho2))
+    return cf, f32(_ru(float(s) * float(f32(1.0 + 1e-6))) + f32(f32(1.6e-5) * f32(1.0 + cmax)))
+
+
+def _in_range(cf, rhof, atom, radius):
+    """mark_shell's test: out of range when |R_A - c|^2 > (radius + rho)^2,
+    widened."""
+    at = [f32(v) for v in atom]
+    dx, dy, dz = (f32(at[d] - cf[d]) for d in range(3))
+    d2 = fma(dx, dx, fma(dy, dy, f32(dz * dz)))
+    reach = f32(_ru(min(radius, 1e30)) + rhof)
+    return not (d2 > fma(f32(reach * reach), f32(1.00001), f32(1e-4)))
+
+
+def test_tile_screen_is_conservative():
+    """A shell the fp32 tile test drops is out of range (|r - R_A| > radius,
+    in FP64) for every point of the tile, over tiles up to 8 Bohr wide
+    anywhere within 40 Bohr, with shells placed to just reach the tile; half
+    the tiles have points on their box's corners, where the bounding sphere
+    is tight and only the widening against the fp32 roundings keeps the test
+    conservative (without it, about 5% of such needed shells are dropped)."""
+    rng = np.random.default_rng(13)
+    dropped = kept = 0
+    for it in range(300):
+        centre = rng.uniform(-40, 40, 3)
+        half = rng.uniform(0.05, 1.0, 3) * 10.0 ** rng.uniform(-2, 0.6)
+        pts = centre + rng.uniform(-1.0, 1.0, (128, 3)) * half
+        if it % 2:  # a box whose corners are tile points: the sphere passes through them
+            pts[:8] = centre + np.array([[sx, sy, sz] for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)]) * half
+        cf, rhof = _tile_sphere(pts)
+        for _ in range(20):
+            radius = 10.0 ** rng.uniform(-1, 1.3)
+            direction = rng.normal(size=3)
+            if it % 2 and rng.uniform() < 0.5:
+                direction = np.sign(direction) * half  # towards a corner
+            direction /= np.linalg.norm(direction)
+            # nuclei at about the distance where the shell just reaches the tile
+            dmin = np.min(np.linalg.norm(pts - centre, axis=1))
+            if rng.uniform() < 0.5:
+                atom = centre + direction * (radius + rng.uniform(-1.0, 1.0) * 0.05 * radius + dmin)
+            else:
+                # within a few 1e-7 of just reaching the tile's outermost point
+                # in that direction: the fp32 roundings decide
+                far = pts[np.argmax(pts @ direction)]
+                atom = far + direction * radius * (1.0 + rng.uniform(-3e-7, 3e-7))
+            need = bool(np.any(np.sum((pts - atom) ** 2, axis=1) <= radius * radius))
+            got = _in_range(cf, rhof, atom, radius)
+            if need:
+                assert got, "a shell some point needs was dropped"
+            dropped += not got
+            kept += got
+    assert dropped > 100 and kept > 100  # the test exercises both sides
