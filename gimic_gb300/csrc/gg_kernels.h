@@ -25,12 +25,13 @@ constexpr int kNDots = 37;
 // bit per half K block (32 functions), all ones on entry.  The kernel
 // clears the bit of every half block whose scaled values are all below
 // kCrossSkipScaled in magnitude for every point of the tile: 2^-14 of the
-// row-scale bound (2^14), itself at least the row's largest value.  The
-// lo part of an fp16 split is at most 2^-11 of the value, so for such a
-// block the two cross products of the split (hi*lo, lo*hi) add at most
-// 2^-24 of the row's largest basis value times the matrix entry per term:
-// one fp32 rounding of the main product's largest terms.  The contraction
-// issues only the block's main product (hi*hi).
+// row-scale bound (2^14), itself at least the row's largest value (and
+// within 2^7 of it on the seeded bases).  The lo part of an fp16 split is at
+// most 2^-11 of the value, so for such a block the two cross products of the
+// split (hi*lo, lo*hi) add at most 2^-24 of the row bound times the matrix
+// entry per term (tests/test_numerics.py): about one fp32 rounding of the
+// products of the row's largest values.  The contraction issues only the
+// block's main product (hi*hi).
 //
 // screen_out (short passes, no more tiles than SMs, only): no tile screen
 // ran before; the kernel screens every tile itself, writes the lists to

@@ -155,3 +155,20 @@ def test_tile_screen_is_conservative():
             dropped += not got
             kept += got
     assert dropped > 100 and kept > 100  # the test exercises both sides
+
+
+# ---- cross-product skip (gimic_gb300/csrc/gg_kernels.h, kCrossSkipScaled) ----
+
+def test_cross_products_of_small_blocks_within_bound():
+    """For scaled basis values below 1 (2^-14 of the row bound 2^14) and
+    scaled matrix entries up to 2^14, the cross products hi*lo + lo*hi of the
+    fp16 splits stay within 2^-24 of the row bound times the entry."""
+    rng = np.random.default_rng(14)
+    a = np.concatenate([rng.uniform(-1, 1, 20000), 10.0 ** rng.uniform(-12, 0, 20000)]).astype(np.float32)
+    b = (rng.uniform(-1, 1, a.size) * 10.0 ** rng.uniform(-6, np.log10(16383.0), a.size)).astype(np.float32)
+    ah = a.astype(np.float16)
+    al = (a - ah.astype(np.float32)).astype(np.float16)
+    bh = b.astype(np.float16)
+    bl = (b - bh.astype(np.float32)).astype(np.float16)
+    cross = np.abs(ah.astype(np.float64) * bl.astype(np.float64) + al.astype(np.float64) * bh.astype(np.float64))
+    assert np.all(cross <= 2.0 ** -24 * 2.0 ** 14 * np.abs(b.astype(np.float64)) + 2.0 ** -48)
