@@ -17,7 +17,10 @@ namespace gg {
 
 // Bounding sphere of tile t (points t*128 .. +127, the tile's first point
 // standing in past the end n), computed by one whole warp; every lane gets
-// the centre cf and the widened radius rhof.
+// the centre cf and the widened radius rhof.  A coordinate is converted to
+// fp32 once (round to nearest, within 2^-24 |x| plus a subnormal step of
+// it) and widened outwards by 2^-23 |x| + 2^-126 in fp32, which contains the
+// fp64 value: one conversion on the FP64 pipe instead of two directed ones.
 __device__ __forceinline__ void warp_tile_sphere(const double* __restrict__ pts, int64_t n, int64_t t, int lane,
                                                  float cf[3], float* rhof) {
   float lo[3], hi[3];
@@ -25,8 +28,9 @@ __device__ __forceinline__ void warp_tile_sphere(const double* __restrict__ pts,
     const int64_t p = t * kBlockM + k * 32 + lane;
     const int64_t q = p < n ? p : t * kBlockM;
     for (int d = 0; d < 3; ++d) {
-      const double v = pts[3 * q + d];
-      const float l = __double2float_rd(v), h = __double2float_ru(v);
+      const float v = __double2float_rn(pts[3 * q + d]);
+      const float e = __fmaf_ru(fabsf(v), 0x1p-23f, 0x1p-126f);
+      const float l = __fsub_rd(v, e), h = __fadd_ru(v, e);
       lo[d] = k == 0 ? l : fminf(lo[d], l);
       hi[d] = k == 0 ? h : fmaxf(hi[d], h);
     }

@@ -32,16 +32,18 @@ __device__ __forceinline__ uint32_t spread3(uint32_t v) {
 }
 }  // namespace
 
-__global__ void morton_key_kernel(const double* __restrict__ pts, int64_t n, double lox, double loy, double loz,
-                                  double inv_cell, uint32_t* __restrict__ keys, int* __restrict__ idx) {
+// The cell of a coordinate in fp32 (one conversion from fp64 per coordinate:
+// this GPU's FP64 pipe is narrow, and the order is a heuristic, so a point
+// within a few 1e-6 Bohr of a cell boundary may fall on either side).
+__global__ void morton_key_kernel(const double* __restrict__ pts, int64_t n, float lox, float loy, float loz,
+                                  float inv_cell, uint32_t* __restrict__ keys, int* __restrict__ idx) {
   const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  const double lo[3] = {lox, loy, loz};
+  const float lo[3] = {lox, loy, loz};
   uint32_t c[3];
   for (int d = 0; d < 3; ++d) {
-    double q = (pts[3 * p + d] - lo[d]) * inv_cell;
-    q = q < 0.0 ? 0.0 : (q > 1023.0 ? 1023.0 : q);  // NaN-free clamp; far points share edge cells
-    c[d] = static_cast<uint32_t>(q);
+    const float q = (__double2float_rn(pts[3 * p + d]) - lo[d]) * inv_cell;
+    c[d] = static_cast<uint32_t>(fminf(fmaxf(q, 0.f), 1023.f));  // NaN goes to 0; far points share edge cells
   }
   keys[p] = spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
   idx[p] = static_cast<int>(p);
@@ -157,7 +159,8 @@ cudaError_t launch_spatial_order(const double* pts, int64_t n, const double lo[3
                                  uint32_t* keys_sorted, int* idx, int* perm, void* temp, size_t temp_bytes,
                                  double* pts_sorted, cudaStream_t st) {
   const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
-  morton_key_kernel<<<blocks, 256, 0, st>>>(pts, n, lo[0], lo[1], lo[2], 1.0 / cell, keys, idx);
+  morton_key_kernel<<<blocks, 256, 0, st>>>(pts, n, static_cast<float>(lo[0]), static_cast<float>(lo[1]),
+                                            static_cast<float>(lo[2]), static_cast<float>(1.0 / cell), keys, idx);
   cudaError_t e = cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys_sorted, idx, perm, static_cast<int>(n),
                                                   0, 30, st);
   if (e != cudaSuccess) return e;

@@ -92,11 +92,20 @@ def _ru(x):
     return np.nextafter(f, f32(np.inf)) if float(f) < x else f
 
 
+def _outward(x):
+    """A coordinate converted to fp32 once (to nearest) and widened by
+    2^-23 |v| + 2^-126 with directed roundings, as warp_tile_sphere does."""
+    v = f32(x)
+    e = _ru(abs(float(v)) * 2.0 ** -23 + 2.0 ** -126)
+    return _rd(float(v) - float(e)), _ru(float(v) + float(e))
+
+
 def _tile_sphere(pts):
-    """warp_tile_sphere: the box from outward-rounded fp32 coordinates, its
+    """warp_tile_sphere: the box from outward-widened fp32 coordinates, its
     centre and the radius widened against the centre's rounding."""
-    lo = [min(_rd(v) for v in pts[:, d]) for d in range(3)]
-    hi = [max(_ru(v) for v in pts[:, d]) for d in range(3)]
+    ends = [[_outward(v) for v in pts[:, d]] for d in range(3)]
+    lo = [min(a for a, _ in ends[d]) for d in range(3)]
+    hi = [max(b for _, b in ends[d]) for d in range(3)]
     cf, rho2, cmax = [], f32(0.0), f32(0.0)
     for d in range(3):
         cf.append(f32(f32(0.5) * f32(lo[d] + hi[d])))
