@@ -49,14 +49,32 @@ __global__ void morton_key_kernel(const double* __restrict__ pts, int64_t n, flo
   idx[p] = static_cast<int>(p);
 }
 
+// Four points per thread: the four indices in one load, then twelve
+// independent coordinate loads in flight (the loads through perm are a
+// latency chain), and the 96 contiguous output bytes in six 16-byte stores.
 __global__ void gather_kernel(const double* __restrict__ pts, const int* __restrict__ perm, int64_t n,
                               double* __restrict__ out) {
-  const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const int64_t s = perm[p];
-  out[3 * p] = pts[3 * s];
-  out[3 * p + 1] = pts[3 * s + 1];
-  out[3 * p + 2] = pts[3 * s + 2];
+  const int64_t p0 = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) * 4;
+  if (p0 >= n) return;
+  if (p0 + 4 <= n) {
+    const int4 s = *reinterpret_cast<const int4*>(perm + p0);  // perm is 16-byte aligned, p0 a multiple of 4
+    const int64_t src[4] = {s.x, s.y, s.z, s.w};
+    double v[12];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[3 * k + c] = pts[3 * src[k] + c];
+    double2* o = reinterpret_cast<double2*>(out + 3 * p0);  // 96 p0 / 4 bytes: 16-byte aligned
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o[k] = make_double2(v[2 * k], v[2 * k + 1]);
+  } else {
+    for (int64_t p = p0; p < n; ++p) {
+      const int64_t s = perm[p];
+      out[3 * p] = pts[3 * s];
+      out[3 * p + 1] = pts[3 * s + 1];
+      out[3 * p + 2] = pts[3 * s + 2];
+    }
+  }
 }
 
 // One warp per tile, four tiles per block of 128 threads: the tile's
@@ -164,7 +182,7 @@ cudaError_t launch_spatial_order(const double* pts, int64_t n, const double lo[3
   cudaError_t e = cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys_sorted, idx, perm, static_cast<int>(n),
                                                   0, 30, st);
   if (e != cudaSuccess) return e;
-  gather_kernel<<<blocks, 256, 0, st>>>(pts, perm, n, pts_sorted);
+  gather_kernel<<<static_cast<unsigned>((n + 1023) / 1024), 256, 0, st>>>(pts, perm, n, pts_sorted);
   return cudaGetLastError();
 }
 
